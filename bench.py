@@ -1,0 +1,308 @@
+#!/usr/bin/env python
+"""Benchmark: interpolated-edge validation (FK + sphere collision) on one GB300.
+
+Workload: 65,536 random edges of an 8-DOF arm (prismatic torso 0-0.4 m + 7 revolute
+joints, 110 link spheres) in a scene of 256 spheres, 64 oriented boxes and 16
+cylinders, interpolated at 0.01 rad maximum joint step; output per edge: collision
+flag and first-collision state index.  Synthetic, seeded inputs (no dataset).
+
+Metric: FK+collision checks/s, where the checks of a batch are the interpolated
+states the reference's checkMotions validates for it (every state of every edge).
+`value` is measured on device-resident inputs; `e2e` goes through the same C-ABI
+call with host buffers (H2D of the edge endpoints and D2H of the results inside the
+timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbmp|reference]
+
+N > 1 runs under torchrun: every rank validates its own 65,536 edges (weak scaling,
+no collective on the data path); the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "FK+collision checks/s"
+UNIT = "checks/s"
+WORKLOAD = "edge_validation_8dof_65536_edges"
+STEP = 0.01
+RULE = 1              # L-infinity: at most 0.01 rad per joint between consecutive states
+CPU_SAMPLE_EDGES = 96
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
+    ap.add_argument("--edges", type=int, default=65536)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def run_reference(args):
+    """CPU arm: the reference algorithm (every interpolated state, every pair, cost mode)
+    restated by the oracle, on all host cores, over a bounded sample per step."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle as O
+    from isaac_sim_ros2_humble_gb300 import workloads as W
+    robot, env, qf, qt = W.edge_workload(n_edges=args.edges)
+    m = O.OracleModel(robot, env)
+    per = 32
+    cores = O.num_threads()
+    times, checks = [], []
+    for it in range(args.warmup + args.steps):
+        lo = (it * per) % (len(qf) - per)
+        t0 = time.perf_counter()
+        ok, fh, ns, ln = m.check_motions(qf[lo:lo + per], qt[lo:lo + per], STEP, RULE, early_exit=False)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            checks.append(int(ns.sum()))
+    value = sum(checks) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "edges_per_step": per, "step_rule": "linf", "resolution": STEP,
+                       "l2_flush": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{per} edges per step of the 65,536-edge batch, reference algorithm "
+                                       f"(all states, all pairs, cost mode), OpenMP"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline(robot, env, qf, qt):
+    import oracle as O
+    m = O.OracleModel(robot, env)
+    n = CPU_SAMPLE_EDGES
+    m.check_motions(qf[:4], qt[:4], STEP, RULE, early_exit=False)
+    t0 = time.perf_counter()
+    ok, fh, ns, ln = m.check_motions(qf[:n], qt[:n], STEP, RULE, early_exit=False)
+    dt = time.perf_counter() - t0
+    return {"value": float(ns.sum()) / dt, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"first {n} of the 65,536 edges ({int(ns.sum())} states), reference algorithm "
+                      f"(all states, all pairs, cost mode), OpenMP, {dt:.1f} s"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+
+    from isaac_sim_ros2_humble_gb300 import _lib, api, roofline, workloads as W
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    robot, env, qf, qt = W.edge_workload(n_edges=args.edges, shard=rank)
+    R, E = api.Robot(robot), api.Env(env)
+    L = robot.num_links
+    n = qf.shape[0]
+    d_from = torch.from_numpy(qf).to(dev)
+    d_to = torch.from_numpy(qt).to(dev)
+    ok = torch.zeros(n, dtype=torch.uint8, device=dev)
+    fh = torch.zeros(n, dtype=torch.int32, device=dev)
+    ln = torch.zeros(n, device=dev)
+    ns = torch.zeros(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(384 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (126 MB)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        api.check_edges(R, E, d_from, d_to, STEP, RULE, ok, fh, ln, ns)
+
+    fp32_peak = _lib.measure_fp32_peak(1.0)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    checks = int(ns.sum().item())
+    units = roofline.edge_units(fh.cpu().numpy(), ns.cpu().numpy())
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clk = ClockSampler(torch.cuda.current_device())
+    _lib.profile_reset()
+    launches0 = _lib.launch_count()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk.start()
+    _lib.profile_enable(True)
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    _lib.profile_enable(False)
+    if ws > 1:
+        dist.barrier()
+    clocks = clk.stop()
+    launches = _lib.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    wave_ms, wave_launches = _lib.profile_read(_lib.PROF_EDGE_WAVE)
+    total_s = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([total_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+        c = torch.tensor([checks], device=dev, dtype=torch.float64)
+        dist.all_reduce(c)
+        all_checks = float(c.item())
+    else:
+        all_checks = float(checks)
+    value = all_checks * args.steps / total_s
+
+    # end-to-end through the same C-ABI call with host buffers
+    h_from = torch.from_numpy(qf).pin_memory()
+    h_to = torch.from_numpy(qt).pin_memory()
+    h_ok = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h_fh = torch.empty(n, dtype=torch.int32).pin_memory()
+    h_ln = torch.empty(n, dtype=torch.float32).pin_memory()
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d_from.copy_(h_from, non_blocking=True)
+        d_to.copy_(h_to, non_blocking=True)
+        step()
+        h_ok.copy_(ok, non_blocking=True)
+        h_fh.copy_(fh, non_blocking=True)
+        h_ln.copy_(ln, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_s = sum(e2e_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = all_checks * args.steps / e2e_s
+
+    if rank == 0:
+        flops_state = roofline.flops_per_state(robot, env, R.P)
+        wave_s_per_step = wave_ms / 1e3 / args.steps
+        achieved = units * flops_state / wave_s_per_step / 1e12 if wave_s_per_step > 0 else None
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "edge_wave_traffic.json")
+        if os.path.exists(tp):
+            try:
+                traffic = json.load(open(tp)).get("bytes_per_launch")
+            except Exception:
+                traffic = None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "edges": n, "dof": robot.dim, "links": L,
+                       "robot_spheres": robot.num_spheres, "self_pairs": R.P,
+                       "obstacles": {"spheres": env.counts[0], "oriented_boxes": env.counts[1],
+                                     "cylinders": env.counts[2]},
+                       "resolution": STEP, "step_rule": "linf", "states_per_step": checks,
+                       "states_needed_per_step": units, "edges_free": int(ok.sum().item()),
+                       "edges_per_s": n * ws * args.steps / total_s,
+                       "l2_flush": "384 MB buffer written between timed steps",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * n * L * 4),
+                    "d2h_bytes_per_step": int(n * (1 + 4 + 4)), "ms_per_step": 1e3 * e2e_s / args.steps},
+            "roofline": {"bound": "fp32", "kernel": "k_edge_wave", "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": (achieved / fp32_peak) if achieved and fp32_peak else None,
+                         "traffic": traffic,
+                         "peak_source": "measured FP32 FMA throughput (gbmp_measure_fp32_peak) on this GPU; "
+                                        "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
+                         "nominal_peak": roofline.nominal_fp32_tflops(),
+                         "flops_per_state": flops_state, "units_per_step": units,
+                         "kernel_ms_per_step": wave_ms / args.steps,
+                         "kernel_launches_per_step": wave_launches / args.steps},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(robot, env, qf, qt)
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,202 @@
+/*
+ * gbmp.h -- C-ABI of the GB300 motion-planning hot path (libgbmp.so).
+ *
+ * Plain C types only: opaque handles, pointers and sizes.  Every function
+ * returns a gbmp_status; nothing throws across the boundary and nothing calls
+ * exit().  gbmp_last_error() returns a message for the calling thread's last
+ * failure.
+ *
+ * Memory: every array argument named d_* is DEVICE memory (cudaMalloc'd, or a
+ * torch CUDA tensor's data pointer); every h_* argument is HOST memory.  Arrays
+ * of joint values are row-major [n x L] "full" vectors with one entry per link
+ * (fixed joints included), the layout of the reference's SingleArmStates
+ * (cudampl/CUDAMPLib/src/states/SingleArmStates.cu:435).
+ *
+ * Streams: `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ * stream).  Calls are stream-ordered and asynchronous unless documented
+ * otherwise.  Handles may be used from several threads if each thread uses its
+ * own stream; a handle must outlive the work queued with it.
+ */
+#ifndef GBMP_H
+#define GBMP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define GBMP_API __declspec(dllexport)
+#else
+#define GBMP_API __attribute__((visibility("default")))
+#endif
+
+#define GBMP_VERSION_MAJOR 0
+#define GBMP_VERSION_MINOR 1
+
+typedef int32_t gbmp_status;
+enum {
+    GBMP_OK = 0,
+    GBMP_ERR_INVALID_ARGUMENT = 1, /* reference: std::runtime_error (SingleArmSpace.cu:65-77, :657-664) */
+    GBMP_ERR_OUT_OF_MEMORY = 2,    /* reference: isValid()=false / nullptr (base/States.h:39-52)        */
+    GBMP_ERR_CUDA = 3,
+    GBMP_ERR_CODEGEN = 4,          /* runtime FK code generation / NVRTC failure                         */
+    GBMP_ERR_CAPACITY = 5,         /* a table does not fit the kernel limits (see gbmp_limits)           */
+    GBMP_ERR_TIMEOUT = 6,          /* a device-side wait or iteration cap gave up                        */
+    GBMP_ERR_NOT_SOLVED = 7,       /* planner finished without a path                                    */
+    GBMP_ERR_UNSUPPORTED = 8
+};
+
+/* Joint types, cudampl/CUDAMPLib/include/states/SingleArmStates.h:190-195. */
+#define GBMP_JOINT_REVOLUTE 1
+#define GBMP_JOINT_PRISMATIC 2
+#define GBMP_JOINT_FIXED 5
+
+typedef struct gbmp_robot_s *gbmp_robot;
+typedef struct gbmp_env_s *gbmp_env;
+
+/* Kinematic tree and collision-sphere model.  Same tables as the constructor of
+ * CUDAMPLib::SingleArmSpace (cudampl/CUDAMPLib/include/spaces/SingleArmSpace.h:24-40)
+ * and CPRRTC::RobotSolver (cudampl/CPRRTC/include/RobotSolver.h:84-101), filled by
+ * RobotInfo (src/foliation_planner/include/foliation_planner/robot_info.hpp:13-220). */
+typedef struct gbmp_robot_desc {
+    int32_t num_links;              /* L: links == joints; joint i drives link i          */
+    const int32_t *joint_types;     /* [L]                                                 */
+    const float *joint_poses;       /* [L*16] row-major 4x4 joint origin in parent frame  */
+    const float *joint_axes;        /* [L*3]                                              */
+    const int32_t *parent;          /* [L] parent[i] < i; parent[0] < 0                   */
+    int32_t num_spheres;            /* S                                                   */
+    const int32_t *sphere_link;     /* [S]                                                 */
+    const float *sphere_pos;        /* [S*3] centre in the link frame                      */
+    const float *sphere_radius;     /* [S]                                                 */
+    const uint8_t *active_joints;   /* [L] 1 = planning joint                              */
+    const float *lower;             /* [L]                                                 */
+    const float *upper;             /* [L]                                                 */
+    const float *default_values;    /* [L] value of inactive joints                        */
+    const uint8_t *self_enables;    /* [L*L] link-pair self-collision mask, NULL = all     */
+    float resolution;               /* edge interpolation step (SingleArmSpace.h:39)       */
+} gbmp_robot_desc;
+
+/* Robot flags. */
+#define GBMP_ROBOT_GENERIC 0x0      /* table-driven kernels compiled ahead of time         */
+#define GBMP_ROBOT_CODEGEN 0x1      /* also generate + NVRTC-compile robot-specific kernels */
+
+typedef struct gbmp_limits {
+    int32_t max_links;
+    int32_t max_spheres;
+    int32_t max_self_pairs;
+    int32_t max_env_words;          /* float4 words of an environment kept in shared memory */
+} gbmp_limits;
+
+GBMP_API const char *gbmp_last_error(void);
+GBMP_API const char *gbmp_status_string(gbmp_status s);
+GBMP_API gbmp_status gbmp_get_limits(gbmp_limits *out);
+GBMP_API gbmp_status gbmp_device_count(int32_t *count);
+
+/* Replaces SingleArmSpace::SingleArmSpace (SingleArmSpace.cu:10-161): validates the
+ * tree (parent[i] < i, :63-69), uploads the tables, builds the self-collision pair
+ * list (SelfCollisionConstraint.cu:28-38) and, with GBMP_ROBOT_CODEGEN, generates
+ * and compiles the robot-specific kernels (replacing KernelGenerator.h:222-406 +
+ * NvrtcUtil.h:58-148).  Synchronous. */
+GBMP_API gbmp_status gbmp_robot_create(const gbmp_robot_desc *desc, int32_t flags, gbmp_robot *out);
+GBMP_API gbmp_status gbmp_robot_destroy(gbmp_robot robot);
+GBMP_API gbmp_status gbmp_robot_info(gbmp_robot robot, int32_t *num_links, int32_t *num_spheres,
+                            int32_t *num_self_pairs, int32_t *dim, int32_t *codegen_active);
+/* Host copy of the self-collision pair list: h_pairs [2*P] (i, j), h_thr_sq [P]. */
+GBMP_API gbmp_status gbmp_robot_self_pairs(gbmp_robot robot, int32_t *h_pairs, float *h_thr_sq, int32_t cap);
+/* Select the kernel family used by later calls: 0 table-driven, 1 generated. */
+GBMP_API gbmp_status gbmp_robot_use_codegen(gbmp_robot robot, int32_t enable);
+
+/* Replaces the constructors of EnvConstraintSphere (EnvConstraintSphere.h:21-25),
+ * EnvConstraintCuboid (EnvConstraintCuboid.h:23-29; pos[3], row-major rotation[9],
+ * min[3], max[3] in the box frame) and EnvConstraintCylinder (EnvConstraintCylinder.h:23-29;
+ * pos, rotation, radius, full height along local z).  Any count may be 0.  Synchronous. */
+GBMP_API gbmp_status gbmp_env_create(int32_t n_spheres, const float *h_sphere_pos, const float *h_sphere_radius,
+                            int32_t n_cuboids, const float *h_cuboid_pos, const float *h_cuboid_rot,
+                            const float *h_cuboid_min, const float *h_cuboid_max,
+                            int32_t n_cylinders, const float *h_cyl_pos, const float *h_cyl_rot,
+                            const float *h_cyl_radius, const float *h_cyl_height, gbmp_env *out);
+GBMP_API gbmp_status gbmp_env_destroy(gbmp_env env);
+GBMP_API gbmp_status gbmp_env_counts(gbmp_env env, int32_t *n_spheres, int32_t *n_cuboids, int32_t *n_cylinders);
+
+/* Forward kinematics, replacing SingleArmStates::update (SingleArmStates.cu:696-723:
+ * generated FK kernel KernelGenerator.h:353-403 + sphere transform :340-393).
+ * d_q [n*L]; d_poses [n*L*16] row-major 4x4 or NULL; d_centers [n*S*3] or NULL. */
+GBMP_API gbmp_status gbmp_fk(gbmp_robot robot, const float *d_q, int64_t n, float *d_poses,
+                    float *d_centers, void *stream);
+
+/* Collision check of n states, replacing SingleArmSpace::checkStates
+ * (SingleArmSpace.cu:1572-1602) with the four collision constraints
+ * (SelfCollisionConstraint.cu:60-133, EnvConstraintSphere.cu:35-117,
+ * EnvConstraintCuboid.cu:84-171, EnvConstraintCylinder.cu:107-196) and
+ * calculateTotalCosts (base/States.cu:5-21).
+ * mode GBMP_CHECK_VERDICT: d_verdict[n] = 1 if the state collides (any-hit, early exit).
+ * mode GBMP_CHECK_COST: also d_costs[4*n] (SoA slots: 0 self, 1 spheres, 2 cuboids,
+ * 3 cylinders; NULL allowed) and d_total[n] (NULL allowed); verdict = total != 0. */
+#define GBMP_CHECK_VERDICT 0
+#define GBMP_CHECK_COST 1
+GBMP_API gbmp_status gbmp_check_states(gbmp_robot robot, gbmp_env env, const float *d_q, int64_t n,
+                              int32_t mode, uint8_t *d_verdict, float *d_costs, float *d_total,
+                              void *stream);
+
+/* Edge validation, replacing SingleArmSpace::checkMotions / checkUnconstrainedMotions
+ * (SingleArmSpace.cu:628-848; step rule KernelGenerator.h:408-465, interpolation
+ * :467-522, feasibility SingleArmSpace.cu:603-626).  Edge k runs from d_from[k] to
+ * d_to[k] ([E*L] each).  States are generated on the fly, never materialised.
+ * Outputs (device, any may be NULL): d_ok[E] 1 = collision-free; d_first_hit[E] lowest
+ * colliding state index or -1; d_length[E] L2 length (the reference's motion cost);
+ * d_num_steps[E] interpolated state count.  step_rule GBMP_STEP_L2 is the reference
+ * rule; GBMP_STEP_LINF bounds the per-joint step by `resolution` instead.
+ * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read). */
+#define GBMP_STEP_L2 0
+#define GBMP_STEP_LINF 1
+GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const float *d_from, const float *d_to,
+                             int64_t n_edges, float resolution, int32_t step_rule, uint8_t *d_ok,
+                             int32_t *d_first_hit, float *d_length, int32_t *d_num_steps, void *stream);
+
+/* Nearest neighbour, replacing SingleArmStateManager::find_the_nearest_neighbors
+ * (SingleArmStates.cu:1265-1431).  d_tree [M*L]; candidate indices d_cand [n_cand]
+ * (NULL = all M nodes); d_queries [Q*L]; d_out [Q] index of the nearest candidate by
+ * L2 distance over the robot's active joints; exact ties go to the lowest candidate
+ * position. */
+GBMP_API gbmp_status gbmp_nearest(gbmp_robot robot, const float *d_tree, int64_t M, const int32_t *d_cand,
+                         int64_t n_cand, const float *d_queries, int64_t Q, int32_t *d_out, void *stream);
+
+/* Steer, replacing SingleArmStateManager::interpolateToStates (SingleArmStates.cu:1488-1557)
+ * and SingleArmSpace::interpolate (SingleArmSpace.cu:219-249, :1368-1409): d_to[k] is moved
+ * onto the segment from d_tree[d_idx[k]] (or d_from[k] when d_idx is NULL) so that its L2
+ * distance is at most max_distance.  In place on d_to [n*L]. */
+GBMP_API gbmp_status gbmp_steer(gbmp_robot robot, const float *d_from, const int32_t *d_idx, float *d_to,
+                       int64_t n, float max_distance, void *stream);
+
+/* Uniform samples within the joint limits, inactive joints at their defaults, replacing
+ * SingleArmSpace::sample / sampleConfigurations (SingleArmSpace.cu:184-217, :251-403).
+ * Counter-based Philox4x32-10: sample k, joint j uses counter (offset + k, j) and key seed,
+ * so the stream is reproducible independent of the launch shape.  d_q [n*L]. */
+GBMP_API gbmp_status gbmp_sample(gbmp_robot robot, uint64_t seed, uint64_t offset, int64_t n, float *d_q,
+                        void *stream);
+
+/* ---- instrumentation ----
+ * With profiling enabled, CUDA events are recorded on the launching stream around
+ * every launch of the named kernel families; gbmp_profile_read() waits for them and
+ * returns the accumulated device time and launch count.  gbmp_launch_count() counts
+ * every kernel launch made by the library since load. */
+#define GBMP_PROF_EDGE_WAVE 0
+#define GBMP_PROF_CHECK_STATES 1
+#define GBMP_PROF_FK 2
+#define GBMP_PROF_OTHER 3
+GBMP_API gbmp_status gbmp_profile_enable(int32_t enable);
+GBMP_API gbmp_status gbmp_profile_reset(void);
+GBMP_API gbmp_status gbmp_profile_read(int32_t family, double *ms, int64_t *launches);
+GBMP_API gbmp_status gbmp_launch_count(int64_t *count);
+
+/* FP32 fused-multiply-add throughput of the current device, measured with a
+ * register-resident FMA loop over `seconds` of wall time (the CUDA-core roofline
+ * denominator for the FK + collision kernels).  Synchronous. */
+GBMP_API gbmp_status gbmp_measure_fp32_peak(double seconds, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBMP_H */

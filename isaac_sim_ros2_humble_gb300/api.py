@@ -1,0 +1,139 @@
+"""Python handles over the libgbmp C-ABI.
+
+`Robot` and `Env` own the C handles; the operations take torch CUDA tensors
+(device memory) and launch on the current torch stream.  Every call goes through
+libgbmp.so; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ptr, stream_handle
+from .workloads import Environment, RobotModel
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class Robot:
+    """A robot model resident on the device (replaces the SingleArmSpace tables)."""
+
+    def __init__(self, model: RobotModel, codegen: bool = False):
+        lib = _lib.load()
+        self.model = model
+        keep = [_c(model.joint_types, np.int32), _c(model.joint_poses.reshape(-1, 16), np.float32),
+                _c(model.joint_axes, np.float32), _c(model.parent, np.int32),
+                _c(model.sphere_link, np.int32), _c(model.sphere_pos, np.float32),
+                _c(model.sphere_r, np.float32), _c(model.active, np.uint8), _c(model.lower, np.float32),
+                _c(model.upper, np.float32), _c(model.default, np.float32), _c(model.enables, np.uint8)]
+        d = _lib.RobotDesc(model.num_links, *(k.ctypes.data for k in keep[:4]), model.num_spheres,
+                           *(k.ctypes.data for k in keep[4:]), float(model.resolution))
+        h = C.c_void_p()
+        check(lib.gbmp_robot_create(C.byref(d), _lib.ROBOT_CODEGEN if codegen else _lib.ROBOT_GENERIC,
+                                    C.byref(h)))
+        self.handle = h
+        L, S, P, dim, cg = (C.c_int32() for _ in range(5))
+        check(lib.gbmp_robot_info(h, C.byref(L), C.byref(S), C.byref(P), C.byref(dim), C.byref(cg)))
+        self.L, self.S, self.P, self.dim = L.value, S.value, P.value, dim.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().gbmp_robot_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def self_pairs(self):
+        pairs = np.zeros(2 * max(self.P, 1), np.int32)
+        thr = np.zeros(max(self.P, 1), np.float32)
+        check(_lib.load().gbmp_robot_self_pairs(self.handle, pairs.ctypes.data, thr.ctypes.data, max(self.P, 1)))
+        return pairs[: 2 * self.P].reshape(-1, 2), thr[: self.P]
+
+    def use_codegen(self, enable: bool):
+        check(_lib.load().gbmp_robot_use_codegen(self.handle, int(enable)))
+
+
+class Env:
+    """An obstacle set resident on the device (replaces the EnvConstraint* tables)."""
+
+    def __init__(self, env: Environment):
+        lib = _lib.load()
+        self.env = env
+        ns, nb, nc = env.counts
+        k = [_c(env.sphere_pos, np.float32), _c(env.sphere_r, np.float32), _c(env.box_pos, np.float32),
+             _c(env.box_rot, np.float32), _c(env.box_min, np.float32), _c(env.box_max, np.float32),
+             _c(env.cyl_pos, np.float32), _c(env.cyl_rot, np.float32), _c(env.cyl_radius, np.float32),
+             _c(env.cyl_height, np.float32)]
+        h = C.c_void_p()
+        check(lib.gbmp_env_create(ns, k[0].ctypes.data, k[1].ctypes.data, nb, k[2].ctypes.data,
+                                  k[3].ctypes.data, k[4].ctypes.data, k[5].ctypes.data, nc,
+                                  k[6].ctypes.data, k[7].ctypes.data, k[8].ctypes.data, k[9].ctypes.data,
+                                  C.byref(h)))
+        self.handle = h
+        self.counts = (ns, nb, nc)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().gbmp_env_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _n(q, L):
+    assert q.is_cuda and q.dtype.__str__() == "torch.float32" and q.is_contiguous(), "q must be contiguous CUDA float32"
+    assert q.shape[-1] == L, f"last dim {q.shape[-1]} != L={L}"
+    return q.numel() // L
+
+
+def fk(robot: Robot, q, poses=None, centers=None, stream=None):
+    n = _n(q, robot.L)
+    check(_lib.load().gbmp_fk(robot.handle, ptr(q), n, ptr(poses), ptr(centers), stream_handle(stream)))
+
+
+def check_states(robot: Robot, env: Env, q, verdict=None, costs=None, total=None, mode=_lib.CHECK_VERDICT,
+                 stream=None):
+    n = _n(q, robot.L)
+    check(_lib.load().gbmp_check_states(robot.handle, env.handle, ptr(q), n, mode, ptr(verdict), ptr(costs),
+                                        ptr(total), stream_handle(stream)))
+
+
+def check_edges(robot: Robot, env: Env, q_from, q_to, resolution: float = 0.0, rule: int = _lib.STEP_L2,
+                ok=None, first_hit=None, length=None, num_steps=None, stream=None):
+    n = _n(q_from, robot.L)
+    assert q_to.shape == q_from.shape
+    check(_lib.load().gbmp_check_edges(robot.handle, env.handle, ptr(q_from), ptr(q_to), n, float(resolution),
+                                       rule, ptr(ok), ptr(first_hit), ptr(length), ptr(num_steps),
+                                       stream_handle(stream)))
+
+
+def nearest(robot: Robot, tree, queries, out, cand=None, stream=None):
+    M = _n(tree, robot.L)
+    Q = _n(queries, robot.L)
+    nc = cand.numel() if cand is not None else 0
+    check(_lib.load().gbmp_nearest(robot.handle, ptr(tree), M, ptr(cand), nc, ptr(queries), Q, ptr(out),
+                                   stream_handle(stream)))
+
+
+def steer(robot: Robot, q_from, q_to, max_distance: float, idx=None, stream=None):
+    n = _n(q_to, robot.L)
+    check(_lib.load().gbmp_steer(robot.handle, ptr(q_from), ptr(idx), ptr(q_to), n, float(max_distance),
+                                 stream_handle(stream)))
+
+
+def sample(robot: Robot, seed: int, offset: int, out, stream=None):
+    n = _n(out, robot.L)
+    check(_lib.load().gbmp_sample(robot.handle, seed, offset, n, ptr(out), stream_handle(stream)))

@@ -1,0 +1,642 @@
+// gbmp_core.cu -- robot / environment handles, FK, state checks and edge
+// validation kernels of libgbmp, and their C-ABI entry points.
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "gbmp_internal.h"
+
+namespace gbmp {
+
+static thread_local std::string g_err;
+
+void set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+// ---------------------------------------------------------------------------------
+// Launch helpers.
+// ---------------------------------------------------------------------------------
+static size_t block_smem(const DevRobot &R, int nwords) {
+    return smem_tables_bytes(R.L, R.S, nwords) + smem_warp_bytes(R.L, R.S) * kWarpsPerBlock;
+}
+
+template <typename K>
+static gbmp_status persistent_grid(K kernel, size_t smem, int num_sms, int *grid) {
+    static thread_local const void *configured[64];
+    static thread_local int n_configured = 0;
+    bool seen = false;
+    for (int i = 0; i < n_configured; ++i) seen |= configured[i] == (const void *)kernel;
+    if (!seen) {
+        GBMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        if (n_configured < 64) configured[n_configured++] = (const void *)kernel;
+    }
+    int per_sm = 0;
+    GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerBlock * kWarp, smem));
+    if (per_sm < 1) {
+        set_error("kernel does not fit on an SM (%zu bytes of shared memory)", smem);
+        return GBMP_ERR_CAPACITY;
+    }
+    *grid = per_sm * num_sms;
+    return GBMP_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Kernels.
+// ---------------------------------------------------------------------------------
+
+// FK (+ sphere centres) of n states; one warp per state.
+__global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
+    k_fk(DevRobot R, const float *__restrict__ q, long long n, float *__restrict__ poses,
+         float *__restrict__ centers) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    DevEnv E{0, 0, 0, nullptr};
+    SmemTables t = carve_tables(smem, R.L, R.S, 0);
+    stage_tables(R, E, t, 0);
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R.L, R.S, 0), R.L, R.S, threadIdx.x / kWarp);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
+    for (long long s = blockIdx.x * (long long)kWarpsPerBlock + threadIdx.x / kWarp; s < n; s += nw) {
+        for (int j = lane; j < R.L; j += kWarp) w.q[j] = q[s * R.L + j];
+        __syncwarp();
+        warp_fk(t, R.L, w, lane);
+        if (poses) {
+            float *P = poses + s * R.L * 16;
+            for (int e = lane; e < R.L * 16; e += kWarp) {
+                const int li = e >> 4, k = e & 15;
+                P[e] = k < 12 ? w.lp[12 * li + k] : (k == 15 ? 1.f : 0.f);
+            }
+        }
+        if (centers) {
+            float *C = centers + s * R.S * 3;
+            for (int k = lane; k < R.S; k += kWarp) {
+                const float4 sp = t.sph[k];
+                const float3 p = xform_point(w.lp + 12 * t.slink[k], sp.x, sp.y, sp.z);
+                C[3 * k] = p.x; C[3 * k + 1] = p.y; C[3 * k + 2] = p.z;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Collision check of n states; one warp per state.
+template <bool COST>
+__global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
+    k_check_states(DevRobot R, DevEnv E, const float *__restrict__ q, long long n,
+                   unsigned char *__restrict__ verdict, float *__restrict__ costs, float *__restrict__ total) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nwords = env_words(E.ns, E.nb, E.nc);
+    SmemTables t = carve_tables(smem, R.L, R.S, nwords);
+    stage_tables(R, E, t, nwords);
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R.L, R.S, nwords), R.L, R.S, threadIdx.x / kWarp);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
+    for (long long s = blockIdx.x * (long long)kWarpsPerBlock + threadIdx.x / kWarp; s < n; s += nw) {
+        for (int j = lane; j < R.L; j += kWarp) w.q[j] = q[s * R.L + j];
+        __syncwarp();
+        warp_fk(t, R.L, w, lane);
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        const bool hit = warp_collide_dispatch<COST>(t, R, E, w, lane, c);
+        if (lane == 0) {
+            if (COST) {
+                const float tot = ((c[0] + c[1]) + c[2]) + c[3];
+                if (costs) { costs[s] = c[0]; costs[n + s] = c[1]; costs[2 * n + s] = c[2]; costs[3 * n + s] = c[3]; }
+                if (total) total[s] = tot;
+                if (verdict) verdict[s] = tot != 0.f;
+            } else if (verdict) {
+                verdict[s] = hit;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Edge set-up: step count, direction, L2 length (KernelGenerator.h:433-465); one thread per edge.
+__global__ void k_edge_setup(const float *__restrict__ from, const float *__restrict__ to, long long E, int L,
+                             float res, int rule, int *__restrict__ nsteps, float *__restrict__ dir,
+                             int *__restrict__ first_hit, int *__restrict__ live, int *__restrict__ ctr,
+                             float *__restrict__ length_out, int *__restrict__ nsteps_out) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k == 0) ctr[1] = (int)E;
+    if (k >= E) return;
+    const float *f = from + k * L, *t = to + k * L;
+    float d2 = 0.f, dinf = 0.f;
+    for (int j = 0; j < L; ++j) {
+        const float d = __fadd_rn(f[j], -t[j]);
+        d2 = __fmaf_rn(d, d, d2);
+        dinf = fmaxf(dinf, fabsf(d));
+    }
+    const float len = __fsqrt_rn(d2);
+    const float metric = rule == GBMP_STEP_LINF ? dinf : len;
+    const int n = (int)__fdiv_rn(metric, res) + 1;
+    const float fn = (float)n;
+    for (int j = 0; j < L; ++j) dir[k * L + j] = __fdiv_rn(__fadd_rn(t[j], -f[j]), fn);
+    nsteps[k] = n;
+    first_hit[k] = INT_MAX;
+    live[k] = (int)k;
+    atomicMax(ctr, n);
+    if (length_out) length_out[k] = len;
+    if (nsteps_out) nsteps_out[k] = n;
+}
+
+// One wave of edge validation: states [b0, b1) of every live edge, one warp per state,
+// state-major order so that lower states of an edge are examined first and later ones
+// can skip once a hit is known.
+__global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
+    k_edge_wave(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
+                const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
+                const int *__restrict__ live, const int *__restrict__ live_count, int b0, int b1) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nwords = env_words(E.ns, E.nb, E.nc);
+    SmemTables t = carve_tables(smem, R.L, R.S, nwords);
+    stage_tables(R, E, t, nwords);
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R.L, R.S, nwords), R.L, R.S, threadIdx.x / kWarp);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const long long count = *live_count;
+    const long long tasks = count * (long long)(b1 - b0);
+    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
+    for (long long task = blockIdx.x * (long long)kWarpsPerBlock + threadIdx.x / kWarp; task < tasks;
+         task += nw) {
+        const int s = b0 + (int)(task / count);
+        const int e = live[task % count];
+        const int n = nsteps[e];
+        if (s >= n) continue;
+        // skip once a lower state of this edge is known to collide; the read is
+        // broadcast from lane 0 so that the whole warp takes the same branch
+        int known = 0;
+        if (lane == 0) known = *(volatile int *)(first_hit + e);
+        known = __shfl_sync(kFull, known, 0);
+        if (known < s) continue;
+        for (int j = lane; j < R.L; j += kWarp)
+            w.q[j] = (s == n - 1) ? to[(long long)e * R.L + j]
+                                  : __fmaf_rn(dir[(long long)e * R.L + j], (float)s, from[(long long)e * R.L + j]);
+        __syncwarp();
+        warp_fk(t, R.L, w, lane);
+        const bool hit = warp_collide_dispatch<false>(t, R, E, w, lane, nullptr);
+        if (hit && lane == 0) atomicMin(first_hit + e, s);
+        __syncwarp();
+    }
+}
+
+// Keep edges that have no hit yet and still have states at or beyond b1.
+__global__ void k_edge_compact(const int *__restrict__ live_in, const int *__restrict__ count_in,
+                               const int *__restrict__ first_hit, const int *__restrict__ nsteps, int b1,
+                               int *__restrict__ live_out, int *__restrict__ count_out) {
+    const int count = *count_in;
+    const int lane = threadIdx.x & 31;
+    for (long long base = blockIdx.x * (long long)blockDim.x; base < count; base += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + threadIdx.x;
+        bool keep = false;
+        int e = 0;
+        if (i < count) {
+            e = live_in[i];
+            keep = first_hit[e] == INT_MAX && nsteps[e] > b1;
+        }
+        const unsigned m = __ballot_sync(kFull, keep);
+        int slot = 0;
+        if (lane == 0 && m) slot = atomicAdd(count_out, __popc(m));
+        slot = __shfl_sync(kFull, slot, 0);
+        if (keep) live_out[slot + __popc(m & ((1u << lane) - 1u))] = e;
+    }
+}
+
+__global__ void k_edge_finish(long long E, const int *__restrict__ fh, unsigned char *__restrict__ ok,
+                              int *__restrict__ first_hit_out) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= E) return;
+    const int h = fh[k];
+    if (ok) ok[k] = h == INT_MAX;
+    if (first_hit_out) first_hit_out[k] = h == INT_MAX ? -1 : h;
+}
+
+// ---------------------------------------------------------------------------------
+// Host helpers.
+// ---------------------------------------------------------------------------------
+static void host_unit_axis(const float *a, float *n) {
+    const float len = sqrtf(fmaf(a[2], a[2], fmaf(a[1], a[1], a[0] * a[0])));
+    const float valid = (len >= 1e-12f) ? 1.f : 0.f;
+    const float inv = 1.f / fmaxf(len, 1e-12f);
+    n[0] = a[0] * inv * valid;
+    n[1] = a[1] * inv * valid;
+    n[2] = a[2] * inv * valid;
+    n[3] = valid;
+}
+
+// Inverse pose [R^T | -R^T t] (EnvConstraintCuboid.cu:13-34, EnvConstraintCylinder.cu:17-45).
+static void host_inverse_pose(const float *pos, const float *rot, float4 *rows) {
+    const float t00 = rot[0], t01 = rot[3], t02 = rot[6];
+    const float t10 = rot[1], t11 = rot[4], t12 = rot[7];
+    const float t20 = rot[2], t21 = rot[5], t22 = rot[8];
+    rows[0] = make_float4(t00, t01, t02, -(t00 * pos[0] + t01 * pos[1] + t02 * pos[2]));
+    rows[1] = make_float4(t10, t11, t12, -(t10 * pos[0] + t11 * pos[1] + t12 * pos[2]));
+    rows[2] = make_float4(t20, t21, t22, -(t20 * pos[0] + t21 * pos[1] + t22 * pos[2]));
+}
+
+static int current_device_sms(int *dev) {
+    int d = 0, sms = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d) != cudaSuccess) return 0;
+    *dev = d;
+    return sms;
+}
+
+// Wave boundaries of edge validation: 4, 8, 16, 32 states, then 64 per wave.  Small
+// first waves retire the many edges that collide near their start before longer
+// edges are expanded further.
+static int wave_end(int b) {
+    if (b < 4) return 4;
+    if (b < 12) return 12;
+    if (b < 28) return 28;
+    if (b < 60) return 60;
+    return b + 64;
+}
+
+constexpr int kMaxWaves = 4096;
+
+static int max_edge_states() {
+    int b = 0;
+    for (int w = 0; w < kMaxWaves; ++w) b = wave_end(b);
+    return b;
+}
+
+}  // namespace gbmp
+
+using namespace gbmp;
+
+// ---------------------------------------------------------------------------------
+// C-ABI.
+// ---------------------------------------------------------------------------------
+extern "C" {
+
+const char *gbmp_last_error(void) { return g_err.c_str(); }
+
+const char *gbmp_status_string(gbmp_status s) {
+    switch (s) {
+    case GBMP_OK: return "ok";
+    case GBMP_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GBMP_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case GBMP_ERR_CUDA: return "CUDA error";
+    case GBMP_ERR_CODEGEN: return "code generation failed";
+    case GBMP_ERR_CAPACITY: return "capacity exceeded";
+    case GBMP_ERR_TIMEOUT: return "timed out";
+    case GBMP_ERR_NOT_SOLVED: return "not solved";
+    case GBMP_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+gbmp_status gbmp_get_limits(gbmp_limits *out) {
+    GBMP_CHECK_ARG(out, "out is NULL");
+    out->max_links = kMaxLinks;
+    out->max_spheres = kMaxSpheres;
+    out->max_self_pairs = kMaxSelfPairs;
+    out->max_env_words = kMaxEnvWords;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_device_count(int32_t *count) {
+    GBMP_CHECK_ARG(count, "count is NULL");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        c = 0;
+    }
+    *count = c;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robot *out) {
+    GBMP_CHECK_ARG(d && out, "desc/out is NULL");
+    *out = nullptr;
+    const int L = d->num_links, S = d->num_spheres;
+    GBMP_CHECK_ARG(L >= 1 && L <= kMaxLinks, "num_links %d outside [1, %d]", L, kMaxLinks);
+    GBMP_CHECK_ARG(S >= 0 && S <= kMaxSpheres, "num_spheres %d outside [0, %d]", S, kMaxSpheres);
+    GBMP_CHECK_ARG(d->joint_types && d->joint_poses && d->joint_axes && d->parent, "kinematic table is NULL");
+    GBMP_CHECK_ARG(d->active_joints && d->lower && d->upper && d->default_values, "joint table is NULL");
+    GBMP_CHECK_ARG(S == 0 || (d->sphere_link && d->sphere_pos && d->sphere_radius), "sphere table is NULL");
+    GBMP_CHECK_ARG(d->resolution > 0.f && std::isfinite(d->resolution), "resolution must be > 0");
+    // SingleArmSpace.cu:63-69: every parent index must be smaller than its link index.
+    for (int i = 0; i < L; ++i) {
+        GBMP_CHECK_ARG(d->parent[i] < i, "Link parent link map is not valid at index %d. Value: %d", i, d->parent[i]);
+        GBMP_CHECK_ARG(i == 0 || d->parent[i] >= 0, "link %d has no parent", i);
+    }
+    for (int k = 0; k < S; ++k)
+        GBMP_CHECK_ARG(d->sphere_link[k] >= 0 && d->sphere_link[k] < L, "sphere %d attached to link %d", k,
+                       d->sphere_link[k]);
+
+    auto *r = new gbmp_robot_s();
+    r->L = L;
+    r->S = S;
+    r->resolution = d->resolution;
+    r->type.assign(d->joint_types, d->joint_types + L);
+    r->parent.assign(d->parent, d->parent + L);
+    r->pose16.assign(d->joint_poses, d->joint_poses + 16 * L);
+    r->axis.assign(d->joint_axes, d->joint_axes + 3 * L);
+    r->active.assign(d->active_joints, d->active_joints + L);
+    r->lower.assign(d->lower, d->lower + L);
+    r->upper.assign(d->upper, d->upper + L);
+    r->defv.assign(d->default_values, d->default_values + L);
+    if (S) {
+        r->slink.assign(d->sphere_link, d->sphere_link + S);
+        r->sph_pos.assign(d->sphere_pos, d->sphere_pos + 3 * S);
+        r->sph_r.assign(d->sphere_radius, d->sphere_radius + S);
+    }
+    if (d->self_enables) r->enables.assign(d->self_enables, d->self_enables + L * L);
+    r->dim = 0;
+    for (int i = 0; i < L; ++i) r->dim += r->active[i] != 0;
+    // Self-collision pair list, SelfCollisionConstraint.cu:28-38.
+    for (int i = 0; i < S; ++i)
+        for (int j = i + 1; j < S; ++j) {
+            const int li = r->slink[i], lj = r->slink[j];
+            if (li == lj) continue;
+            if (!r->enables.empty() && !r->enables[li * L + lj]) continue;
+            r->pairs.push_back(i);
+            r->pairs.push_back(j);
+            const float s = r->sph_r[i] + r->sph_r[j];
+            r->thr.push_back(s * s);
+        }
+    r->P = (int)r->thr.size();
+    if (r->P > kMaxSelfPairs) {
+        delete r;
+        set_error("%d self-collision pairs exceed the limit %d", (int)r->thr.size(), kMaxSelfPairs);
+        return GBMP_ERR_CAPACITY;
+    }
+
+    // Pack the device tables.
+    std::vector<unsigned char> blob;
+    auto put = [&](const void *src, size_t bytes) {
+        size_t off = align16(blob.size());
+        blob.resize(off + align16(bytes ? bytes : 1), 0);
+        if (bytes) memcpy(blob.data() + off, src, bytes);
+        return off;
+    };
+    std::vector<float> jl(12 * L), axn(4 * L), axr(4 * L), sph(4 * (S ? S : 1));
+    for (int i = 0; i < L; ++i) {
+        for (int k = 0; k < 12; ++k) jl[12 * i + k] = r->pose16[16 * i + k];
+        host_unit_axis(&r->axis[3 * i], &axn[4 * i]);
+        axr[4 * i] = r->axis[3 * i]; axr[4 * i + 1] = r->axis[3 * i + 1]; axr[4 * i + 2] = r->axis[3 * i + 2];
+        axr[4 * i + 3] = 0.f;
+    }
+    for (int k = 0; k < S; ++k) {
+        sph[4 * k] = r->sph_pos[3 * k]; sph[4 * k + 1] = r->sph_pos[3 * k + 1];
+        sph[4 * k + 2] = r->sph_pos[3 * k + 2]; sph[4 * k + 3] = r->sph_r[k];
+    }
+    std::vector<unsigned> packed(r->P);
+    for (int p = 0; p < r->P; ++p) packed[p] = (unsigned)r->pairs[2 * p] | ((unsigned)r->pairs[2 * p + 1] << 16);
+    size_t o_jl = put(jl.data(), jl.size() * 4), o_axn = put(axn.data(), axn.size() * 4);
+    size_t o_axr = put(axr.data(), axr.size() * 4), o_sph = put(sph.data(), 4 * 4 * (size_t)S);
+    size_t o_type = put(r->type.data(), 4 * L), o_par = put(r->parent.data(), 4 * L);
+    size_t o_sl = put(r->slink.data(), 4 * (size_t)S);
+    size_t o_pairs = put(packed.data(), 4 * (size_t)r->P), o_thr = put(r->thr.data(), 4 * (size_t)r->P);
+    size_t o_lo = put(r->lower.data(), 4 * L), o_up = put(r->upper.data(), 4 * L);
+    size_t o_def = put(r->defv.data(), 4 * L), o_act = put(r->active.data(), L);
+
+    int dev = 0;
+    r->num_sms = current_device_sms(&dev);
+    r->device = dev;
+    if (r->num_sms <= 0) {
+        delete r;
+        set_error("no CUDA device available");
+        return GBMP_ERR_CUDA;
+    }
+    cudaError_t e = cudaMalloc(&r->d_block, blob.size());
+    if (e == cudaSuccess) e = cudaMemcpy(r->d_block, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_error("uploading robot tables failed: %s", cudaGetErrorString(e));
+        gbmp_robot_destroy(r);
+        return e == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+    }
+    auto *b = static_cast<unsigned char *>(r->d_block);
+    DevRobot &D = r->dev;
+    D.L = L; D.S = S; D.P = r->P; D.spl = S ? (S + kWarp - 1) / kWarp : 1;
+    D.jl = (const float *)(b + o_jl); D.axn = (const float *)(b + o_axn); D.axr = (const float *)(b + o_axr);
+    D.sph = (const float *)(b + o_sph); D.type = (const int *)(b + o_type); D.parent = (const int *)(b + o_par);
+    D.slink = (const int *)(b + o_sl); D.pairs = (const unsigned *)(b + o_pairs); D.thr = (const float *)(b + o_thr);
+    D.lower = (const float *)(b + o_lo); D.upper = (const float *)(b + o_up); D.defv = (const float *)(b + o_def);
+    D.active = (const unsigned char *)(b + o_act);
+    (void)flags;
+    *out = r;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_robot_destroy(gbmp_robot r) {
+    if (!r) return GBMP_OK;
+    if (r->d_block) cudaFree(r->d_block);
+    delete r;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_robot_info(gbmp_robot r, int32_t *L, int32_t *S, int32_t *P, int32_t *dim, int32_t *cg) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    if (L) *L = r->L;
+    if (S) *S = r->S;
+    if (P) *P = r->P;
+    if (dim) *dim = r->dim;
+    if (cg) *cg = r->use_cg ? 1 : 0;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_robot_self_pairs(gbmp_robot r, int32_t *h_pairs, float *h_thr, int32_t cap) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    GBMP_CHECK_ARG(cap >= r->P, "capacity %d < %d pairs", cap, r->P);
+    if (h_pairs) memcpy(h_pairs, r->pairs.data(), sizeof(int32_t) * 2 * r->P);
+    if (h_thr) memcpy(h_thr, r->thr.data(), sizeof(float) * r->P);
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_robot_use_codegen(gbmp_robot r, int32_t enable) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    if (enable && !r->cg) {
+        set_error("robot was created without GBMP_ROBOT_CODEGEN");
+        return GBMP_ERR_UNSUPPORTED;
+    }
+    r->use_cg = enable != 0;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_t nb, const float *bp,
+                            const float *brot, const float *bmin, const float *bmax, int32_t nc, const float *cp,
+                            const float *crot, const float *crad, const float *chei, gbmp_env *out) {
+    GBMP_CHECK_ARG(out, "out is NULL");
+    *out = nullptr;
+    GBMP_CHECK_ARG(ns >= 0 && nb >= 0 && nc >= 0, "negative obstacle count");
+    GBMP_CHECK_ARG(ns == 0 || (sp && sr), "sphere arrays are NULL");
+    GBMP_CHECK_ARG(nb == 0 || (bp && brot && bmin && bmax), "cuboid arrays are NULL");
+    GBMP_CHECK_ARG(nc == 0 || (cp && crot && crad && chei), "cylinder arrays are NULL");
+    const long long words = (long long)ns + 5LL * nb + 4LL * nc;
+    if (words > kMaxEnvWords) {
+        set_error("environment needs %lld float4 words, limit %d", words, kMaxEnvWords);
+        return GBMP_ERR_CAPACITY;
+    }
+    auto *e = new gbmp_env_s();
+    e->ns = ns; e->nb = nb; e->nc = nc;
+    e->h_words.resize(words ? words : 1);
+    float4 *w = e->h_words.data();
+    for (int i = 0; i < ns; ++i) w[i] = make_float4(sp[3 * i], sp[3 * i + 1], sp[3 * i + 2], sr[i]);
+    w += ns;
+    for (int i = 0; i < nb; ++i) {
+        host_inverse_pose(bp + 3 * i, brot + 9 * i, w + 5 * i);
+        w[5 * i + 3] = make_float4(bmin[3 * i], bmin[3 * i + 1], bmin[3 * i + 2], 0.f);
+        w[5 * i + 4] = make_float4(bmax[3 * i], bmax[3 * i + 1], bmax[3 * i + 2], 0.f);
+    }
+    w += 5 * nb;
+    for (int i = 0; i < nc; ++i) {
+        host_inverse_pose(cp + 3 * i, crot + 9 * i, w + 4 * i);
+        w[4 * i + 3] = make_float4(crad[i], chei[i] * 0.5f, 0.f, 0.f);
+    }
+    cudaError_t err = cudaMalloc(&e->d_words, sizeof(float4) * e->h_words.size());
+    if (err == cudaSuccess)
+        err = cudaMemcpy(e->d_words, e->h_words.data(), sizeof(float4) * e->h_words.size(), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+        set_error("uploading environment failed: %s", cudaGetErrorString(err));
+        gbmp_env_destroy(e);
+        return err == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+    }
+    *out = e;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_env_destroy(gbmp_env e) {
+    if (!e) return GBMP_OK;
+    if (e->d_words) cudaFree(e->d_words);
+    delete e;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_env_counts(gbmp_env e, int32_t *ns, int32_t *nb, int32_t *nc) {
+    GBMP_CHECK_ARG(e, "env is NULL");
+    if (ns) *ns = e->ns;
+    if (nb) *nb = e->nb;
+    if (nc) *nc = e->nc;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_fk(gbmp_robot r, const float *d_q, int64_t n, float *d_poses, float *d_centers, void *stream) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    GBMP_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_q, "q is NULL");
+    const size_t smem = smem_tables_bytes(r->L, r->S, 0) + smem_warp_bytes(r->L, r->S) * kWarpsPerBlock;
+    int grid = 0;
+    gbmp_status st = persistent_grid(k_fk, smem, r->num_sms, &grid);
+    if (st) return st;
+    const long long need = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (need < grid) grid = (int)need;
+    ProfScope ps(GBMP_PROF_FK, (cudaStream_t)stream);
+    k_fk<<<grid, kWarpsPerBlock * kWarp, smem, (cudaStream_t)stream>>>(r->dev, d_q, n, d_poses, d_centers);
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int64_t n, int32_t mode,
+                              uint8_t *d_verdict, float *d_costs, float *d_total, void *stream) {
+    GBMP_CHECK_ARG(r && env, "robot/env is NULL");
+    GBMP_CHECK_ARG(n >= 0, "n < 0");
+    GBMP_CHECK_ARG(mode == GBMP_CHECK_VERDICT || mode == GBMP_CHECK_COST, "unknown mode %d", mode);
+    if (n == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_q, "q is NULL");
+    const DevEnv E = env->dev();
+    const size_t smem = block_smem(r->dev, env_words(E.ns, E.nb, E.nc));
+    int grid = 0;
+    gbmp_status st = mode == GBMP_CHECK_COST ? persistent_grid(k_check_states<true>, smem, r->num_sms, &grid)
+                                             : persistent_grid(k_check_states<false>, smem, r->num_sms, &grid);
+    if (st) return st;
+    const long long need = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (need < grid) grid = (int)need;
+    ProfScope ps(GBMP_PROF_CHECK_STATES, (cudaStream_t)stream);
+    if (mode == GBMP_CHECK_COST)
+        k_check_states<true><<<grid, kWarpsPerBlock * kWarp, smem, (cudaStream_t)stream>>>(r->dev, E, d_q, n, d_verdict,
+                                                                                         d_costs, d_total);
+    else
+        k_check_states<false><<<grid, kWarpsPerBlock * kWarp, smem, (cudaStream_t)stream>>>(r->dev, E, d_q, n,
+                                                                                          d_verdict, nullptr, nullptr);
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to, int64_t E,
+                             float res, int32_t rule, uint8_t *d_ok, int32_t *d_first_hit, float *d_length,
+                             int32_t *d_num_steps, void *stream) {
+    GBMP_CHECK_ARG(r && env, "robot/env is NULL");
+    GBMP_CHECK_ARG(E >= 0 && E < INT_MAX, "edge count %lld outside [0, 2^31)", (long long)E);
+    GBMP_CHECK_ARG(rule == GBMP_STEP_L2 || rule == GBMP_STEP_LINF, "unknown step rule %d", rule);
+    if (E == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
+    if (!(res > 0.f)) res = r->resolution;
+    GBMP_CHECK_ARG(std::isfinite(res), "resolution is not finite");
+    cudaStream_t s = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lock(r->scratch_mu);
+    const int L = r->L;
+    // scratch: nsteps[E], first_hit[E], liveA[E], liveB[E], dir[E*L], ctr[kMaxWaves + 2]
+    // (ctr[0] = longest edge, ctr[1 + w] = live edges entering wave w)
+    const size_t eb = align16(sizeof(int) * (size_t)E);
+    const size_t bytes = 4 * eb + align16(sizeof(float) * (size_t)E * L) + (kMaxWaves + 2) * sizeof(int);
+    gbmp_status st = r->scratch.reserve(bytes);
+    if (st) return st;
+    auto *base = static_cast<unsigned char *>(r->scratch.ptr);
+    int *nsteps = (int *)base, *fh = (int *)(base + eb), *liveA = (int *)(base + 2 * eb),
+        *liveB = (int *)(base + 3 * eb);
+    float *dir = (float *)(base + 4 * eb);
+    int *ctr = (int *)(base + 4 * eb + align16(sizeof(float) * (size_t)E * L));
+    GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
+    const int tb = 256;
+    const unsigned blocks = (unsigned)((E + tb - 1) / tb);
+    { ProfScope ps(GBMP_PROF_OTHER, s);
+    k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, fh, liveA, ctr, d_length,
+                                      d_num_steps); }
+    GBMP_CUDA(cudaGetLastError());
+    int n_max = 0;
+    GBMP_CUDA(cudaMemcpyAsync(&n_max, ctr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GBMP_CUDA(cudaStreamSynchronize(s));
+    {
+        int b = 0, waves = 0;
+        while (b < n_max && waves <= kMaxWaves) { b = wave_end(b); ++waves; }
+        if (waves > kMaxWaves) {
+            set_error("an edge has %d interpolated states; at most %d are supported per call", n_max,
+                      max_edge_states());
+            return GBMP_ERR_CAPACITY;
+        }
+    }
+
+    const DevEnv Ev = env->dev();
+    const size_t smem = block_smem(r->dev, env_words(Ev.ns, Ev.nb, Ev.nc));
+    int grid = 0;
+    st = persistent_grid(k_edge_wave, smem, r->num_sms, &grid);
+    if (st) return st;
+    int b0 = 0, wave = 0;
+    int *live_in = liveA, *live_out = liveB;
+    while (b0 < n_max) {
+        const int b1 = wave_end(b0);
+        int *cnt_in = ctr + 1 + wave, *cnt_out = ctr + 2 + wave;
+        {
+            ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
+            k_edge_wave<<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, Ev, d_from, d_to, nsteps, dir, fh,
+                                                                   live_in, cnt_in, b0, b1);
+        }
+        GBMP_CUDA(cudaGetLastError());
+        if (b1 < n_max) {
+            ProfScope ps(GBMP_PROF_OTHER, s);
+            k_edge_compact<<<(unsigned)std::min<long long>(blocks, 4LL * r->num_sms), tb, 0, s>>>(
+                live_in, cnt_in, fh, nsteps, b1, live_out, cnt_out);
+            GBMP_CUDA(cudaGetLastError());
+        }
+        std::swap(live_in, live_out);
+        b0 = b1;
+        ++wave;
+    }
+    { ProfScope ps(GBMP_PROF_OTHER, s);
+    k_edge_finish<<<blocks, tb, 0, s>>>(E, fh, d_ok, d_first_hit); }
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// gbmp_device.cuh -- device-side data layout and the warp-per-state FK + collision
+// routine shared by every kernel of libgbmp.
+//
+// Execution model: one warp validates one joint state.
+//   * FK: lanes 0..11 each own one element of the 3x4 pose of the current link and
+//     walk the chain link by link (KernelGenerator.h:369-400); the poses stay in the
+//     warp's shared-memory scratch, never in HBM unless the caller asks for them.
+//   * Collision: lane l owns robot spheres l, l+32, ... (registers); obstacles are
+//     staged once per block in shared memory and read as broadcasts; self pairs are
+//     strided over the lanes.  Any-hit early exit uses __any_sync.
+// Arithmetic that decides parity with the CPU oracle (matrix products, sphere
+// centres, interpolation) is written with explicit __fmul_rn/__fmaf_rn/__fadd_rn so
+// that FMA contraction cannot change it.
+#pragma once
+
+#include <cstdint>
+
+namespace gbmp {
+
+constexpr int kMaxLinks = 64;
+constexpr int kMaxSpheres = 256;          // 8 spheres per lane
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slots
+
+// ---------------------------------------------------------------------------------
+// Device tables (global memory).  Robot block layout, all 16-byte aligned:
+//   jl    [L*12]  joint origin pose, 3x4 row-major (rows 0..2 of the 4x4)
+//   axn   [L*4]   normalised axis (nx, ny, nz, valid)  (KernelGenerator.h:295-304)
+//   axr   [L*4]   raw axis (prismatic translation uses it unnormalised, :349-354)
+//   sph   [S*4]   sphere (x, y, z, r) in its link frame
+//   type  [L], parent [L], slink [S] (int32)
+//   pairs [P] packed (i | j << 16), thr [P] squared distance thresholds
+// Environment words (float4):
+//   spheres  [ns]     (x, y, z, r)
+//   cuboids  [nb*5]   inverse pose rows 0..2, (min xyz, 0), (max xyz, 0)
+//   cylinders[nc*4]   inverse pose rows 0..2, (radius, half height, 0, 0)
+// ---------------------------------------------------------------------------------
+struct DevRobot {
+    int L, S, P, spl;                 // spl = spheres per lane = ceil(S/32)
+    const float *jl, *axn, *axr, *sph;
+    const int *type, *parent, *slink;
+    const unsigned *pairs;
+    const float *thr;
+    const float *lower, *upper, *defv;
+    const unsigned char *active;
+};
+
+struct DevEnv {
+    int ns, nb, nc;
+    const float4 *words;              // ns + 5*nb + 4*nc float4
+};
+
+__host__ __device__ inline int env_words(int ns, int nb, int nc) { return ns + 5 * nb + 4 * nc; }
+
+// Shared-memory staging of the robot tables and the environment.
+struct SmemTables {
+    float *jl, *axn, *axr;
+    float4 *sph;
+    int *type, *parent, *slink;
+    float4 *env;                      // staged environment words
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+__host__ __device__ inline size_t smem_tables_bytes(int L, int S, int nwords) {
+    size_t b = 0;
+    b += align16(sizeof(float) * 12 * L);
+    b += align16(sizeof(float) * 4 * L) * 2;
+    b += align16(sizeof(float4) * S);
+    b += align16(sizeof(int) * L) * 2;
+    b += align16(sizeof(int) * S);
+    b += align16(sizeof(float4) * nwords);
+    return b;
+}
+
+// Per-warp scratch: link poses [L*12], temp [16], joint state [L], sphere centres [S].
+__host__ __device__ inline size_t smem_warp_bytes(int L, int S) {
+    return align16(sizeof(float) * 12 * L) + align16(sizeof(float) * 16) + align16(sizeof(float) * L) +
+           align16(sizeof(float4) * S);
+}
+
+struct WarpScratch {
+    float *lp;      // link poses
+    float *tmp;     // 12-element temporary
+    float *q;       // joint values of the state under test
+    float4 *cen;    // sphere centres (x, y, z, r)
+};
+
+__device__ inline SmemTables carve_tables(unsigned char *base, int L, int S, int nwords) {
+    SmemTables t;
+    size_t off = 0;
+    t.jl = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 12 * L);
+    t.axn = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 4 * L);
+    t.axr = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 4 * L);
+    t.sph = reinterpret_cast<float4 *>(base + off); off += align16(sizeof(float4) * S);
+    t.type = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * L);
+    t.parent = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * L);
+    t.slink = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * S);
+    t.env = reinterpret_cast<float4 *>(base + off);
+    return t;
+}
+
+__device__ inline WarpScratch carve_warp(unsigned char *base, int L, int S, int warp) {
+    size_t per = smem_warp_bytes(L, S);
+    unsigned char *p = base + per * warp;
+    WarpScratch w;
+    size_t off = 0;
+    w.lp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * L);
+    w.tmp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 16);
+    w.q = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * L);
+    w.cen = reinterpret_cast<float4 *>(p + off);
+    return w;
+}
+
+// Block-cooperative copy of the robot tables and environment into shared memory.
+__device__ inline void stage_tables(const DevRobot &R, const DevEnv &E, const SmemTables &t, int nwords) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < 12 * R.L; i += nt) t.jl[i] = R.jl[i];
+    for (int i = tid; i < 4 * R.L; i += nt) { t.axn[i] = R.axn[i]; t.axr[i] = R.axr[i]; }
+    for (int i = tid; i < R.S; i += nt) {
+        t.sph[i] = reinterpret_cast<const float4 *>(R.sph)[i];
+        t.slink[i] = R.slink[i];
+    }
+    for (int i = tid; i < R.L; i += nt) { t.type[i] = R.type[i]; t.parent[i] = R.parent[i]; }
+    for (int i = tid; i < nwords; i += nt) t.env[i] = E.words[i];
+}
+
+// ---------------------------------------------------------------------------------
+// Forward kinematics (warp-cooperative).  Element e = 4*r + c of a 3x4 product
+// C = A * B with B's implicit last row (0 0 0 1), in the reference's multiply4x4
+// order (KernelGenerator.h:257-280) with its multiply-adds fused.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float mul_elem(const float *A, const float *B, int r, int c) {
+    float acc = __fmul_rn(A[4 * r + 0], B[0 * 4 + c]);
+    acc = __fmaf_rn(A[4 * r + 1], B[1 * 4 + c], acc);
+    acc = __fmaf_rn(A[4 * r + 2], B[2 * 4 + c], acc);
+    if (c == 3) acc = __fadd_rn(acc, A[4 * r + 3]);
+    return acc;
+}
+
+// Rodrigues rotation (KernelGenerator.h:305-325), rows 0..2 of the 4x4 as 3x4.
+__device__ __forceinline__ void rot34(const float *n4, float angle, float *R) {
+    const float nx = n4[0], ny = n4[1], nz = n4[2], valid = n4[3];
+    float s, c;
+    sincosf(angle, &s, &c);
+    const float oc = __fadd_rn(1.f, -c);
+    const float iv = __fadd_rn(1.f, -valid);
+    const float r0 = __fmaf_rn(__fmul_rn(nx, nx), oc, c);
+    const float r1 = __fmaf_rn(__fmul_rn(nx, ny), oc, -__fmul_rn(nz, s));
+    const float r2 = __fmaf_rn(__fmul_rn(nx, nz), oc, __fmul_rn(ny, s));
+    const float r4 = __fmaf_rn(__fmul_rn(ny, nx), oc, __fmul_rn(nz, s));
+    const float r5 = __fmaf_rn(__fmul_rn(ny, ny), oc, c);
+    const float r6 = __fmaf_rn(__fmul_rn(ny, nz), oc, -__fmul_rn(nx, s));
+    const float r8 = __fmaf_rn(__fmul_rn(nz, nx), oc, -__fmul_rn(ny, s));
+    const float r9 = __fmaf_rn(__fmul_rn(nz, ny), oc, __fmul_rn(nx, s));
+    const float r10 = __fmaf_rn(__fmul_rn(nz, nz), oc, c);
+    R[0] = __fadd_rn(__fmul_rn(r0, valid), iv); R[1] = __fmul_rn(r1, valid);
+    R[2] = __fmul_rn(r2, valid); R[3] = 0.f;
+    R[4] = __fmul_rn(r4, valid); R[5] = __fadd_rn(__fmul_rn(r5, valid), iv);
+    R[6] = __fmul_rn(r6, valid); R[7] = 0.f;
+    R[8] = __fmul_rn(r8, valid); R[9] = __fmul_rn(r9, valid);
+    R[10] = __fadd_rn(__fmul_rn(r10, valid), iv); R[11] = 0.f;
+}
+
+// FK of the state in w.q into w.lp.  All lanes of the warp must call it.
+__device__ inline void warp_fk(const SmemTables &t, int L, const WarpScratch &w, int lane) {
+    const int r = lane >> 2, c = lane & 3;
+    const bool own = lane < 12;
+    if (own) w.lp[lane] = (r == c) ? 1.f : 0.f;
+    __syncwarp();
+    for (int i = 1; i < L; ++i) {
+        const int ty = t.type[i];
+        const float *A = w.lp + 12 * t.parent[i];
+        const float *Jp = t.jl + 12 * i;
+        float *out = w.lp + 12 * i;
+        if (ty == 1) {                               // revolute: (parent * pose) * R
+            float Rm[12];
+            rot34(t.axn + 4 * i, w.q[i], Rm);
+            if (own) w.tmp[lane] = mul_elem(A, Jp, r, c);
+            __syncwarp();
+            if (own) out[lane] = mul_elem(w.tmp, Rm, r, c);
+        } else if (ty == 2) {                        // prismatic: parent * (pose * T)
+            const float qi = w.q[i];
+            const float *a = t.axr + 4 * i;
+            float T[12] = {1.f, 0.f, 0.f, __fmul_rn(a[0], qi), 0.f, 1.f, 0.f, __fmul_rn(a[1], qi),
+                           0.f, 0.f, 1.f, __fmul_rn(a[2], qi)};
+            if (own) w.tmp[lane] = mul_elem(Jp, T, r, c);
+            __syncwarp();
+            if (own) out[lane] = mul_elem(A, w.tmp, r, c);
+        } else if (ty == 5) {                        // fixed: parent * pose
+            if (own) out[lane] = mul_elem(A, Jp, r, c);
+        } else {                                     // unsupported: identity
+            if (own) out[lane] = (r == c) ? 1.f : 0.f;
+        }
+        __syncwarp();
+    }
+}
+
+// Sphere centre in the base frame (SingleArmStates.cu:340-393).
+__device__ __forceinline__ float3 xform_point(const float *T, float x, float y, float z) {
+    float3 o;
+    o.x = __fadd_rn(__fmaf_rn(T[2], z, __fmaf_rn(T[1], y, __fmul_rn(T[0], x))), T[3]);
+    o.y = __fadd_rn(__fmaf_rn(T[6], z, __fmaf_rn(T[5], y, __fmul_rn(T[4], x))), T[7]);
+    o.z = __fadd_rn(__fmaf_rn(T[10], z, __fmaf_rn(T[9], y, __fmul_rn(T[8], x))), T[11]);
+    return o;
+}
+
+__device__ __forceinline__ float3 xform_rows(const float4 r0, const float4 r1, const float4 r2, float x, float y,
+                                             float z) {
+    float3 o;
+    o.x = __fadd_rn(__fmaf_rn(r0.z, z, __fmaf_rn(r0.y, y, __fmul_rn(r0.x, x))), r0.w);
+    o.y = __fadd_rn(__fmaf_rn(r1.z, z, __fmaf_rn(r1.y, y, __fmul_rn(r1.x, x))), r1.w);
+    o.z = __fadd_rn(__fmaf_rn(r2.z, z, __fmaf_rn(r2.y, y, __fmul_rn(r2.x, x))), r2.w);
+    return o;
+}
+
+__device__ __forceinline__ float sq3(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// ---------------------------------------------------------------------------------
+// Collision of one state.  Returns true if it collides.  With COST, costs[0..3] of
+// lane 0 receive the warp totals per constraint slot (self, spheres, cuboids,
+// cylinders), following the per-pair cost formulas of SelfCollisionConstraint.cu:80-112,
+// EnvConstraintSphere.cu:57-96, EnvConstraintCuboid.cu:105-159,
+// EnvConstraintCylinder.cu:130-180.
+// ---------------------------------------------------------------------------------
+template <int SPL, bool COST>
+__device__ inline bool warp_collide(const SmemTables &t, const DevRobot &R, const DevEnv &E,
+                                    const WarpScratch &w, int lane, float *costs) {
+    float cx[SPL], cy[SPL], cz[SPL], cr[SPL];
+#pragma unroll
+    for (int m = 0; m < SPL; ++m) {
+        const int k = lane + kWarp * m;
+        if (k < R.S) {
+            const float4 s = t.sph[k];
+            const float3 p = xform_point(w.lp + 12 * t.slink[k], s.x, s.y, s.z);
+            cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
+            w.cen[k] = make_float4(p.x, p.y, p.z, s.w);
+        } else {
+            cx[m] = kFar; cy[m] = kFar; cz[m] = kFar; cr[m] = 0.f;
+        }
+    }
+    __syncwarp();
+
+    bool hit = false;
+    float c_self = 0.f, c_sph = 0.f, c_box = 0.f, c_cyl = 0.f;
+    const float4 *env = t.env;
+
+    // --- environment spheres ---
+    for (int o0 = 0; o0 < E.ns; o0 += 8) {
+        const int oe = min(o0 + 8, E.ns);
+        for (int o = o0; o < oe; ++o) {
+            const float4 b = env[o];
+#pragma unroll
+            for (int m = 0; m < SPL; ++m) {
+                const float d2 = sq3(cx[m] - b.x, cy[m] - b.y, cz[m] - b.z);
+                const float rr = cr[m] + b.w;
+                const bool h = d2 < rr * rr;
+                if (COST) { if (h) c_sph += fmaxf(0.f, rr - sqrtf(d2)); }
+                hit |= h;
+            }
+        }
+        if (!COST && __any_sync(kFull, hit)) return true;
+    }
+    env += E.ns;
+
+    // --- cuboids (inverse pose, clamp to [min, max]) ---
+    for (int o0 = 0; o0 < E.nb; o0 += 4) {
+        const int oe = min(o0 + 4, E.nb);
+        for (int o = o0; o < oe; ++o) {
+            const float4 r0 = env[5 * o], r1 = env[5 * o + 1], r2 = env[5 * o + 2];
+            const float4 mn = env[5 * o + 3], mx = env[5 * o + 4];
+#pragma unroll
+            for (int m = 0; m < SPL; ++m) {
+                const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
+                const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                const float d2 = sq3(dx, dy, dz);
+                const bool h = d2 < cr[m] * cr[m];
+                if (COST) { if (h) c_box += cr[m] - sqrtf(d2); }
+                hit |= h;
+            }
+        }
+        if (!COST && __any_sync(kFull, hit)) return true;
+    }
+    env += 5 * E.nb;
+
+    // --- cylinders (finite, local z axis) ---
+    for (int o0 = 0; o0 < E.nc; o0 += 4) {
+        const int oe = min(o0 + 4, E.nc);
+        for (int o = o0; o < oe; ++o) {
+            const float4 r0 = env[4 * o], r1 = env[4 * o + 1], r2 = env[4 * o + 2], pr = env[4 * o + 3];
+#pragma unroll
+            for (int m = 0; m < SPL; ++m) {
+                const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
+                const float dxy = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x)));
+                const float dx = dxy - pr.x;
+                const float dz = fabsf(l.z) - pr.y;
+                const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                const float outside = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox)));
+                const float inside = fminf(fmaxf(dx, dz), 0.f);
+                const float pen = cr[m] - (outside + inside);
+                if (COST) c_cyl += pen > 0.f ? pen : 0.f;
+                hit |= pen > 0.f;
+            }
+        }
+        if (!COST && __any_sync(kFull, hit)) return true;
+    }
+
+    // --- self collision pairs ---
+    for (int p0 = 0; p0 < R.P; p0 += kWarp * 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = p0 + u * kWarp + lane;
+            if (p < R.P) {
+                const unsigned ij = __ldg(R.pairs + p);
+                const float thr = __ldg(R.thr + p);
+                const float4 a = w.cen[ij & 0xffffu], b = w.cen[ij >> 16];
+                const float d2 = sq3(a.x - b.x, a.y - b.y, a.z - b.z);
+                const bool h = d2 < thr;
+                if (COST) { if (h) c_self += sqrtf(thr) - sqrtf(d2); }
+                hit |= h;
+            }
+        }
+        if (!COST && __any_sync(kFull, hit)) return true;
+    }
+
+    if (COST) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            c_self += __shfl_xor_sync(kFull, c_self, off);
+            c_sph += __shfl_xor_sync(kFull, c_sph, off);
+            c_box += __shfl_xor_sync(kFull, c_box, off);
+            c_cyl += __shfl_xor_sync(kFull, c_cyl, off);
+        }
+        costs[0] = c_self; costs[1] = c_sph; costs[2] = c_box; costs[3] = c_cyl;
+    }
+    return __any_sync(kFull, hit);
+}
+
+// Dispatch on spheres-per-lane.
+template <bool COST>
+__device__ inline bool warp_collide_dispatch(const SmemTables &t, const DevRobot &R, const DevEnv &E,
+                                             const WarpScratch &w, int lane, float *costs) {
+    switch (R.spl) {
+    case 1: return warp_collide<1, COST>(t, R, E, w, lane, costs);
+    case 2: return warp_collide<2, COST>(t, R, E, w, lane, costs);
+    case 3: return warp_collide<3, COST>(t, R, E, w, lane, costs);
+    case 4: return warp_collide<4, COST>(t, R, E, w, lane, costs);
+    case 5: return warp_collide<5, COST>(t, R, E, w, lane, costs);
+    case 6: return warp_collide<6, COST>(t, R, E, w, lane, costs);
+    case 7: return warp_collide<7, COST>(t, R, E, w, lane, costs);
+    default: return warp_collide<8, COST>(t, R, E, w, lane, costs);
+    }
+}
+
+}  // namespace gbmp

@@ -1,0 +1,110 @@
+// gbmp_internal.h -- host-side handle structures and helpers shared by the
+// translation units of libgbmp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbmp.h"
+#include "gbmp_device.cuh"
+
+namespace gbmp {
+
+void set_error(const char *fmt, ...);
+
+#define GBMP_CUDA(call)                                                                        \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            ::gbmp::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                              __LINE__);                                                       \
+            return e_ == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;   \
+        }                                                                                      \
+    } while (0)
+
+#define GBMP_CHECK_ARG(cond, ...)                 \
+    do {                                          \
+        if (!(cond)) {                            \
+            ::gbmp::set_error(__VA_ARGS__);       \
+            return GBMP_ERR_INVALID_ARGUMENT;     \
+        }                                         \
+    } while (0)
+
+constexpr int kMaxSelfPairs = 65535 * 4;
+constexpr int kMaxEnvWords = 12 * 1024;     // 192 KB of float4 staged in shared memory
+constexpr int kWarpsPerBlock = 8;
+
+// Growable device buffer owned by a handle.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    gbmp_status reserve(size_t n) {
+        if (n <= bytes) return GBMP_OK;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t want = n + n / 4 + 256;
+        GBMP_CUDA(cudaMalloc(&ptr, want));
+        bytes = want;
+        return GBMP_OK;
+    }
+    ~DevBuf() {
+        if (ptr) cudaFree(ptr);
+    }
+};
+
+struct Codegen;   // runtime-generated robot kernels (gbmp_codegen.cpp)
+
+// Instrumentation (gbmp_prof.cu).  A ProfScope around a launch counts it and, when
+// profiling is on, records CUDA events on the launching stream around it.
+constexpr int kProfFamilies = 4;
+void count_launch(int n);
+struct ProfScope {
+    int fam;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(int family, cudaStream_t stream);
+    ~ProfScope();
+    ProfScope(const ProfScope &) = delete;
+    ProfScope &operator=(const ProfScope &) = delete;
+};
+
+}  // namespace gbmp
+
+struct gbmp_robot_s {
+    int L = 0, S = 0, P = 0, dim = 0;
+    float resolution = 0.02f;
+    int device = 0;
+    int num_sms = 0;
+    // host copies
+    std::vector<int> type, parent, slink;
+    std::vector<float> pose16, axis, sph_pos, sph_r, lower, upper, defv;
+    std::vector<unsigned char> active, enables;
+    std::vector<int> pairs;          // 2*P
+    std::vector<float> thr;          // P
+    // device tables (one allocation)
+    void *d_block = nullptr;
+    gbmp::DevRobot dev{};
+    // edge-check scratch
+    std::mutex scratch_mu;
+    gbmp::DevBuf scratch;
+    gbmp::Codegen *cg = nullptr;
+    bool use_cg = false;
+};
+
+struct gbmp_env_s {
+    int ns = 0, nb = 0, nc = 0;
+    float4 *d_words = nullptr;
+    std::vector<float4> h_words;
+    gbmp::DevEnv dev() const {
+        gbmp::DevEnv e;
+        e.ns = ns; e.nb = nb; e.nc = nc;
+        e.words = d_words;
+        return e;
+    }
+};

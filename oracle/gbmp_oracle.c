@@ -1,0 +1,631 @@
+/*
+ * gbmp_oracle.c -- CPU restatement of the reference hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference arm of bench.py, never by the product library.
+ *
+ * Build: gcc -O2 -ffp-contract=off -fopenmp (see oracle/build.py).  Contraction
+ * is off so that every fused multiply-add below is the explicit fmaf() written
+ * here; the CUDA kernels use the same explicit __fmaf_rn chain, so the FP32
+ * results differ only where cosf/sinf differ in the last bit.
+ */
+#include "gbmp_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int32_t or_num_threads(void)
+{
+#ifdef _OPENMP
+    return (int32_t)omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------- */
+/* Forward kinematics.                                                       */
+/* Follows the generated kernel cudampl/CUDAMPLib/include/spaces/            */
+/* KernelGenerator.h:222-406 (multiply4x4 :257-280, make_rotation_axis_angle */
+/* :293-325, revolute :328-340, prismatic :343-361, unrolled chain :369-400) */
+/* and the table-driven twin cudampl/CUDAMPLib/src/states/                   */
+/* SingleArmStates.cu:178-221.  Poses are 3x4 affine blocks of a row-major   */
+/* 4x4; the last row is always (0,0,0,1) (KernelGenerator.h:275).           */
+/* ------------------------------------------------------------------------- */
+
+/* C = A * B for row-major 4x4 with implicit last row (0 0 0 1). */
+static void mul_f32(const float *A, const float *B, float *C)
+{
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 4; ++c) {
+            float acc = A[r * 4 + 0] * B[0 * 4 + c];
+            acc = fmaf(A[r * 4 + 1], B[1 * 4 + c], acc);
+            acc = fmaf(A[r * 4 + 2], B[2 * 4 + c], acc);
+            if (c == 3) acc = acc + A[r * 4 + 3];
+            C[r * 4 + c] = acc;
+        }
+    }
+    C[12] = 0.f; C[13] = 0.f; C[14] = 0.f; C[15] = 1.f;
+}
+
+static void mul_f64(const double *A, const double *B, double *C)
+{
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) {
+            double acc = A[r * 4 + 0] * B[c] + A[r * 4 + 1] * B[4 + c] + A[r * 4 + 2] * B[8 + c];
+            if (c == 3) acc += A[r * 4 + 3];
+            C[r * 4 + c] = acc;
+        }
+    C[12] = 0.; C[13] = 0.; C[14] = 0.; C[15] = 1.;
+}
+
+/* Normalised axis, KernelGenerator.h:295-304 (length threshold 1e-12). */
+static void unit_axis_f32(const float *a, float *n)
+{
+    float len = sqrtf(fmaf(a[2], a[2], fmaf(a[1], a[1], a[0] * a[0])));
+    float valid = (len >= 1e-12f) ? 1.f : 0.f;
+    float inv = 1.f / fmaxf(len, 1e-12f);
+    n[0] = a[0] * inv * valid;
+    n[1] = a[1] * inv * valid;
+    n[2] = a[2] * inv * valid;
+    n[3] = valid;
+}
+
+/* Rodrigues rotation, KernelGenerator.h:305-325. */
+static void rot_f32(const float *n, float angle, float *R)
+{
+    float nx = n[0], ny = n[1], nz = n[2], valid = n[3];
+    float c = cosf(angle), s = sinf(angle), oc = 1.f - c;
+    float r0 = fmaf(nx * nx, oc, c);
+    float r1 = fmaf(nx * ny, oc, -(nz * s));
+    float r2 = fmaf(nx * nz, oc, ny * s);
+    float r4 = fmaf(ny * nx, oc, nz * s);
+    float r5 = fmaf(ny * ny, oc, c);
+    float r6 = fmaf(ny * nz, oc, -(nx * s));
+    float r8 = fmaf(nz * nx, oc, -(ny * s));
+    float r9 = fmaf(nz * ny, oc, nx * s);
+    float r10 = fmaf(nz * nz, oc, c);
+    float iv = 1.f - valid;
+    R[0] = r0 * valid + iv; R[1] = r1 * valid; R[2] = r2 * valid; R[3] = 0.f;
+    R[4] = r4 * valid; R[5] = r5 * valid + iv; R[6] = r6 * valid; R[7] = 0.f;
+    R[8] = r8 * valid; R[9] = r9 * valid; R[10] = r10 * valid + iv; R[11] = 0.f;
+    R[12] = 0.f; R[13] = 0.f; R[14] = 0.f; R[15] = 1.f;
+}
+
+static void rot_f64(const float *a, double angle, double *R)
+{
+    double x = a[0], y = a[1], z = a[2];
+    double len = sqrt(x * x + y * y + z * z);
+    double valid = len >= 1e-12 ? 1. : 0.;
+    double inv = 1. / fmax(len, 1e-12);
+    double nx = x * inv * valid, ny = y * inv * valid, nz = z * inv * valid;
+    double c = cos(angle), s = sin(angle), oc = 1. - c, iv = 1. - valid;
+    R[0] = (c + nx * nx * oc) * valid + iv; R[1] = (nx * ny * oc - nz * s) * valid;
+    R[2] = (nx * nz * oc + ny * s) * valid; R[3] = 0.;
+    R[4] = (ny * nx * oc + nz * s) * valid; R[5] = (c + ny * ny * oc) * valid + iv;
+    R[6] = (ny * nz * oc - nx * s) * valid; R[7] = 0.;
+    R[8] = (nz * nx * oc - ny * s) * valid; R[9] = (nz * ny * oc + nx * s) * valid;
+    R[10] = (c + nz * nz * oc) * valid + iv; R[11] = 0.;
+    R[12] = 0.; R[13] = 0.; R[14] = 0.; R[15] = 1.;
+}
+
+static void fk_one_f32(const or_robot *r, const float *q, float *P)
+{
+    static const float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    memcpy(P, I, sizeof I);                       /* link 0 = identity (:365-368) */
+    float tmp[16], M[16], n[4];
+    for (int i = 1; i < r->L; ++i) {
+        const float *par = P + 16 * r->parent[i];
+        const float *jp = r->pose + 16 * i;
+        float *out = P + 16 * i;
+        switch (r->type[i]) {
+        case OR_REVOLUTE:                         /* (parent * pose) * R(axis, q) */
+            unit_axis_f32(r->axis + 3 * i, n);
+            rot_f32(n, q[i], M);
+            mul_f32(par, jp, tmp);
+            mul_f32(tmp, M, out);
+            break;
+        case OR_PRISMATIC: {                      /* parent * (pose * T(axis q)) */
+            const float *a = r->axis + 3 * i;
+            float T[16] = {1, 0, 0, a[0] * q[i], 0, 1, 0, a[1] * q[i], 0, 0, 1, a[2] * q[i], 0, 0, 0, 1};
+            mul_f32(jp, T, tmp);
+            mul_f32(par, tmp, out);
+            break;
+        }
+        case OR_FIXED:
+            mul_f32(par, jp, out);
+            break;
+        default:                                  /* unsupported type: pose left unwritten in the
+                                                     reference (:397); identity here */
+            memcpy(out, I, sizeof I);
+            break;
+        }
+    }
+}
+
+static void fk_one_f64(const or_robot *r, const double *q, double *P)
+{
+    for (int k = 0; k < 16; ++k) P[k] = (k % 5 == 0) ? 1. : 0.;
+    double tmp[16], M[16], jp[16];
+    for (int i = 1; i < r->L; ++i) {
+        const double *par = P + 16 * r->parent[i];
+        double *out = P + 16 * i;
+        for (int k = 0; k < 16; ++k) jp[k] = r->pose[16 * i + k];
+        if (r->type[i] == OR_REVOLUTE) {
+            rot_f64(r->axis + 3 * i, q[i], M);
+            mul_f64(par, jp, tmp);
+            mul_f64(tmp, M, out);
+        } else if (r->type[i] == OR_PRISMATIC) {
+            const float *a = r->axis + 3 * i;
+            double T[16] = {1, 0, 0, a[0] * q[i], 0, 1, 0, a[1] * q[i], 0, 0, 1, a[2] * q[i], 0, 0, 0, 1};
+            mul_f64(jp, T, tmp);
+            mul_f64(par, tmp, out);
+        } else if (r->type[i] == OR_FIXED) {
+            mul_f64(par, jp, out);
+        } else {
+            for (int k = 0; k < 16; ++k) out[k] = (k % 5 == 0) ? 1. : 0.;
+        }
+    }
+}
+
+void or_fk_f32(const or_robot *r, const float *q, int64_t n, float *poses)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < n; ++s) fk_one_f32(r, q + s * r->L, poses + s * r->L * 16);
+}
+
+void or_fk_f64(const or_robot *r, const double *q, int64_t n, double *poses)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < n; ++s) fk_one_f64(r, q + s * r->L, poses + s * r->L * 16);
+}
+
+/* Sphere centres in the base frame, cudampl/CUDAMPLib/src/states/SingleArmStates.cu:340-393. */
+static void centers_one_f32(const or_robot *r, const float *P, float *C)
+{
+    for (int i = 0; i < r->S; ++i) {
+        const float *T = P + 16 * r->sph_link[i];
+        float sx = r->sph_pos[3 * i], sy = r->sph_pos[3 * i + 1], sz = r->sph_pos[3 * i + 2];
+        for (int row = 0; row < 3; ++row)
+            C[3 * i + row] = fmaf(T[4 * row + 2], sz, fmaf(T[4 * row + 1], sy, T[4 * row] * sx)) + T[4 * row + 3];
+    }
+}
+
+void or_sphere_centers_f32(const or_robot *r, const float *poses, int64_t n, float *centers)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < n; ++s) centers_one_f32(r, poses + s * r->L * 16, centers + s * r->S * 3);
+}
+
+void or_sphere_centers_f64(const or_robot *r, const double *poses, int64_t n, double *centers)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < n; ++s) {
+        const double *P = poses + s * r->L * 16;
+        double *C = centers + s * r->S * 3;
+        for (int i = 0; i < r->S; ++i) {
+            const double *T = P + 16 * r->sph_link[i];
+            double sx = r->sph_pos[3 * i], sy = r->sph_pos[3 * i + 1], sz = r->sph_pos[3 * i + 2];
+            for (int row = 0; row < 3; ++row)
+                C[3 * i + row] = T[4 * row] * sx + T[4 * row + 1] * sy + T[4 * row + 2] * sz + T[4 * row + 3];
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Collision model.                                                          */
+/* ------------------------------------------------------------------------- */
+
+/* Self-collision pair list, cudampl/CUDAMPLib/src/constraints/
+ * SelfCollisionConstraint.cu:28-38: i < j, different links, link pair enabled;
+ * threshold stored squared.  enables == NULL means every link pair enabled. */
+int32_t or_self_pairs(const or_robot *r, const uint8_t *enables, int32_t *pairs, float *thr_sq, int32_t cap)
+{
+    int32_t k = 0;
+    for (int i = 0; i < r->S; ++i)
+        for (int j = i + 1; j < r->S; ++j) {
+            int li = r->sph_link[i], lj = r->sph_link[j];
+            if (li == lj) continue;
+            if (enables && !enables[li * r->L + lj]) continue;
+            if (k < cap) {
+                pairs[2 * k] = i;
+                pairs[2 * k + 1] = j;
+                float s = r->sph_r[i] + r->sph_r[j];
+                thr_sq[k] = s * s;
+            }
+            ++k;
+        }
+    return k;
+}
+
+/* Inverse pose [R^T | -R^T t] of an obstacle, cudampl/CUDAMPLib/src/constraints/
+ * EnvConstraintCuboid.cu:13-34 and EnvConstraintCylinder.cu:17-45. */
+void or_inverse_pose(const float *pos, const float *rot, float *inv)
+{
+    float t00 = rot[0], t01 = rot[3], t02 = rot[6];
+    float t10 = rot[1], t11 = rot[4], t12 = rot[7];
+    float t20 = rot[2], t21 = rot[5], t22 = rot[8];
+    inv[0] = t00; inv[1] = t01; inv[2] = t02;
+    inv[4] = t10; inv[5] = t11; inv[6] = t12;
+    inv[8] = t20; inv[9] = t21; inv[10] = t22;
+    inv[3] = -(t00 * pos[0] + t01 * pos[1] + t02 * pos[2]);
+    inv[7] = -(t10 * pos[0] + t11 * pos[1] + t12 * pos[2]);
+    inv[11] = -(t20 * pos[0] + t21 * pos[1] + t22 * pos[2]);
+}
+
+static inline void xform34(const float *M, float x, float y, float z, float *o)
+{
+    o[0] = fmaf(M[2], z, fmaf(M[1], y, M[0] * x)) + M[3];
+    o[1] = fmaf(M[6], z, fmaf(M[5], y, M[4] * x)) + M[7];
+    o[2] = fmaf(M[10], z, fmaf(M[9], y, M[8] * x)) + M[11];
+}
+
+/* Self cost, SelfCollisionConstraint.cu:80-112. */
+static float self_cost(const float *C, int32_t np, const int32_t *pairs, const float *thr_sq)
+{
+    float sum = 0.f;
+    for (int k = 0; k < np; ++k) {
+        const float *a = C + 3 * pairs[2 * k], *b = C + 3 * pairs[2 * k + 1];
+        float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        if (d2 < thr_sq[k]) sum += sqrtf(thr_sq[k]) - sqrtf(d2);
+    }
+    return sum;
+}
+
+/* Environment spheres, cudampl/CUDAMPLib/src/constraints/EnvConstraintSphere.cu:57-96. */
+static float env_sphere_cost(const or_robot *r, const or_env *e, const float *C)
+{
+    float sum = 0.f;
+    for (int i = 0; i < r->S; ++i) {
+        float rs = r->sph_r[i];
+        for (int o = 0; o < e->ns; ++o) {
+            const float *b = e->sph + 4 * o;
+            float dx = C[3 * i] - b[0], dy = C[3 * i + 1] - b[1], dz = C[3 * i + 2] - b[2];
+            float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            float rr = rs + b[3];
+            if (d2 < rr * rr) sum += fmaxf(0.f, rr - sqrtf(d2));
+        }
+    }
+    return sum;
+}
+
+/* Cuboids, cudampl/CUDAMPLib/src/constraints/EnvConstraintCuboid.cu:105-159. */
+static float env_cuboid_cost(const or_robot *r, const or_env *e, const float *C)
+{
+    float sum = 0.f;
+    for (int i = 0; i < r->S; ++i) {
+        float rs = r->sph_r[i];
+        for (int o = 0; o < e->nb; ++o) {
+            float l[3];
+            xform34(e->box_inv + 12 * o, C[3 * i], C[3 * i + 1], C[3 * i + 2], l);
+            const float *mn = e->box_min + 3 * o, *mx = e->box_max + 3 * o;
+            float dx = l[0] - fminf(fmaxf(l[0], mn[0]), mx[0]);
+            float dy = l[1] - fminf(fmaxf(l[1], mn[1]), mx[1]);
+            float dz = l[2] - fminf(fmaxf(l[2], mn[2]), mx[2]);
+            float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (d2 < rs * rs) sum += rs - sqrtf(d2);
+        }
+    }
+    return sum;
+}
+
+/* Cylinders along local z, cudampl/CUDAMPLib/src/constraints/EnvConstraintCylinder.cu:130-180. */
+static float env_cylinder_cost(const or_robot *r, const or_env *e, const float *C)
+{
+    float sum = 0.f;
+    for (int i = 0; i < r->S; ++i) {
+        float rs = r->sph_r[i];
+        for (int o = 0; o < e->nc; ++o) {
+            float l[3];
+            xform34(e->cyl_inv + 12 * o, C[3 * i], C[3 * i + 1], C[3 * i + 2], l);
+            float dxy = sqrtf(fmaf(l[1], l[1], l[0] * l[0]));
+            float dx = dxy - e->cyl_r[o];
+            float dz = fabsf(l[2]) - e->cyl_h[o] * 0.5f;
+            float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+            float outside = sqrtf(fmaf(oz, oz, ox * ox));
+            float inside = fminf(fmaxf(dx, dz), 0.f);
+            float pen = rs - (outside + inside);
+            sum += pen > 0.f ? pen : 0.f;
+        }
+    }
+    return sum;
+}
+
+/* checkStates: per-constraint cost in SoA slots, total = sum of slots
+ * (cudampl/CUDAMPLib/src/spaces/SingleArmSpace.cu:1572-1602,
+ *  cudampl/CUDAMPLib/src/base/States.cu:5-21).  Feasible <=> total == 0. */
+void or_check_states(const or_robot *r, const or_env *e, int32_t npairs, const int32_t *pairs,
+                     const float *thr_sq, const float *q, int64_t n, float *costs, float *total,
+                     int32_t nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+#pragma omp parallel num_threads(nthreads)
+    {
+        float *P = (float *)malloc(sizeof(float) * 16 * r->L);
+        float *C = (float *)malloc(sizeof(float) * 3 * (r->S + 1));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t s = 0; s < n; ++s) {
+            fk_one_f32(r, q + s * r->L, P);
+            centers_one_f32(r, P, C);
+            float c0 = self_cost(C, npairs, pairs, thr_sq);
+            float c1 = env_sphere_cost(r, e, C);
+            float c2 = env_cuboid_cost(r, e, C);
+            float c3 = env_cylinder_cost(r, e, C);
+            if (costs) {
+                costs[0 * n + s] = c0; costs[1 * n + s] = c1;
+                costs[2 * n + s] = c2; costs[3 * n + s] = c3;
+            }
+            if (total) total[s] = ((c0 + c1) + c2) + c3;
+        }
+        free(P);
+        free(C);
+    }
+}
+
+/* Signed clearance (FP64): min over every checked pair of distance minus radii;
+ * negative = penetration.  Used to exclude states within a band of the contact
+ * surface from verdict comparisons. */
+void or_clearance_f64(const or_robot *r, const or_env *e, int32_t npairs, const int32_t *pairs,
+                      const double *q, int64_t n, double *clearance, int32_t nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+#pragma omp parallel num_threads(nthreads)
+    {
+        double *P = (double *)malloc(sizeof(double) * 16 * r->L);
+        double *C = (double *)malloc(sizeof(double) * 3 * (r->S + 1));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t s = 0; s < n; ++s) {
+            fk_one_f64(r, q + s * r->L, P);
+            for (int i = 0; i < r->S; ++i) {
+                const double *T = P + 16 * r->sph_link[i];
+                double sx = r->sph_pos[3 * i], sy = r->sph_pos[3 * i + 1], sz = r->sph_pos[3 * i + 2];
+                for (int row = 0; row < 3; ++row)
+                    C[3 * i + row] = T[4 * row] * sx + T[4 * row + 1] * sy + T[4 * row + 2] * sz + T[4 * row + 3];
+            }
+            double best = DBL_MAX;
+            for (int k = 0; k < npairs; ++k) {
+                const double *a = C + 3 * pairs[2 * k], *b = C + 3 * pairs[2 * k + 1];
+                double d = sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+                double c = d - ((double)r->sph_r[pairs[2 * k]] + (double)r->sph_r[pairs[2 * k + 1]]);
+                if (c < best) best = c;
+            }
+            for (int i = 0; i < r->S; ++i) {
+                double x = C[3 * i], y = C[3 * i + 1], z = C[3 * i + 2], rs = r->sph_r[i];
+                for (int o = 0; o < e->ns; ++o) {
+                    const float *b = e->sph + 4 * o;
+                    double d = sqrt((x - b[0]) * (x - b[0]) + (y - b[1]) * (y - b[1]) + (z - b[2]) * (z - b[2]));
+                    double c = d - (rs + (double)b[3]);
+                    if (c < best) best = c;
+                }
+                for (int o = 0; o < e->nb; ++o) {
+                    const float *M = e->box_inv + 12 * o;
+                    double l[3];
+                    for (int row = 0; row < 3; ++row)
+                        l[row] = M[4 * row] * x + M[4 * row + 1] * y + M[4 * row + 2] * z + M[4 * row + 3];
+                    const float *mn = e->box_min + 3 * o, *mx = e->box_max + 3 * o;
+                    double out2 = 0., depth = DBL_MAX;
+                    int inside = 1;
+                    for (int a = 0; a < 3; ++a) {
+                        double lo = mn[a], hi = mx[a];
+                        if (l[a] < lo) { out2 += (lo - l[a]) * (lo - l[a]); inside = 0; }
+                        else if (l[a] > hi) { out2 += (l[a] - hi) * (l[a] - hi); inside = 0; }
+                        else { double dd = fmin(l[a] - lo, hi - l[a]); if (dd < depth) depth = dd; }
+                    }
+                    double sd = inside ? -depth : sqrt(out2);
+                    double c = sd - rs;
+                    if (c < best) best = c;
+                }
+                for (int o = 0; o < e->nc; ++o) {
+                    const float *M = e->cyl_inv + 12 * o;
+                    double l[3];
+                    for (int row = 0; row < 3; ++row)
+                        l[row] = M[4 * row] * x + M[4 * row + 1] * y + M[4 * row + 2] * z + M[4 * row + 3];
+                    double dx = sqrt(l[0] * l[0] + l[1] * l[1]) - e->cyl_r[o];
+                    double dz = fabs(l[2]) - 0.5 * e->cyl_h[o];
+                    double ox = dx > 0 ? dx : 0, oz = dz > 0 ? dz : 0;
+                    double sdf = sqrt(ox * ox + oz * oz) + fmin(fmax(dx, dz), 0.);
+                    double c = sdf - rs;
+                    if (c < best) best = c;
+                }
+            }
+            clearance[s] = best;
+        }
+        free(P);
+        free(C);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Edges.                                                                    */
+/* Step rule of the generated get_step kernel, KernelGenerator.h:408-465:    */
+/*   d = ||to - from||_2 over all J entries, n = (int)(d / res) + 1,         */
+/*   dir = (to - from) / n.                                                  */
+/* Interpolation, KernelGenerator.h:467-522: state k = from + dir * k for    */
+/* k < n, then state n-1 := to.  The generated code is compiled by NVRTC     */
+/* with FMA contraction on (cudampl/CUDAMPLib/include/NvrtcUtil.h:85-94), so */
+/* the sum of squares and the interpolation are fused multiply-adds.         */
+/* The L-infinity rule (max |to - from| <= res per step) keeps the same n/dir */
+/* structure with d = max_j |to_j - from_j|.                                 */
+/* ------------------------------------------------------------------------- */
+
+int32_t or_edge_steps(const float *from, const float *to, int32_t J, float res, int32_t rule,
+                      float *dir, float *length)
+{
+    float d2 = 0.f, dinf = 0.f;
+    for (int j = 0; j < J; ++j) {
+        float d = from[j] - to[j];
+        d2 = fmaf(d, d, d2);
+        float a = fabsf(d);
+        dinf = a > dinf ? a : dinf;
+    }
+    float d = sqrtf(d2);
+    if (length) *length = d;
+    float metric = (rule == OR_STEP_LINF) ? dinf : d;
+    int32_t n = (int32_t)(metric / res) + 1;
+    if (dir)
+        for (int j = 0; j < J; ++j) dir[j] = (to[j] - from[j]) / (float)n;
+    return n;
+}
+
+void or_edge_state(const float *from, const float *to, const float *dir, int32_t J, int32_t n,
+                   int32_t k, float *out)
+{
+    if (k == n - 1) {
+        memcpy(out, to, sizeof(float) * J);
+        return;
+    }
+    for (int j = 0; j < J; ++j) out[j] = fmaf(dir[j], (float)k, from[j]);
+}
+
+/* checkMotions (SingleArmSpace.cu:628-848): every interpolated state is checked;
+ * an edge is feasible iff the sum of its states' total costs is 0 (:603-626);
+ * its cost is d (:831).  first_hit (not produced by the reference) is the lowest
+ * state index with non-zero total cost, -1 if none.  early_exit=0 evaluates every
+ * state of every edge like the reference; early_exit=1 stops an edge at its first
+ * hit (same outputs). */
+void or_check_motions(const or_robot *r, const or_env *e, int32_t npairs, const int32_t *pairs,
+                      const float *thr_sq, const float *from, const float *to, int64_t E,
+                      float res, int32_t rule, int32_t early_exit, uint8_t *ok, int32_t *first_hit,
+                      int32_t *num_steps, float *length, int32_t nthreads)
+{
+    const int J = r->L;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+#pragma omp parallel num_threads(nthreads)
+    {
+        float *P = (float *)malloc(sizeof(float) * 16 * J);
+        float *C = (float *)malloc(sizeof(float) * 3 * (r->S + 1));
+        float *dir = (float *)malloc(sizeof(float) * J);
+        float *st = (float *)malloc(sizeof(float) * J);
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t k = 0; k < E; ++k) {
+            const float *f = from + k * J, *t = to + k * J;
+            float len;
+            int32_t n = or_edge_steps(f, t, J, res, rule, dir, &len);
+            int32_t hit = -1;
+            float sum = 0.f;
+            for (int32_t s = 0; s < n; ++s) {
+                or_edge_state(f, t, dir, J, n, s, st);
+                fk_one_f32(r, st, P);
+                centers_one_f32(r, P, C);
+                float tot = self_cost(C, npairs, pairs, thr_sq);
+                tot += env_sphere_cost(r, e, C);
+                tot += env_cuboid_cost(r, e, C);
+                tot += env_cylinder_cost(r, e, C);
+                sum += tot;
+                if (tot != 0.f && hit < 0) {
+                    hit = s;
+                    if (early_exit) break;
+                }
+            }
+            if (ok) ok[k] = (sum == 0.f);
+            if (first_hit) first_hit[k] = hit;
+            if (num_steps) num_steps[k] = n;
+            if (length) length[k] = len;
+        }
+        free(P);
+        free(C);
+        free(dir);
+        free(st);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* State-manager kernels.                                                    */
+/* ------------------------------------------------------------------------- */
+
+/* Nearest neighbour among candidate indices, distance over active joints only,
+ * cudampl/CUDAMPLib/src/states/SingleArmStates.cu:1265-1336.  The squared
+ * distance is accumulated in joint order with fused multiply-adds (the reference's
+ * contracted loop, :1285-1300) and compared without the monotone sqrt.  Exact ties
+ * resolve to the lowest candidate position. */
+void or_nearest(const float *tree, int64_t M, int32_t J, const uint8_t *active,
+                const int32_t *cand, int64_t ncand, const float *queries, int64_t Q,
+                int32_t *out, int32_t nthreads)
+{
+    (void)M;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t q = 0; q < Q; ++q) {
+        const float *x = queries + q * J;
+        float best = INFINITY;
+        int32_t bi = -1;
+        for (int64_t c = 0; c < ncand; ++c) {
+            int64_t idx = cand ? cand[c] : c;
+            const float *y = tree + idx * J;
+            float s = 0.f;
+            for (int j = 0; j < J; ++j)
+                if (!active || active[j]) {
+                    float d = x[j] - y[j];
+                    s = fmaf(d, d, s);
+                }
+            if (s < best) {
+                best = s;
+                bi = (int32_t)idx;
+            }
+        }
+        out[q] = bi;
+    }
+}
+
+/* Philox4x32-10 (Salmon et al., SC'11), the counter-based generator behind the
+ * product's sampler: sample k, joint j uses counter (offset + k, j), key seed, and
+ * the 24 high bits of output word 0.  Value = fma(u, upper - lower, lower). */
+static void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+}
+
+void or_sample(const float *lower, const float *upper, const uint8_t *active, const float *defv,
+               int32_t J, uint64_t seed, uint64_t offset, int64_t n, float *q)
+{
+    for (int64_t k = 0; k < n; ++k)
+        for (int j = 0; j < J; ++j) {
+            if (!active[j]) { q[k * J + j] = defv[j]; continue; }
+            uint64_t ctr = offset + (uint64_t)k;
+            uint32_t c[4] = {(uint32_t)ctr, (uint32_t)(ctr >> 32), (uint32_t)j, 0u};
+            philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+            float u = (float)(c[0] >> 8) * (1.0f / 16777216.0f);
+            q[k * J + j] = fmaf(u, upper[j] - lower[j], lower[j]);
+        }
+}
+
+/* Steer towards a sample, limiting the step to max_distance
+ * (SingleArmStates.cu:1488-1522, SingleArmSpace.cu:219-249). */
+void or_steer(const float *from, float *to, int64_t n, int32_t J, float max_distance)
+{
+    for (int64_t k = 0; k < n; ++k) {
+        const float *f = from + k * J;
+        float *t = to + k * J;
+        float s = 0.f;
+        for (int j = 0; j < J; ++j) {
+            float d = f[j] - t[j];
+            s = fmaf(d, d, s);
+        }
+        float d = sqrtf(s);
+        if (d > max_distance) {
+            float sc = max_distance / d;
+            for (int j = 0; j < J; ++j) t[j] = fmaf(sc, t[j] - f[j], f[j]);
+        }
+    }
+}

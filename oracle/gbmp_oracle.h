@@ -1,0 +1,101 @@
+/*
+ * gbmp_oracle.h -- CPU restatement of the reference motion-planning hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This code is the checker for the CUDA product
+ * path and the timed CPU baseline; the product never links or calls it.
+ *
+ * Every function restates one piece of CUDAMPLib / CPRRTC arithmetic and cites
+ * the reference file:line it follows (paths relative to the reference tree).
+ * The FP32 functions keep the reference's operation order; the FP64 functions
+ * are the high-precision truth used for tolerance checks.
+ *
+ * Pinning: the FK, edge-step and interpolation restatements are checked in
+ * tests against the reference's own generated kernels (compiled for the CPU
+ * from cudampl/CUDAMPLib/include/spaces/KernelGenerator.h by oracle/ref_build.py);
+ * the collision-cost restatements are checked against the reference's own
+ * constraint kernels compiled for the CPU by the same recipe (block-level SIMT
+ * emulation).  Where the recipe cannot run (no reference tree), parity of the
+ * collision costs rests on this restatement alone.
+ */
+#ifndef GBMP_ORACLE_H
+#define GBMP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Joint type codes, cudampl/CUDAMPLib/include/states/SingleArmStates.h:190-195. */
+#define OR_REVOLUTE 1
+#define OR_PRISMATIC 2
+#define OR_FIXED 5
+
+typedef struct or_robot {
+    int32_t L;                 /* links == joints (joint i drives link i)        */
+    const int32_t *type;       /* [L]                                            */
+    const float *pose;         /* [L*16] row-major joint origin in parent frame  */
+    const float *axis;         /* [L*3]                                          */
+    const int32_t *parent;     /* [L]  parent[i] < i, parent[0] < 0              */
+    int32_t S;                 /* collision spheres                              */
+    const int32_t *sph_link;   /* [S]                                            */
+    const float *sph_pos;      /* [S*3] centre in link frame                     */
+    const float *sph_r;        /* [S]                                            */
+} or_robot;
+
+typedef struct or_env {
+    int32_t ns;                /* obstacle spheres                               */
+    const float *sph;          /* [ns*4] x y z r                                 */
+    int32_t nb;                /* cuboids                                        */
+    const float *box_inv;      /* [nb*12] inverse pose 3x4 row-major             */
+    const float *box_min;      /* [nb*3]                                         */
+    const float *box_max;      /* [nb*3]                                         */
+    int32_t nc;                /* cylinders (local z axis)                       */
+    const float *cyl_inv;      /* [nc*12]                                        */
+    const float *cyl_r;        /* [nc]                                           */
+    const float *cyl_h;        /* [nc] full height                               */
+} or_env;
+
+/* ---- kinematics ---- */
+void or_fk_f32(const or_robot *r, const float *q, int64_t n, float *poses);
+void or_fk_f64(const or_robot *r, const double *q, int64_t n, double *poses);
+void or_sphere_centers_f32(const or_robot *r, const float *poses, int64_t n, float *centers);
+void or_sphere_centers_f64(const or_robot *r, const double *poses, int64_t n, double *centers);
+
+/* ---- collision model ---- */
+int32_t or_self_pairs(const or_robot *r, const uint8_t *enables, int32_t *pairs, float *thr_sq, int32_t cap);
+void or_inverse_pose(const float *pos, const float *rot, float *inv);
+
+/* costs: SoA out[4*n]: slot 0 self, 1 env spheres, 2 cuboids, 3 cylinders */
+void or_check_states(const or_robot *r, const or_env *e, int32_t npairs, const int32_t *pairs,
+                     const float *thr_sq, const float *q, int64_t n, float *costs, float *total,
+                     int32_t nthreads);
+void or_clearance_f64(const or_robot *r, const or_env *e, int32_t npairs, const int32_t *pairs,
+                      const double *q, int64_t n, double *clearance, int32_t nthreads);
+
+/* ---- edges ---- */
+#define OR_STEP_L2 0
+#define OR_STEP_LINF 1
+int32_t or_edge_steps(const float *from, const float *to, int32_t J, float res, int32_t rule,
+                      float *dir, float *length);
+void or_edge_state(const float *from, const float *to, const float *dir, int32_t J, int32_t n,
+                   int32_t k, float *out);
+void or_check_motions(const or_robot *r, const or_env *e, int32_t npairs, const int32_t *pairs,
+                      const float *thr_sq, const float *from, const float *to, int64_t E,
+                      float res, int32_t rule, int32_t early_exit, uint8_t *ok, int32_t *first_hit,
+                      int32_t *num_steps, float *length, int32_t nthreads);
+
+/* ---- state-manager kernels ---- */
+void or_nearest(const float *tree, int64_t M, int32_t J, const uint8_t *active,
+                const int32_t *cand, int64_t ncand, const float *queries, int64_t Q,
+                int32_t *out, int32_t nthreads);
+void or_steer(const float *from, float *to, int64_t n, int32_t J, float max_distance);
+void or_sample(const float *lower, const float *upper, const uint8_t *active, const float *defv,
+               int32_t J, uint64_t seed, uint64_t offset, int64_t n, float *q);
+
+int32_t or_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

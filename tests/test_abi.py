@@ -1,0 +1,104 @@
+"""The C-ABI library loads and exports every entry point of include/gbmp.h, and its
+argument validation answers without a GPU (no compute calls here)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from isaac_sim_ros2_humble_gb300 import _lib, workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for hdr in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if hdr.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", hdr)).read()
+            names += re.findall(r"^GBMP_API\s+[\w\s\*]+?\b(gbmp_\w+)\s*\(", txt, flags=re.M)
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 18
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT (gbmp_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(lib, n)
+        assert n in _lib.SIGNATURES, f"{n} has no ctypes signature"
+
+
+def test_status_strings_and_limits():
+    lib = _lib.load()
+    assert lib.gbmp_status_string(0) == b"ok"
+    assert lib.gbmp_status_string(1) == b"invalid argument"
+    lim = _lib.Limits()
+    _lib.check(lib.gbmp_get_limits(C.byref(lim)))
+    assert lim.max_links >= 16 and lim.max_spheres >= 128
+
+
+def _desc(model, parent=None):
+    keep = [np.ascontiguousarray(model.joint_types, np.int32),
+            np.ascontiguousarray(model.joint_poses.reshape(-1, 16), np.float32),
+            np.ascontiguousarray(model.joint_axes, np.float32),
+            np.ascontiguousarray(model.parent if parent is None else parent, np.int32),
+            np.ascontiguousarray(model.sphere_link, np.int32), np.ascontiguousarray(model.sphere_pos, np.float32),
+            np.ascontiguousarray(model.sphere_r, np.float32), np.ascontiguousarray(model.active, np.uint8),
+            np.ascontiguousarray(model.lower, np.float32), np.ascontiguousarray(model.upper, np.float32),
+            np.ascontiguousarray(model.default, np.float32), np.ascontiguousarray(model.enables, np.uint8)]
+    d = _lib.RobotDesc(model.num_links, *(k.ctypes.data for k in keep[:4]), model.num_spheres,
+                       *(k.ctypes.data for k in keep[4:]), float(model.resolution))
+    return d, keep
+
+
+def test_invalid_parent_map_rejected_like_reference():
+    """SingleArmSpace.cu:63-69 throws when parent[i] >= i; the C-ABI returns
+    GBMP_ERR_INVALID_ARGUMENT with the same message."""
+    lib = _lib.load()
+    model = W.serial_arm(1, dof=3, n_spheres=6)
+    bad = model.parent.copy()
+    bad[2] = 2
+    d, keep = _desc(model, bad)
+    h = C.c_void_p()
+    st = lib.gbmp_robot_create(C.byref(d), 0, C.byref(h))
+    assert st == 1
+    assert b"Link parent link map is not valid at index 2" in lib.gbmp_last_error()
+    assert not h.value
+    with pytest.raises(_lib.GbmpError):
+        _lib.check(st)
+
+
+def test_other_invalid_descriptors():
+    lib = _lib.load()
+    model = W.serial_arm(1, dof=3, n_spheres=6)
+    d, keep = _desc(model)
+    h = C.c_void_p()
+    d.resolution = 0.0
+    assert lib.gbmp_robot_create(C.byref(d), 0, C.byref(h)) == 1
+    d.resolution = 0.02
+    d.num_links = 0
+    assert lib.gbmp_robot_create(C.byref(d), 0, C.byref(h)) == 1
+    d.num_links = 1000
+    assert lib.gbmp_robot_create(C.byref(d), 0, C.byref(h)) == 1
+    d.num_links = model.num_links
+    sl = keep[4].copy()
+    sl[0] = 99
+    d.sphere_link = sl.ctypes.data
+    assert lib.gbmp_robot_create(C.byref(d), 0, C.byref(h)) == 1
+    assert lib.gbmp_robot_create(None, 0, C.byref(h)) == 1
+    assert lib.gbmp_env_create(-1, None, None, 0, None, None, None, None, 0, None, None, None, None,
+                               C.byref(h)) == 1
+    assert lib.gbmp_env_create(1, None, None, 0, None, None, None, None, 0, None, None, None, None,
+                               C.byref(h)) == 1
+    # NULL handles are rejected, not dereferenced
+    assert lib.gbmp_check_states(None, None, None, 1, 0, None, None, None, None) == 1
+    assert lib.gbmp_check_edges(None, None, None, None, 1, 0.0, 0, None, None, None, None, None) == 1
+    assert lib.gbmp_robot_destroy(None) == 0

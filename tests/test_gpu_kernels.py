@@ -1,0 +1,182 @@
+"""Parity of the CUDA kernels (through the C-ABI) with the CPU oracle.
+
+Bars: FK link poses within 1e-5 of the FP64 oracle; collision verdicts identical for
+every state whose signed clearance exceeds 1e-4 m; costs within FP32 summation
+tolerance; step counts, lengths, interpolation, nearest-neighbour indices and
+samples bit-exact; edge first-hit indices identical wherever no state up to the
+hit lies inside the 1e-4 m clearance band.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from isaac_sim_ros2_humble_gb300 import api, workloads as W
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+BAND = 1e-4
+FK_TOL = 1e-5
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.fixture(scope="module")
+def plain():
+    robot, env, q = W.plain_check_workload(n=4096)
+    return robot, env, q, O.OracleModel(robot, env), api.Robot(robot), api.Env(env)
+
+
+@pytest.fixture(scope="module")
+def edge():
+    robot, env, qf, qt = W.edge_workload(n_edges=512)
+    return robot, env, qf, qt, O.OracleModel(robot, env), api.Robot(robot), api.Env(env)
+
+
+def test_fk_poses_and_centers(plain, edge):
+    for robot, q, m, R in ((plain[0], plain[2], plain[3], plain[4]), (edge[0], edge[2], edge[4], edge[5])):
+        n = q.shape[0]
+        poses = torch.zeros((n, robot.num_links, 16), device="cuda")
+        cen = torch.zeros((n, robot.num_spheres, 3), device="cuda")
+        api.fk(R, dev(q), poses, cen)
+        torch.cuda.synchronize()
+        p64 = m.fk(q.astype(np.float64), f64=True)
+        assert np.abs(poses.cpu().numpy() - p64).max() < FK_TOL
+        c64 = m.sphere_centers(p64)
+        assert np.abs(cen.cpu().numpy() - c64).max() < FK_TOL
+        # FP32 mirror: identical operation order, only sin/cos may differ in the last bit
+        assert np.abs(poses.cpu().numpy() - m.fk(q)).max() < 2e-6
+
+
+def _verdict_parity(m, q, verdict):
+    cl = m.clearance(q)
+    clear = np.abs(cl) > BAND
+    assert clear.mean() > 0.95
+    np.testing.assert_array_equal(verdict[clear], (cl < 0)[clear])
+
+
+def test_check_states_verdict(plain, edge):
+    for robot, q, m, R, E in ((plain[0], plain[2], plain[3], plain[4], plain[5]),
+                              (edge[0], edge[2], edge[4], edge[5], edge[6])):
+        v = torch.zeros(q.shape[0], dtype=torch.uint8, device="cuda")
+        api.check_states(R, E, dev(q), verdict=v)
+        torch.cuda.synchronize()
+        _verdict_parity(m, q, v.cpu().numpy().astype(bool))
+
+
+def test_check_states_costs(plain, edge):
+    for robot, q, m, R, E in ((plain[0], plain[2], plain[3], plain[4], plain[5]),
+                              (edge[0], edge[2], edge[4], edge[5], edge[6])):
+        n = q.shape[0]
+        costs = torch.zeros((4, n), device="cuda")
+        total = torch.zeros(n, device="cuda")
+        v = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        api.check_states(R, E, dev(q), verdict=v, costs=costs, total=total, mode=1)
+        torch.cuda.synchronize()
+        oc, ot = m.check_states(q)
+        np.testing.assert_allclose(costs.cpu().numpy(), oc, rtol=1e-4, atol=2e-5)
+        np.testing.assert_allclose(total.cpu().numpy(), ot, rtol=1e-4, atol=2e-5)
+        cl = m.clearance(q)
+        clear = np.abs(cl) > BAND
+        np.testing.assert_array_equal(v.cpu().numpy().astype(bool)[clear], (ot > 0)[clear])
+
+
+def _edge_parity(m, qf, qt, res, rule, ok, fh, ln, ns):
+    o_ok, o_fh, o_ns, o_ln = m.check_motions(qf, qt, res, rule, early_exit=True)
+    np.testing.assert_array_equal(ns, o_ns)
+    np.testing.assert_array_equal(ln, o_ln)
+    bad = np.nonzero(fh != o_fh)[0]
+    for k in bad:
+        # a disagreement is only allowed if a state up to the earlier hit is in the band
+        states = m.edge_states(qf[k], qt[k], res, rule)
+        upto = len(states) - 1 if min(fh[k], o_fh[k]) < 0 else max(fh[k], o_fh[k])
+        cl = m.clearance(states[: upto + 1])
+        assert np.any(np.abs(cl) <= BAND), (k, fh[k], o_fh[k])
+    assert len(bad) <= max(2, len(qf) // 100)
+    np.testing.assert_array_equal(ok[fh == o_fh], o_ok[fh == o_fh])
+    np.testing.assert_array_equal(ok, fh < 0)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_check_edges(edge, rule):
+    robot, env, qf, qt, m, R, E = edge
+    res = 0.05 if rule == 0 else 0.02
+    n = qf.shape[0]
+    ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    fh = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(n, device="cuda")
+    ns = torch.zeros(n, dtype=torch.int32, device="cuda")
+    api.check_edges(R, E, dev(qf), dev(qt), res, rule, ok, fh, ln, ns)
+    torch.cuda.synchronize()
+    _edge_parity(m, qf, qt, res, rule, ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(),
+                 ns.cpu().numpy())
+    assert ok.sum().item() > 0 and ok.sum().item() < n
+
+
+def test_check_edges_plain_robot_reference_rule(plain):
+    robot, env, q, m, R, E = plain
+    qf, qt = q[:256], q[256:512]
+    n = 256
+    ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    fh = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(n, device="cuda")
+    ns = torch.zeros(n, dtype=torch.int32, device="cuda")
+    api.check_edges(R, E, dev(qf), dev(qt), 0.02, 0, ok, fh, ln, ns)
+    torch.cuda.synchronize()
+    _edge_parity(m, qf, qt, 0.02, 0, ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(),
+                 ns.cpu().numpy())
+
+
+def test_edges_edge_cases(edge):
+    robot, env, qf, qt, m, R, E = edge
+    # zero-length edge (n = 1, only the goal is checked) and repeated calls reuse scratch
+    same = qf[:8].copy()
+    ok = torch.zeros(8, dtype=torch.uint8, device="cuda")
+    fh = torch.zeros(8, dtype=torch.int32, device="cuda")
+    ns = torch.zeros(8, dtype=torch.int32, device="cuda")
+    api.check_edges(R, E, dev(same), dev(same), 0.01, 0, ok, fh, None, ns)
+    torch.cuda.synchronize()
+    assert np.all(ns.cpu().numpy() == 1)
+    _, tot = m.check_states(same)
+    np.testing.assert_array_equal(ok.cpu().numpy().astype(bool), tot == 0)
+    # empty batch is a no-op
+    api.check_edges(R, E, dev(qf[:0]), dev(qt[:0]), 0.01, 0)
+    # empty environment: only self-collision remains
+    E0 = api.Env(W.Environment.empty())
+    v = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E0, dev(qf[:64]), verdict=v)
+    torch.cuda.synchronize()
+    m0 = O.OracleModel(robot, W.Environment.empty())
+    _verdict_parity(m0, qf[:64], v.cpu().numpy().astype(bool))
+
+
+def test_nearest_bit_exact(edge):
+    robot, env, qf, qt, m, R, E = edge
+    tree = np.concatenate([qf, qt])
+    qs = robot.sample_full(np.random.default_rng(9), 300)
+    out = torch.zeros(300, dtype=torch.int32, device="cuda")
+    api.nearest(R, dev(tree), dev(qs), out)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), O.nearest(tree, qs, active=robot.active))
+    cand = np.random.default_rng(3).choice(len(tree), 77, replace=False).astype(np.int32)
+    api.nearest(R, dev(tree), dev(qs), out, cand=dev(cand))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), O.nearest(tree, qs, active=robot.active, cand=cand))
+
+
+def test_steer_bit_exact(edge):
+    robot, env, qf, qt, m, R, E = edge
+    to = dev(qt)
+    api.steer(R, dev(qf), to, 0.5)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(to.cpu().numpy(), O.steer(qf, qt, 0.5))
+
+
+def test_sample_bit_exact(edge):
+    robot, env, qf, qt, m, R, E = edge
+    out = torch.zeros((1000, robot.num_links), device="cuda")
+    api.sample(R, 77, 5, out)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), O.sample(robot, 77, 5, 1000))

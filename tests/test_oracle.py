@@ -1,0 +1,181 @@
+"""CPU tests of the oracle (the checker) and of the synthetic workloads.
+
+The oracle is pinned here against independent float64 implementations and, where
+oracle/_ref has been built from the reference tree, against the reference's own
+generated kernels (tests/test_reference_pin.py)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from isaac_sim_ros2_humble_gb300 import workloads as W
+
+
+@pytest.fixture(scope="module")
+def arm7():
+    robot, env, q = W.plain_check_workload(n=512)
+    return robot, env, q, O.OracleModel(robot, env)
+
+
+@pytest.fixture(scope="module")
+def arm8():
+    robot, env, qf, qt = W.edge_workload(n_edges=64)
+    return robot, env, qf, qt, O.OracleModel(robot, env)
+
+
+def test_workloads_are_deterministic():
+    a = W.plain_check_workload(seed=3, n=16)
+    b = W.plain_check_workload(seed=3, n=16)
+    np.testing.assert_array_equal(a[2], b[2])
+    np.testing.assert_array_equal(a[0].joint_poses, b[0].joint_poses)
+    np.testing.assert_array_equal(a[1].sphere_pos, b[1].sphere_pos)
+
+
+def test_workload_shapes():
+    robot, env, q = W.plain_check_workload(n=8)
+    assert robot.num_links == 8 and robot.num_spheres == 59 and robot.dim == 7
+    assert env.counts == (32, 8, 0)
+    robot2, env2, qf, qt = W.edge_workload(n_edges=8)
+    assert robot2.num_links == 9 and robot2.num_spheres == 110 and robot2.dim == 8
+    assert robot2.joint_types[1] == W.PRISMATIC
+    assert env2.counts == (256, 64, 16)
+    assert np.all((qf >= robot2.lower) & (qf <= robot2.upper))
+
+
+def test_fk_f32_matches_f64(arm7):
+    robot, env, q, m = arm7
+    p32 = m.fk(q)
+    p64 = m.fk(q.astype(np.float64), f64=True)
+    assert np.abs(p32 - p64).max() < 1e-5
+    # last row of every pose is (0, 0, 0, 1) (KernelGenerator.h:275)
+    np.testing.assert_array_equal(p32[:, :, 12:], np.tile([0, 0, 0, 1], (q.shape[0], robot.num_links, 1)))
+
+
+def test_fk_f64_matches_independent_numpy(arm7, arm8):
+    for robot, q, m in ((arm7[0], arm7[2], arm7[3]), (arm8[0], arm8[2], arm8[4])):
+        p64 = m.fk(q.astype(np.float64), f64=True).reshape(-1, robot.num_links, 4, 4)
+        ref = W.fk_numpy(robot, q)
+        assert np.abs(p64 - ref).max() < 1e-6
+
+
+def test_sphere_centers_match_numpy(arm8):
+    robot, env, qf, qt, m = arm8
+    c = m.sphere_centers(m.fk(qf.astype(np.float64), f64=True))
+    np.testing.assert_allclose(c, W.sphere_centers_numpy(robot, qf), atol=1e-9)
+
+
+def test_self_pairs_follow_reference_rule(arm7):
+    robot, env, q, m = arm7
+    pairs = m.pairs.reshape(-1, 2)
+    assert np.all(pairs[:, 0] < pairs[:, 1])
+    li, lj = robot.sphere_link[pairs[:, 0]], robot.sphere_link[pairs[:, 1]]
+    assert np.all(li != lj)
+    assert np.all(robot.enables[li, lj] == 1)
+    s = robot.sphere_r[pairs[:, 0]] + robot.sphere_r[pairs[:, 1]]
+    np.testing.assert_array_equal(m.thr_sq, (s * s).astype(np.float32))
+    # count every admissible pair exactly once
+    S = robot.num_spheres
+    expect = sum(1 for i in range(S) for j in range(i + 1, S)
+                 if robot.sphere_link[i] != robot.sphere_link[j]
+                 and robot.enables[robot.sphere_link[i], robot.sphere_link[j]])
+    assert m.npairs == expect
+
+
+def test_costs_agree_with_clearance(arm7, arm8):
+    for robot, q, m in ((arm7[0], arm7[2], arm7[3]), (arm8[0], arm8[2], arm8[4])):
+        costs, total = m.check_states(q)
+        cl = m.clearance(q)
+        clear = np.abs(cl) > 1e-4
+        np.testing.assert_array_equal((total > 0)[clear], (cl < 0)[clear])
+        np.testing.assert_allclose(total, costs.sum(0), rtol=1e-6, atol=1e-7)
+        assert (total > 0).any() and (total == 0).any()
+
+
+def test_cost_terms_by_hand():
+    """One sphere on link 1 against one obstacle of each kind, checked by hand."""
+    robot = W.serial_arm(11, dof=1, n_spheres=1)
+    robot.sphere_pos[:] = 0.0
+    robot.sphere_r[:] = 0.1
+    robot.joint_poses[1] = np.eye(4, dtype=np.float32)
+    e = W.Environment.empty()
+    e.sphere_pos = np.array([[0.15, 0, 0]], np.float32)
+    e.sphere_r = np.array([0.1], np.float32)
+    e.box_pos = np.array([[0, 0.17, 0]], np.float32)
+    e.box_rot = np.eye(3, dtype=np.float32)[None]
+    e.box_min = np.array([[-0.1, -0.1, -0.1]], np.float32)
+    e.box_max = np.array([[0.1, 0.1, 0.1]], np.float32)
+    e.cyl_pos = np.array([[0, 0, -0.35]], np.float32)
+    e.cyl_rot = np.eye(3, dtype=np.float32)[None]
+    e.cyl_radius = np.array([0.05], np.float32)
+    e.cyl_height = np.array([0.5], np.float32)
+    m = O.OracleModel(robot, e)
+    costs, total = m.check_states(np.zeros((1, robot.num_links), np.float32))
+    assert costs[1, 0] == pytest.approx(0.05, abs=1e-6)      # 0.2 - 0.15
+    assert costs[2, 0] == pytest.approx(0.03, abs=1e-6)      # r - (0.17 - 0.1)
+    assert costs[3, 0] == pytest.approx(0.0, abs=1e-7)       # cylinder top at z = -0.1: touching
+    assert costs[0, 0] == 0.0
+
+
+def test_edge_steps_reference_rule():
+    J = 4
+    f = np.zeros(J, np.float32)
+    t = np.array([0.3, 0.4, 0, 0], np.float32)            # |d| = 0.5
+    m = O.OracleModel(W.serial_arm(5, dof=3, n_spheres=3))
+    n, d = m.edge_steps(f, t, 0.1, O.STEP_L2)
+    assert n == int(np.float32(0.5) / np.float32(0.1)) + 1
+    st = m.edge_states(f, t, 0.1, O.STEP_L2)
+    np.testing.assert_array_equal(st[0], f)
+    np.testing.assert_array_equal(st[-1], t)
+    n2, _ = m.edge_steps(f, t, 0.1, O.STEP_LINF)
+    assert n2 == int(np.float32(0.4) / np.float32(0.1)) + 1
+    # single-step edge: only the goal state is checked (KernelGenerator.h:508-516)
+    n3, _ = m.edge_steps(f, f + np.float32(1e-3), 0.1, O.STEP_L2)
+    assert n3 == 1
+    np.testing.assert_array_equal(m.edge_states(f, f + np.float32(1e-3), 0.1)[0], f + np.float32(1e-3))
+
+
+def test_check_motions_early_exit_same_outputs(arm8):
+    robot, env, qf, qt, m = arm8
+    a = m.check_motions(qf[:16], qt[:16], 0.05, O.STEP_LINF, early_exit=True)
+    b = m.check_motions(qf[:16], qt[:16], 0.05, O.STEP_LINF, early_exit=False)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    ok, hit, ns, ln = a
+    assert np.all(ok == (hit < 0))
+    np.testing.assert_allclose(ln, np.linalg.norm(qt[:16] - qf[:16], axis=1), rtol=1e-5)
+
+
+def test_nearest_matches_bruteforce():
+    rng = np.random.default_rng(0)
+    tree = rng.random((1000, 8), dtype=np.float32)
+    qs = rng.random((50, 8), dtype=np.float32)
+    act = np.ones(8, np.uint8)
+    act[0] = 0
+    out = O.nearest(tree, qs, active=act)
+    d = ((qs[:, None, 1:] - tree[None, :, 1:]) ** 2).sum(-1)
+    np.testing.assert_array_equal(out, d.argmin(1))
+    cand = rng.choice(1000, 100, replace=False).astype(np.int32)
+    out2 = O.nearest(tree, qs, active=act, cand=cand)
+    np.testing.assert_array_equal(out2, cand[d[:, cand].argmin(1)])
+
+
+def test_steer_limits_distance():
+    rng = np.random.default_rng(1)
+    f = rng.random((20, 5), dtype=np.float32)
+    t = f + rng.normal(size=(20, 5)).astype(np.float32)
+    out = O.steer(f, t, 0.3)
+    d_in = np.linalg.norm(t - f, axis=1)
+    d_out = np.linalg.norm(out - f, axis=1)
+    assert np.all(d_out <= 0.3 + 1e-5)
+    np.testing.assert_array_equal(out[d_in <= 0.3], t[d_in <= 0.3])
+
+
+def test_sampler_in_limits_and_reproducible():
+    robot = W.edge_workload(n_edges=1)[0]
+    a = O.sample(robot, 123, 0, 1000)
+    b = O.sample(robot, 123, 500, 500)
+    np.testing.assert_array_equal(a[500:], b)
+    assert np.all(a >= robot.lower) and np.all(a <= robot.upper)
+    np.testing.assert_array_equal(a[:, 0], robot.default[0])
+    # uniformity (loose): mean of the unit-range coordinate
+    u = (a[:, 2] - robot.lower[2]) / (robot.upper[2] - robot.lower[2])
+    assert abs(u.mean() - 0.5) < 0.05
