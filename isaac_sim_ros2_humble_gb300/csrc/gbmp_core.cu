@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
 }
 
 // Collision check of n states; one warp per state.
-template <bool COST>
+template <bool COST, int SPL>
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     k_check_states(DevRobot R, DevEnv E, const float *__restrict__ q, long long n,
                    unsigned char *__restrict__ verdict, float *__restrict__ costs, float *__restrict__ total) {
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
         __syncwarp();
         warp_fk(t, R.L, w, lane);
         float c[4] = {0.f, 0.f, 0.f, 0.f};
-        const bool hit = warp_collide_dispatch<COST>(t, R, E, w, lane, c);
+        const bool hit = warp_collide<SPL, COST>(t, R, E, w, lane, c);
         if (lane == 0) {
             if (COST) {
                 const float tot = ((c[0] + c[1]) + c[2]) + c[3];
@@ -149,6 +149,7 @@ __global__ void k_edge_setup(const float *__restrict__ from, const float *__rest
 // One wave of edge validation: states [b0, b1) of every live edge, one warp per state,
 // state-major order so that lower states of an edge are examined first and later ones
 // can skip once a hit is known.
+template <int SPL>
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     k_edge_wave(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
                 const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
                                   : __fmaf_rn(dir[(long long)e * R.L + j], (float)s, from[(long long)e * R.L + j]);
         __syncwarp();
         warp_fk(t, R.L, w, lane);
-        const bool hit = warp_collide_dispatch<false>(t, R, E, w, lane, nullptr);
+        const bool hit = warp_collide<SPL, false>(t, R, E, w, lane, nullptr);
         if (hit && lane == 0) atomicMin(first_hit + e, s);
         __syncwarp();
     }
@@ -266,6 +267,20 @@ static int max_edge_states() {
     for (int w = 0; w < kMaxWaves; ++w) b = wave_end(b);
     return b;
 }
+
+// Host-side dispatch on spheres per lane (each instantiation gets its own register
+// allocation).
+#define GBMP_SPL_SWITCH(spl, ...)                          \
+    switch (spl) {                                         \
+    case 1: { constexpr int SPL = 1; __VA_ARGS__; } break; \
+    case 2: { constexpr int SPL = 2; __VA_ARGS__; } break; \
+    case 3: { constexpr int SPL = 3; __VA_ARGS__; } break; \
+    case 4: { constexpr int SPL = 4; __VA_ARGS__; } break; \
+    case 5: { constexpr int SPL = 5; __VA_ARGS__; } break; \
+    case 6: { constexpr int SPL = 6; __VA_ARGS__; } break; \
+    case 7: { constexpr int SPL = 7; __VA_ARGS__; } break; \
+    default: { constexpr int SPL = 8; __VA_ARGS__; } break; \
+    }
 
 }  // namespace gbmp
 
@@ -472,7 +487,7 @@ gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_
     GBMP_CHECK_ARG(ns == 0 || (sp && sr), "sphere arrays are NULL");
     GBMP_CHECK_ARG(nb == 0 || (bp && brot && bmin && bmax), "cuboid arrays are NULL");
     GBMP_CHECK_ARG(nc == 0 || (cp && crot && crad && chei), "cylinder arrays are NULL");
-    const long long words = (long long)ns + 5LL * nb + 4LL * nc;
+    const long long words = 3LL * ns + 5LL * nb + 4LL * nc;
     if (words > kMaxEnvWords) {
         set_error("environment needs %lld float4 words, limit %d", words, kMaxEnvWords);
         return GBMP_ERR_CAPACITY;
@@ -492,6 +507,12 @@ gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_
     for (int i = 0; i < nc; ++i) {
         host_inverse_pose(cp + 3 * i, crot + 9 * i, w + 4 * i);
         w[4 * i + 3] = make_float4(crad[i], chei[i] * 0.5f, 0.f, 0.f);
+    }
+    w += 4 * nc;
+    for (int i = 0; i < ns; ++i) {
+        const double x = sp[3 * i], y = sp[3 * i + 1], z = sp[3 * i + 2], rr = sr[i];
+        w[2 * i] = make_float4(2.f * sp[3 * i], 2.f * sp[3 * i + 1], 2.f * sp[3 * i + 2], 2.f * sr[i]);
+        w[2 * i + 1] = make_float4((float)(-(x * x + y * y + z * z - rr * rr)), 0.f, 0.f, 0.f);
     }
     cudaError_t err = cudaMalloc(&e->d_words, sizeof(float4) * e->h_words.size());
     if (err == cudaSuccess)
@@ -546,19 +567,27 @@ gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int6
     GBMP_CHECK_ARG(d_q, "q is NULL");
     const DevEnv E = env->dev();
     const size_t smem = block_smem(r->dev, env_words(E.ns, E.nb, E.nc));
-    int grid = 0;
-    gbmp_status st = mode == GBMP_CHECK_COST ? persistent_grid(k_check_states<true>, smem, r->num_sms, &grid)
-                                             : persistent_grid(k_check_states<false>, smem, r->num_sms, &grid);
-    if (st) return st;
     const long long need = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    if (need < grid) grid = (int)need;
-    ProfScope ps(GBMP_PROF_CHECK_STATES, (cudaStream_t)stream);
-    if (mode == GBMP_CHECK_COST)
-        k_check_states<true><<<grid, kWarpsPerBlock * kWarp, smem, (cudaStream_t)stream>>>(r->dev, E, d_q, n, d_verdict,
-                                                                                         d_costs, d_total);
-    else
-        k_check_states<false><<<grid, kWarpsPerBlock * kWarp, smem, (cudaStream_t)stream>>>(r->dev, E, d_q, n,
-                                                                                          d_verdict, nullptr, nullptr);
+    gbmp_status st = GBMP_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    GBMP_SPL_SWITCH(r->dev.spl, {
+        int grid = 0;
+        if (mode == GBMP_CHECK_COST) {
+            st = persistent_grid(k_check_states<true, SPL>, smem, r->num_sms, &grid);
+            if (st) return st;
+            if (need < grid) grid = (int)need;
+            ProfScope ps(GBMP_PROF_CHECK_STATES, s);
+            k_check_states<true, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, E, d_q, n, d_verdict,
+                                                                                 d_costs, d_total);
+        } else {
+            st = persistent_grid(k_check_states<false, SPL>, smem, r->num_sms, &grid);
+            if (st) return st;
+            if (need < grid) grid = (int)need;
+            ProfScope ps(GBMP_PROF_CHECK_STATES, s);
+            k_check_states<false, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, E, d_q, n, d_verdict,
+                                                                                  nullptr, nullptr);
+        }
+    });
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
 }
@@ -610,7 +639,7 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     const DevEnv Ev = env->dev();
     const size_t smem = block_smem(r->dev, env_words(Ev.ns, Ev.nb, Ev.nc));
     int grid = 0;
-    st = persistent_grid(k_edge_wave, smem, r->num_sms, &grid);
+    GBMP_SPL_SWITCH(r->dev.spl, { st = persistent_grid(k_edge_wave<SPL>, smem, r->num_sms, &grid); });
     if (st) return st;
     int b0 = 0, wave = 0;
     int *live_in = liveA, *live_out = liveB;
@@ -619,8 +648,10 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
         int *cnt_in = ctr + 1 + wave, *cnt_out = ctr + 2 + wave;
         {
             ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
-            k_edge_wave<<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, Ev, d_from, d_to, nsteps, dir, fh,
-                                                                   live_in, cnt_in, b0, b1);
+            GBMP_SPL_SWITCH(r->dev.spl, {
+                k_edge_wave<SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, Ev, d_from, d_to, nsteps, dir,
+                                                                            fh, live_in, cnt_in, b0, b1);
+            });
         }
         GBMP_CUDA(cudaGetLastError());
         if (b1 < n_max) {

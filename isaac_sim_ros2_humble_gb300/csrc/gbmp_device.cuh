@@ -35,6 +35,7 @@ constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slot
 //   spheres  [ns]     (x, y, z, r)
 //   cuboids  [nb*5]   inverse pose rows 0..2, (min xyz, 0), (max xyz, 0)
 //   cylinders[nc*4]   inverse pose rows 0..2, (radius, half height, 0, 0)
+//   spheres  [ns*2]   expanded form (2x, 2y, 2z, 2r), (-(|o|^2 - r^2), 0, 0, 0)
 // ---------------------------------------------------------------------------------
 struct DevRobot {
     int L, S, P, spl;                 // spl = spheres per lane = ceil(S/32)
@@ -48,10 +49,10 @@ struct DevRobot {
 
 struct DevEnv {
     int ns, nb, nc;
-    const float4 *words;              // ns + 5*nb + 4*nc float4
+    const float4 *words;              // env_words(ns, nb, nc) float4
 };
 
-__host__ __device__ inline int env_words(int ns, int nb, int nc) { return ns + 5 * nb + 4 * nc; }
+__host__ __device__ inline int env_words(int ns, int nb, int nc) { return 3 * ns + 5 * nb + 4 * nc; }
 
 // Shared-memory staging of the robot tables and the environment.
 struct SmemTables {
@@ -139,28 +140,37 @@ __device__ __forceinline__ float mul_elem(const float *A, const float *B, int r,
     return acc;
 }
 
-// Rodrigues rotation (KernelGenerator.h:305-325), rows 0..2 of the 4x4 as 3x4.
-__device__ __forceinline__ void rot34(const float *n4, float angle, float *R) {
+// Column c (rows 0..2) of the Rodrigues rotation (KernelGenerator.h:305-325); column 3
+// is zero.  All nine entries are formed in registers and the column is selected, so
+// nothing is dynamically indexed.
+__device__ __forceinline__ float3 rot_col(const float *n4, float s, float c, int col) {
     const float nx = n4[0], ny = n4[1], nz = n4[2], valid = n4[3];
-    float s, c;
-    sincosf(angle, &s, &c);
     const float oc = __fadd_rn(1.f, -c);
     const float iv = __fadd_rn(1.f, -valid);
-    const float r0 = __fmaf_rn(__fmul_rn(nx, nx), oc, c);
-    const float r1 = __fmaf_rn(__fmul_rn(nx, ny), oc, -__fmul_rn(nz, s));
-    const float r2 = __fmaf_rn(__fmul_rn(nx, nz), oc, __fmul_rn(ny, s));
-    const float r4 = __fmaf_rn(__fmul_rn(ny, nx), oc, __fmul_rn(nz, s));
-    const float r5 = __fmaf_rn(__fmul_rn(ny, ny), oc, c);
-    const float r6 = __fmaf_rn(__fmul_rn(ny, nz), oc, -__fmul_rn(nx, s));
-    const float r8 = __fmaf_rn(__fmul_rn(nz, nx), oc, -__fmul_rn(ny, s));
-    const float r9 = __fmaf_rn(__fmul_rn(nz, ny), oc, __fmul_rn(nx, s));
-    const float r10 = __fmaf_rn(__fmul_rn(nz, nz), oc, c);
-    R[0] = __fadd_rn(__fmul_rn(r0, valid), iv); R[1] = __fmul_rn(r1, valid);
-    R[2] = __fmul_rn(r2, valid); R[3] = 0.f;
-    R[4] = __fmul_rn(r4, valid); R[5] = __fadd_rn(__fmul_rn(r5, valid), iv);
-    R[6] = __fmul_rn(r6, valid); R[7] = 0.f;
-    R[8] = __fmul_rn(r8, valid); R[9] = __fmul_rn(r9, valid);
-    R[10] = __fadd_rn(__fmul_rn(r10, valid), iv); R[11] = 0.f;
+    const float r0 = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(nx, nx), oc, c), valid), iv);
+    const float r1 = __fmul_rn(__fmaf_rn(__fmul_rn(nx, ny), oc, -__fmul_rn(nz, s)), valid);
+    const float r2 = __fmul_rn(__fmaf_rn(__fmul_rn(nx, nz), oc, __fmul_rn(ny, s)), valid);
+    const float r4 = __fmul_rn(__fmaf_rn(__fmul_rn(ny, nx), oc, __fmul_rn(nz, s)), valid);
+    const float r5 = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(ny, ny), oc, c), valid), iv);
+    const float r6 = __fmul_rn(__fmaf_rn(__fmul_rn(ny, nz), oc, -__fmul_rn(nx, s)), valid);
+    const float r8 = __fmul_rn(__fmaf_rn(__fmul_rn(nz, nx), oc, -__fmul_rn(ny, s)), valid);
+    const float r9 = __fmul_rn(__fmaf_rn(__fmul_rn(nz, ny), oc, __fmul_rn(nx, s)), valid);
+    const float r10 = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(nz, nz), oc, c), valid), iv);
+    float3 o;
+    o.x = col == 0 ? r0 : (col == 1 ? r1 : (col == 2 ? r2 : 0.f));
+    o.y = col == 0 ? r4 : (col == 1 ? r5 : (col == 2 ? r6 : 0.f));
+    o.z = col == 0 ? r8 : (col == 1 ? r9 : (col == 2 ? r10 : 0.f));
+    return o;
+}
+
+// Element (r, c) of A * B where B is given by its column c (rows 0..2), same
+// operation order as mul_elem.
+__device__ __forceinline__ float mul_col(const float *A, float3 bc, int r, int c) {
+    float acc = __fmul_rn(A[4 * r + 0], bc.x);
+    acc = __fmaf_rn(A[4 * r + 1], bc.y, acc);
+    acc = __fmaf_rn(A[4 * r + 2], bc.z, acc);
+    if (c == 3) acc = __fadd_rn(acc, A[4 * r + 3]);
+    return acc;
 }
 
 // FK of the state in w.q into w.lp.  All lanes of the warp must call it.
@@ -175,19 +185,28 @@ __device__ inline void warp_fk(const SmemTables &t, int L, const WarpScratch &w,
         const float *Jp = t.jl + 12 * i;
         float *out = w.lp + 12 * i;
         if (ty == 1) {                               // revolute: (parent * pose) * R
-            float Rm[12];
-            rot34(t.axn + 4 * i, w.q[i], Rm);
-            if (own) w.tmp[lane] = mul_elem(A, Jp, r, c);
-            __syncwarp();
-            if (own) out[lane] = mul_elem(w.tmp, Rm, r, c);
+            if (own) {
+                float sn, cs;
+                sincosf(w.q[i], &sn, &cs);
+                const float3 rc = rot_col(t.axn + 4 * i, sn, cs, c);
+                w.tmp[lane] = mul_elem(A, Jp, r, c);
+                __syncwarp(0xfffu);
+                out[lane] = mul_col(w.tmp, rc, r, c);
+            }
         } else if (ty == 2) {                        // prismatic: parent * (pose * T)
-            const float qi = w.q[i];
-            const float *a = t.axr + 4 * i;
-            float T[12] = {1.f, 0.f, 0.f, __fmul_rn(a[0], qi), 0.f, 1.f, 0.f, __fmul_rn(a[1], qi),
-                           0.f, 0.f, 1.f, __fmul_rn(a[2], qi)};
-            if (own) w.tmp[lane] = mul_elem(Jp, T, r, c);
-            __syncwarp();
-            if (own) out[lane] = mul_elem(A, w.tmp, r, c);
+            if (own) {
+                const float qi = w.q[i];
+                const float *a = t.axr + 4 * i;
+                float3 tc;
+                if (c == 3) {
+                    tc = make_float3(__fmul_rn(a[0], qi), __fmul_rn(a[1], qi), __fmul_rn(a[2], qi));
+                } else {
+                    tc = make_float3(c == 0 ? 1.f : 0.f, c == 1 ? 1.f : 0.f, c == 2 ? 1.f : 0.f);
+                }
+                w.tmp[lane] = mul_col(Jp, tc, r, c);
+                __syncwarp(0xfffu);
+                out[lane] = mul_elem(A, w.tmp, r, c);
+            }
         } else if (ty == 5) {                        // fixed: parent * pose
             if (own) out[lane] = mul_elem(A, Jp, r, c);
         } else {                                     // unsupported: identity
@@ -249,20 +268,39 @@ __device__ inline bool warp_collide(const SmemTables &t, const DevRobot &R, cons
     const float4 *env = t.env;
 
     // --- environment spheres ---
-    for (int o0 = 0; o0 < E.ns; o0 += 8) {
-        const int oe = min(o0 + 8, E.ns);
-        for (int o = o0; o < oe; ++o) {
+    if (COST) {
+        for (int o = 0; o < E.ns; ++o) {
             const float4 b = env[o];
 #pragma unroll
             for (int m = 0; m < SPL; ++m) {
                 const float d2 = sq3(cx[m] - b.x, cy[m] - b.y, cz[m] - b.z);
                 const float rr = cr[m] + b.w;
-                const bool h = d2 < rr * rr;
-                if (COST) { if (h) c_sph += fmaxf(0.f, rr - sqrtf(d2)); }
-                hit |= h;
+                if (d2 < rr * rr) c_sph += fmaxf(0.f, rr - sqrtf(d2));
             }
         }
-        if (!COST && __any_sync(kFull, hit)) return true;
+    } else {
+        // Expanded form: d^2 - (rs + ro)^2 = A + B - 2 (c.o + rs ro) with A = |c|^2 - rs^2
+        // per robot sphere and B = |o|^2 - ro^2 per obstacle (staged as (2o, 2ro, -B)),
+        // so a test is four FMAs and a compare.  Rounding moves the contact surface by
+        // ~1e-5 m at workspace scale.
+        float A[SPL];
+#pragma unroll
+        for (int m = 0; m < SPL; ++m) A[m] = __fmaf_rn(cz[m], cz[m], __fmaf_rn(cy[m], cy[m], __fmaf_rn(cx[m], cx[m], -cr[m] * cr[m])));
+        const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
+        for (int o0 = 0; o0 < E.ns; o0 += 16) {
+            const int oe = min(o0 + 16, E.ns);
+#pragma unroll 4
+            for (int o = o0; o < oe; ++o) {
+                const float4 b = sx[2 * o];
+                const float nb = sx[2 * o + 1].x;
+#pragma unroll
+                for (int m = 0; m < SPL; ++m) {
+                    const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
+                    hit |= v > A[m];
+                }
+            }
+            if (__any_sync(kFull, hit)) return true;
+        }
     }
     env += E.ns;
 
