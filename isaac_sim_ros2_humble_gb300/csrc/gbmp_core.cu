@@ -1,5 +1,6 @@
 // gbmp_core.cu -- robot / environment handles, FK, state checks and edge
 // validation kernels of libgbmp, and their C-ABI entry points.
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -23,7 +24,7 @@ void set_error(const char *fmt, ...) {
 // Launch helpers.
 // ---------------------------------------------------------------------------------
 static size_t block_smem(const DevRobot &R, int nwords) {
-    return smem_tables_bytes(R.L, R.S, nwords) + smem_warp_bytes(R.L, R.S) * kWarpsPerBlock;
+    return smem_tables_bytes(R, nwords) + smem_warp_bytes(R) * kWarpsPerBlock;
 }
 
 template <typename K>
@@ -56,9 +57,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
          float *__restrict__ centers) {
     extern __shared__ __align__(16) unsigned char smem[];
     DevEnv E{0, 0, 0, nullptr};
-    SmemTables t = carve_tables(smem, R.L, R.S, 0);
+    SmemTables t = carve_tables(smem, R, 0);
     stage_tables(R, E, t, 0);
-    WarpScratch w = carve_warp(smem + smem_tables_bytes(R.L, R.S, 0), R.L, R.S, threadIdx.x / kWarp);
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R, 0), R, threadIdx.x / kWarp);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long nw = (long long)gridDim.x * kWarpsPerBlock;
@@ -92,9 +93,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
                    unsigned char *__restrict__ verdict, float *__restrict__ costs, float *__restrict__ total) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
-    SmemTables t = carve_tables(smem, R.L, R.S, nwords);
+    SmemTables t = carve_tables(smem, R, nwords);
     stage_tables(R, E, t, nwords);
-    WarpScratch w = carve_warp(smem + smem_tables_bytes(R.L, R.S, nwords), R.L, R.S, threadIdx.x / kWarp);
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R, nwords), R, threadIdx.x / kWarp);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long nw = (long long)gridDim.x * kWarpsPerBlock;
@@ -103,7 +104,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
         __syncwarp();
         warp_fk(t, R.L, w, lane);
         float c[4] = {0.f, 0.f, 0.f, 0.f};
-        const bool hit = warp_collide<SPL, COST>(t, R, E, w, lane, c);
+        const bool hit = (!COST && R.cull) ? warp_collide_culled<SPL>(t, R, E, w, lane)
+                                           : warp_collide<SPL, COST>(t, R, E, w, lane, c);
         if (lane == 0) {
             if (COST) {
                 const float tot = ((c[0] + c[1]) + c[2]) + c[3];
@@ -149,16 +151,16 @@ __global__ void k_edge_setup(const float *__restrict__ from, const float *__rest
 // One wave of edge validation: states [b0, b1) of every live edge, one warp per state,
 // state-major order so that lower states of an edge are examined first and later ones
 // can skip once a hit is known.
-template <int SPL>
-__global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
+template <int SPL, bool CULL>
+__global__ void __launch_bounds__(kWarpsPerBlock *kWarp, CULL ? 3 : 1)
     k_edge_wave(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
                 const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
                 const int *__restrict__ live, const int *__restrict__ live_count, int b0, int b1) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
-    SmemTables t = carve_tables(smem, R.L, R.S, nwords);
+    SmemTables t = carve_tables(smem, R, nwords);
     stage_tables(R, E, t, nwords);
-    WarpScratch w = carve_warp(smem + smem_tables_bytes(R.L, R.S, nwords), R.L, R.S, threadIdx.x / kWarp);
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R, nwords), R, threadIdx.x / kWarp);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long count = *live_count;
@@ -181,7 +183,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
                                   : __fmaf_rn(dir[(long long)e * R.L + j], (float)s, from[(long long)e * R.L + j]);
         __syncwarp();
         warp_fk(t, R.L, w, lane);
-        const bool hit = warp_collide<SPL, false>(t, R, E, w, lane, nullptr);
+        const bool hit = CULL ? warp_collide_culled<SPL>(t, R, E, w, lane)
+                              : warp_collide<SPL, false>(t, R, E, w, lane, nullptr);
         if (hit && lane == 0) atomicMin(first_hit + e, s);
         __syncwarp();
     }
@@ -405,15 +408,62 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
         sph[4 * k] = r->sph_pos[3 * k]; sph[4 * k + 1] = r->sph_pos[3 * k + 1];
         sph[4 * k + 2] = r->sph_pos[3 * k + 2]; sph[4 * k + 3] = r->sph_r[k];
     }
+    // Sphere groups (links that carry spheres, in link order) and their bounding spheres.
+    std::vector<int> link2grp(L, -1), glink, sgrp(S ? S : 1, 0);
+    for (int l = 0; l < L; ++l)
+        for (int k = 0; k < S; ++k)
+            if (r->slink[k] == l) { link2grp[l] = (int)glink.size(); glink.push_back(l); break; }
+    const int G = (int)glink.size();
+    for (int k = 0; k < S; ++k) sgrp[k] = link2grp[r->slink[k]];
+    std::vector<float> grp(4 * (G ? G : 1), 0.f);
+    for (int g = 0; g < G; ++g) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int k = 0; k < S; ++k)
+            if (sgrp[k] == g)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], (double)r->sph_pos[3 * k + a] - r->sph_r[k]);
+                    hi[a] = std::max(hi[a], (double)r->sph_pos[3 * k + a] + r->sph_r[k]);
+                }
+        double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])}, rad = 0.0;
+        for (int k = 0; k < S; ++k)
+            if (sgrp[k] == g) {
+                double d2 = 0.0;
+                for (int a = 0; a < 3; ++a) d2 += (r->sph_pos[3 * k + a] - c[a]) * (r->sph_pos[3 * k + a] - c[a]);
+                rad = std::max(rad, std::sqrt(d2) + r->sph_r[k]);
+            }
+        for (int a = 0; a < 3; ++a) grp[4 * g + a] = (float)c[a];
+        grp[4 * g + 3] = nextafterf((float)(rad + kBroadMargin), 1e30f);
+    }
+    // Device pair list sorted by group pair; each enabled group pair owns a range.
+    std::vector<int> order(r->P);
+    for (int p = 0; p < r->P; ++p) order[p] = p;
+    auto key = [&](int p) {
+        const int a = sgrp[r->pairs[2 * p]], b = sgrp[r->pairs[2 * p + 1]];
+        return std::make_pair(std::min(a, b), std::max(a, b));
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
     std::vector<unsigned> packed(r->P);
-    for (int p = 0; p < r->P; ++p) packed[p] = (unsigned)r->pairs[2 * p] | ((unsigned)r->pairs[2 * p + 1] << 16);
+    std::vector<float> thr_sorted(r->P);
+    std::vector<int> lpair;
+    for (int q = 0; q < r->P; ++q) {
+        const int p = order[q];
+        packed[q] = (unsigned)r->pairs[2 * p] | ((unsigned)r->pairs[2 * p + 1] << 16);
+        thr_sorted[q] = r->thr[p];
+        if (q == 0 || key(p) != key(order[q - 1])) {
+            lpair.insert(lpair.end(), {key(p).first, key(p).second, q, q});
+        }
+        lpair.back() = q + 1;
+    }
+    const int NPL = (int)lpair.size() / 4;
     size_t o_jl = put(jl.data(), jl.size() * 4), o_axn = put(axn.data(), axn.size() * 4);
     size_t o_axr = put(axr.data(), axr.size() * 4), o_sph = put(sph.data(), 4 * 4 * (size_t)S);
     size_t o_type = put(r->type.data(), 4 * L), o_par = put(r->parent.data(), 4 * L);
     size_t o_sl = put(r->slink.data(), 4 * (size_t)S);
-    size_t o_pairs = put(packed.data(), 4 * (size_t)r->P), o_thr = put(r->thr.data(), 4 * (size_t)r->P);
+    size_t o_pairs = put(packed.data(), 4 * (size_t)r->P), o_thr = put(thr_sorted.data(), 4 * (size_t)r->P);
     size_t o_lo = put(r->lower.data(), 4 * L), o_up = put(r->upper.data(), 4 * L);
     size_t o_def = put(r->defv.data(), 4 * L), o_act = put(r->active.data(), L);
+    size_t o_grp = put(grp.data(), 4 * 4 * (size_t)G), o_glink = put(glink.data(), 4 * (size_t)G);
+    size_t o_sgrp = put(sgrp.data(), 4 * (size_t)S), o_lpair = put(lpair.data(), 4 * lpair.size());
 
     int dev = 0;
     r->num_sms = current_device_sms(&dev);
@@ -438,6 +488,9 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     D.slink = (const int *)(b + o_sl); D.pairs = (const unsigned *)(b + o_pairs); D.thr = (const float *)(b + o_thr);
     D.lower = (const float *)(b + o_lo); D.upper = (const float *)(b + o_up); D.defv = (const float *)(b + o_def);
     D.active = (const unsigned char *)(b + o_act);
+    D.G = G; D.NPL = NPL; D.cull = (G <= kMaxGroups) ? 1 : 0;
+    D.grp = (const float *)(b + o_grp); D.glink = (const int *)(b + o_glink);
+    D.sgrp = (const int *)(b + o_sgrp); D.lpair = (const int4 *)(b + o_lpair);
     (void)flags;
     *out = r;
     return GBMP_OK;
@@ -546,7 +599,7 @@ gbmp_status gbmp_fk(gbmp_robot r, const float *d_q, int64_t n, float *d_poses, f
     GBMP_CHECK_ARG(n >= 0, "n < 0");
     if (n == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_q, "q is NULL");
-    const size_t smem = smem_tables_bytes(r->L, r->S, 0) + smem_warp_bytes(r->L, r->S) * kWarpsPerBlock;
+    const size_t smem = smem_tables_bytes(r->dev, 0) + smem_warp_bytes(r->dev) * kWarpsPerBlock;
     int grid = 0;
     gbmp_status st = persistent_grid(k_fk, smem, r->num_sms, &grid);
     if (st) return st;
@@ -639,7 +692,11 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     const DevEnv Ev = env->dev();
     const size_t smem = block_smem(r->dev, env_words(Ev.ns, Ev.nb, Ev.nc));
     int grid = 0;
-    GBMP_SPL_SWITCH(r->dev.spl, { st = persistent_grid(k_edge_wave<SPL>, smem, r->num_sms, &grid); });
+    const bool cull = r->dev.cull != 0;
+    GBMP_SPL_SWITCH(r->dev.spl, {
+        st = cull ? persistent_grid(k_edge_wave<SPL, true>, smem, r->num_sms, &grid)
+                  : persistent_grid(k_edge_wave<SPL, false>, smem, r->num_sms, &grid);
+    });
     if (st) return st;
     int b0 = 0, wave = 0;
     int *live_in = liveA, *live_out = liveB;
@@ -649,8 +706,12 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
         {
             ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
             GBMP_SPL_SWITCH(r->dev.spl, {
-                k_edge_wave<SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, Ev, d_from, d_to, nsteps, dir,
-                                                                            fh, live_in, cnt_in, b0, b1);
+                if (cull)
+                    k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                        r->dev, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+                else
+                    k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                        r->dev, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
             });
         }
         GBMP_CUDA(cudaGetLastError());

@@ -30,7 +30,11 @@ constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slot
 //   axr   [L*4]   raw axis (prismatic translation uses it unnormalised, :349-354)
 //   sph   [S*4]   sphere (x, y, z, r) in its link frame
 //   type  [L], parent [L], slink [S] (int32)
-//   pairs [P] packed (i | j << 16), thr [P] squared distance thresholds
+//   pairs [P] packed (i | j << 16), thr [P] squared distance thresholds, sorted by
+//         link pair so that each enabled link pair owns a contiguous range
+//   grp   [G*4]  per sphere-carrying link ("group"): bounding sphere (x, y, z, R) in the
+//         link frame enclosing all its spheres, inflated by kBroadMargin
+//   glink [G], sgrp [S] (group of each sphere), lpair [NPL*4] (ga, gb, p0, p1)
 // Environment words (float4):
 //   spheres  [ns]     (x, y, z, r)
 //   cuboids  [nb*5]   inverse pose rows 0..2, (min xyz, 0), (max xyz, 0)
@@ -39,13 +43,21 @@ constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slot
 // ---------------------------------------------------------------------------------
 struct DevRobot {
     int L, S, P, spl;                 // spl = spheres per lane = ceil(S/32)
+    int G, NPL;                       // sphere groups, enabled group pairs
+    int cull;                         // 1: groups fit a 32-bit mask, broad phase available
     const float *jl, *axn, *axr, *sph;
     const int *type, *parent, *slink;
     const unsigned *pairs;
     const float *thr;
     const float *lower, *upper, *defv;
     const unsigned char *active;
+    const float *grp;
+    const int *glink, *sgrp;
+    const int4 *lpair;
 };
+
+constexpr int kMaxGroups = 32;
+constexpr float kBroadMargin = 1e-3f;    // metres added to every group bounding radius
 
 struct DevEnv {
     int ns, nb, nc;
@@ -59,26 +71,35 @@ struct SmemTables {
     float *jl, *axn, *axr;
     float4 *sph;
     int *type, *parent, *slink;
+    float4 *grp;
+    int *glink, *sgrp;
+    int4 *lpair;
     float4 *env;                      // staged environment words
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline size_t smem_tables_bytes(int L, int S, int nwords) {
+__host__ __device__ inline size_t smem_tables_bytes(const DevRobot &R, int nwords) {
     size_t b = 0;
-    b += align16(sizeof(float) * 12 * L);
-    b += align16(sizeof(float) * 4 * L) * 2;
-    b += align16(sizeof(float4) * S);
-    b += align16(sizeof(int) * L) * 2;
-    b += align16(sizeof(int) * S);
+    b += align16(sizeof(float) * 12 * R.L);
+    b += align16(sizeof(float) * 4 * R.L) * 2;
+    b += align16(sizeof(float4) * R.S);
+    b += align16(sizeof(int) * R.L) * 2;
+    b += align16(sizeof(int) * R.S);
+    b += align16(sizeof(float4) * R.G);
+    b += align16(sizeof(int) * R.G);
+    b += align16(sizeof(int) * R.S);
+    b += align16(sizeof(int4) * R.NPL);
     b += align16(sizeof(float4) * nwords);
     return b;
 }
 
-// Per-warp scratch: link poses [L*12], temp [16], joint state [L], sphere centres [S].
-__host__ __device__ inline size_t smem_warp_bytes(int L, int S) {
-    return align16(sizeof(float) * 12 * L) + align16(sizeof(float) * 16) + align16(sizeof(float) * L) +
-           align16(sizeof(float4) * S);
+// Per-warp scratch: link poses [L*12], temp [16], joint state [L], sphere centres [S],
+// group bounding spheres in the base frame [G] + their A terms [G], candidate list [32].
+__host__ __device__ inline size_t smem_warp_bytes(const DevRobot &R) {
+    return align16(sizeof(float) * 12 * R.L) + align16(sizeof(float) * 16) + align16(sizeof(float) * R.L) +
+           align16(sizeof(float4) * R.S) + align16(sizeof(float4) * R.G) + align16(sizeof(float) * R.G) +
+           align16(sizeof(int) * kWarp) * 2;
 }
 
 struct WarpScratch {
@@ -86,31 +107,43 @@ struct WarpScratch {
     float *tmp;     // 12-element temporary
     float *q;       // joint values of the state under test
     float4 *cen;    // sphere centres (x, y, z, r)
+    float4 *gb;     // group bounding spheres in the base frame (x, y, z, R)
+    float *gA;      // |c|^2 - R^2 of each group sphere
+    int *cand;      // candidate obstacle indices of the current chunk
+    unsigned *cmask;// their group masks
 };
 
-__device__ inline SmemTables carve_tables(unsigned char *base, int L, int S, int nwords) {
+__device__ inline SmemTables carve_tables(unsigned char *base, const DevRobot &R, int nwords) {
     SmemTables t;
     size_t off = 0;
-    t.jl = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 12 * L);
-    t.axn = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 4 * L);
-    t.axr = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 4 * L);
-    t.sph = reinterpret_cast<float4 *>(base + off); off += align16(sizeof(float4) * S);
-    t.type = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * L);
-    t.parent = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * L);
-    t.slink = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * S);
+    t.jl = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 12 * R.L);
+    t.axn = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 4 * R.L);
+    t.axr = reinterpret_cast<float *>(base + off); off += align16(sizeof(float) * 4 * R.L);
+    t.sph = reinterpret_cast<float4 *>(base + off); off += align16(sizeof(float4) * R.S);
+    t.type = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.L);
+    t.parent = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.L);
+    t.slink = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.S);
+    t.grp = reinterpret_cast<float4 *>(base + off); off += align16(sizeof(float4) * R.G);
+    t.glink = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.G);
+    t.sgrp = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.S);
+    t.lpair = reinterpret_cast<int4 *>(base + off); off += align16(sizeof(int4) * R.NPL);
     t.env = reinterpret_cast<float4 *>(base + off);
     return t;
 }
 
-__device__ inline WarpScratch carve_warp(unsigned char *base, int L, int S, int warp) {
-    size_t per = smem_warp_bytes(L, S);
+__device__ inline WarpScratch carve_warp(unsigned char *base, const DevRobot &R, int warp) {
+    size_t per = smem_warp_bytes(R);
     unsigned char *p = base + per * warp;
     WarpScratch w;
     size_t off = 0;
-    w.lp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * L);
+    w.lp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L);
     w.tmp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 16);
-    w.q = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * L);
-    w.cen = reinterpret_cast<float4 *>(p + off);
+    w.q = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * R.L);
+    w.cen = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.S);
+    w.gb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.G);
+    w.gA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * R.G);
+    w.cand = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * kWarp);
+    w.cmask = reinterpret_cast<unsigned *>(p + off);
     return w;
 }
 
@@ -122,8 +155,14 @@ __device__ inline void stage_tables(const DevRobot &R, const DevEnv &E, const Sm
     for (int i = tid; i < R.S; i += nt) {
         t.sph[i] = reinterpret_cast<const float4 *>(R.sph)[i];
         t.slink[i] = R.slink[i];
+        t.sgrp[i] = R.sgrp[i];
     }
     for (int i = tid; i < R.L; i += nt) { t.type[i] = R.type[i]; t.parent[i] = R.parent[i]; }
+    for (int i = tid; i < R.G; i += nt) {
+        t.grp[i] = reinterpret_cast<const float4 *>(R.grp)[i];
+        t.glink[i] = R.glink[i];
+    }
+    for (int i = tid; i < R.NPL; i += nt) t.lpair[i] = R.lpair[i];
     for (int i = tid; i < nwords; i += nt) t.env[i] = E.words[i];
 }
 
@@ -377,6 +416,190 @@ __device__ inline bool warp_collide(const SmemTables &t, const DevRobot &R, cons
         costs[0] = c_self; costs[1] = c_sph; costs[2] = c_box; costs[3] = c_cyl;
     }
     return __any_sync(kFull, hit);
+}
+
+// ---------------------------------------------------------------------------------
+// Verdict-only collision with a broad phase.  Every sphere-carrying link ("group") has
+// a bounding sphere that encloses its collision spheres plus kBroadMargin.  Obstacles
+// are taken 32 at a time, one per lane; each lane tests its obstacle against every
+// group bounding sphere and keeps a mask of overlapping groups.  Obstacles with a
+// non-empty mask are compacted (ballot + popc) into a per-warp candidate list, and
+// only the robot spheres of the overlapping groups are tested against them with the
+// exact per-sphere formulas.  Self-collision uses the group-pair ranges of the sorted
+// pair list the same way.  The broad tests are conservative (a sphere inside its group
+// sphere cannot touch an obstacle the group sphere misses, and every distance function
+// used is 1-Lipschitz), so the verdict equals that of warp_collide up to floating-point
+// rounding at the contact surface.
+// ---------------------------------------------------------------------------------
+template <int SPL>
+__device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &R, const DevEnv &E,
+                                           const WarpScratch &w, int lane) {
+    float cx[SPL], cy[SPL], cz[SPL], cr[SPL], A[SPL];
+    unsigned gbit[SPL];
+#pragma unroll
+    for (int m = 0; m < SPL; ++m) {
+        const int k = lane + kWarp * m;
+        if (k < R.S) {
+            const float4 s = t.sph[k];
+            const float3 p = xform_point(w.lp + 12 * t.slink[k], s.x, s.y, s.z);
+            cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
+            gbit[m] = 1u << t.sgrp[k];
+            w.cen[k] = make_float4(p.x, p.y, p.z, s.w);
+        } else {
+            cx[m] = kFar; cy[m] = kFar; cz[m] = kFar; cr[m] = 0.f;
+            gbit[m] = 0u;
+        }
+        A[m] = __fmaf_rn(cz[m], cz[m], __fmaf_rn(cy[m], cy[m], __fmaf_rn(cx[m], cx[m], -cr[m] * cr[m])));
+    }
+    if (lane < R.G) {
+        const float4 g = t.grp[lane];
+        const float3 c = xform_point(w.lp + 12 * t.glink[lane], g.x, g.y, g.z);
+        w.gb[lane] = make_float4(c.x, c.y, c.z, g.w);
+        w.gA[lane] = __fmaf_rn(c.z, c.z, __fmaf_rn(c.y, c.y, __fmaf_rn(c.x, c.x, -g.w * g.w)));
+    }
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    bool hit = false;
+
+    // --- environment spheres (expanded form, see warp_collide) ---
+    const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
+    for (int o0 = 0; o0 < E.ns; o0 += kWarp) {
+        const int o = o0 + lane;
+        unsigned mask = 0u;
+        if (o < E.ns) {
+            const float4 b = sx[2 * o];
+            const float nb = sx[2 * o + 1].x;
+            for (int g = 0; g < R.G; ++g) {
+                const float4 gs = w.gb[g];
+                const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
+                if (v > w.gA[g]) mask |= 1u << g;
+            }
+        }
+        const unsigned bal = __ballot_sync(kFull, mask != 0u);
+        if (mask) { const int pos = __popc(bal & lt); w.cand[pos] = o; w.cmask[pos] = mask; }
+        __syncwarp();
+        const int nc = __popc(bal);
+        for (int i = 0; i < nc; ++i) {
+            const int oc = w.cand[i];
+            const unsigned cm = w.cmask[i];
+            const float4 b = sx[2 * oc];
+            const float nb = sx[2 * oc + 1].x;
+#pragma unroll
+            for (int m = 0; m < SPL; ++m) {
+                const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
+                hit |= (cm & gbit[m]) && v > A[m];
+            }
+        }
+        if (__any_sync(kFull, hit)) return true;
+    }
+
+    // --- cuboids ---
+    const float4 *bx = t.env + E.ns;
+    for (int o0 = 0; o0 < E.nb; o0 += kWarp) {
+        const int o = o0 + lane;
+        unsigned mask = 0u;
+        if (o < E.nb) {
+            const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
+            for (int g = 0; g < R.G; ++g) {
+                const float4 gs = w.gb[g];
+                const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                if (sq3(dx, dy, dz) < gs.w * gs.w) mask |= 1u << g;
+            }
+        }
+        const unsigned bal = __ballot_sync(kFull, mask != 0u);
+        if (mask) { const int pos = __popc(bal & lt); w.cand[pos] = o; w.cmask[pos] = mask; }
+        __syncwarp();
+        const int nc = __popc(bal);
+        for (int i = 0; i < nc; ++i) {
+            const int oc = w.cand[i];
+            const unsigned cm = w.cmask[i];
+            const float4 r0 = bx[5 * oc], r1 = bx[5 * oc + 1], r2 = bx[5 * oc + 2], mn = bx[5 * oc + 3], mx = bx[5 * oc + 4];
+#pragma unroll
+            for (int m = 0; m < SPL; ++m) {
+                if (cm & gbit[m]) {
+                    const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
+                    const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                    const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                    const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                    hit |= sq3(dx, dy, dz) < cr[m] * cr[m];
+                }
+            }
+        }
+        if (__any_sync(kFull, hit)) return true;
+    }
+
+    // --- cylinders ---
+    const float4 *cyl = t.env + E.ns + 5 * E.nb;
+    for (int o0 = 0; o0 < E.nc; o0 += kWarp) {
+        const int o = o0 + lane;
+        unsigned mask = 0u;
+        if (o < E.nc) {
+            const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
+            for (int g = 0; g < R.G; ++g) {
+                const float4 gs = w.gb[g];
+                const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
+                const float dz = fabsf(l.z) - pr.y;
+                const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                const float sdf = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox))) + fminf(fmaxf(dx, dz), 0.f);
+                if (gs.w - sdf > 0.f) mask |= 1u << g;
+            }
+        }
+        const unsigned bal = __ballot_sync(kFull, mask != 0u);
+        if (mask) { const int pos = __popc(bal & lt); w.cand[pos] = o; w.cmask[pos] = mask; }
+        __syncwarp();
+        const int nc = __popc(bal);
+        for (int i = 0; i < nc; ++i) {
+            const int oc = w.cand[i];
+            const unsigned cm = w.cmask[i];
+            const float4 r0 = cyl[4 * oc], r1 = cyl[4 * oc + 1], r2 = cyl[4 * oc + 2], pr = cyl[4 * oc + 3];
+#pragma unroll
+            for (int m = 0; m < SPL; ++m) {
+                if (cm & gbit[m]) {
+                    const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
+                    const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
+                    const float dz = fabsf(l.z) - pr.y;
+                    const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                    const float outside = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox)));
+                    const float inside = fminf(fmaxf(dx, dz), 0.f);
+                    hit |= cr[m] - (outside + inside) > 0.f;
+                }
+            }
+        }
+        if (__any_sync(kFull, hit)) return true;
+    }
+
+    // --- self collision: group pairs whose bounding spheres overlap ---
+    for (int k0 = 0; k0 < R.NPL; k0 += kWarp) {
+        const int k = k0 + lane;
+        bool on = false;
+        int p0 = 0, p1 = 0;
+        if (k < R.NPL) {
+            const int4 lp = t.lpair[k];
+            const float4 a = w.gb[lp.x], b = w.gb[lp.y];
+            const float rr = a.w + b.w;
+            on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
+            p0 = lp.z;
+            p1 = lp.w;
+        }
+        unsigned bal = __ballot_sync(kFull, on);
+        while (bal) {
+            const int j = __ffs(bal) - 1;
+            bal &= bal - 1u;
+            const int q0 = __shfl_sync(kFull, p0, j), q1 = __shfl_sync(kFull, p1, j);
+            for (int p = q0 + lane; p < q1; p += kWarp) {
+                const unsigned ij = __ldg(R.pairs + p);
+                const float thr = __ldg(R.thr + p);
+                const float4 a = w.cen[ij & 0xffffu], b = w.cen[ij >> 16];
+                hit |= sq3(a.x - b.x, a.y - b.y, a.z - b.z) < thr;
+            }
+            if (__any_sync(kFull, hit)) return true;
+        }
+    }
+    return false;
 }
 
 // Dispatch on spheres-per-lane.

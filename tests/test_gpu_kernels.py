@@ -180,3 +180,26 @@ def test_sample_bit_exact(edge):
     api.sample(R, 77, 5, out)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), O.sample(robot, 77, 5, 1000))
+
+
+def test_many_links_uses_full_path():
+    """More than 32 sphere-carrying links: the broad phase is off and every pair is
+    tested; verdicts still match the oracle."""
+    robot = W.serial_arm(4, dof=40, n_spheres=80, offset_range=(0.03, 0.06), radius_range=(0.01, 0.02))
+    env = W.random_env(8, 24, 6, 4, oriented=True)
+    R, E = api.Robot(robot), api.Env(env)
+    m = O.OracleModel(robot, env)
+    q = robot.sample_full(np.random.default_rng(1), 512)
+    v = torch.zeros(512, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E, dev(q), verdict=v)
+    torch.cuda.synchronize()
+    _verdict_parity(m, q, v.cpu().numpy().astype(bool))
+    qf, qt = q[:64], q[64:128]
+    ok = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    fh = torch.zeros(64, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(64, device="cuda")
+    ns = torch.zeros(64, dtype=torch.int32, device="cuda")
+    api.check_edges(R, E, dev(qf), dev(qt), 0.05, 1, ok, fh, ln, ns)
+    torch.cuda.synchronize()
+    _edge_parity(m, qf, qt, 0.05, 1, ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(),
+                 ns.cpu().numpy())
