@@ -190,6 +190,12 @@ GBMP_API gbmp_status gbmp_profile_enable(int32_t enable);
 GBMP_API gbmp_status gbmp_profile_reset(void);
 GBMP_API gbmp_status gbmp_profile_read(int32_t family, double *ms, int64_t *launches);
 GBMP_API gbmp_status gbmp_launch_count(int64_t *count);
+/* Executed-work accounting of the broad-phase collision kernels: while enabled, every
+ * checked state adds the floating-point operations its tests executed (same weights as
+ * the roofline model) and 1 to the state count.  Enabling resets the counters.  The
+ * counting adds work, so time a batch with it off. */
+GBMP_API gbmp_status gbmp_work_counting(int32_t enable);
+GBMP_API gbmp_status gbmp_work_read(uint64_t *flops, uint64_t *states);
 
 /* FP32 fused-multiply-add throughput of the current device, measured with a
  * register-resident FMA loop over `seconds` of wall time (the CUDA-core roofline

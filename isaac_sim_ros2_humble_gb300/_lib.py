@@ -67,6 +67,8 @@ SIGNATURES = {
     "gbmp_profile_reset": [],
     "gbmp_profile_read": [_i32, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
     "gbmp_launch_count": [C.POINTER(C.c_int64)],
+    "gbmp_work_counting": [_i32],
+    "gbmp_work_read": [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
     "gbmp_measure_fp32_peak": [C.c_double, C.POINTER(C.c_double)],
 }
 PROF_EDGE_WAVE, PROF_CHECK_STATES, PROF_FK, PROF_OTHER = 0, 1, 2, 3
@@ -145,6 +147,16 @@ def launch_count() -> int:
     n = C.c_int64()
     check(load().gbmp_launch_count(C.byref(n)))
     return n.value
+
+
+def work_counting(on: bool) -> None:
+    check(load().gbmp_work_counting(int(on)))
+
+
+def work_read():
+    f, n = C.c_uint64(), C.c_uint64()
+    check(load().gbmp_work_read(C.byref(f), C.byref(n)))
+    return f.value, n.value
 
 
 def measure_fp32_peak(seconds: float = 1.0) -> float:

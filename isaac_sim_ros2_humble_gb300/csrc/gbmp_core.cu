@@ -489,6 +489,12 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     D.lower = (const float *)(b + o_lo); D.upper = (const float *)(b + o_up); D.defv = (const float *)(b + o_def);
     D.active = (const unsigned char *)(b + o_act);
     D.G = G; D.NPL = NPL; D.cull = (G <= kMaxGroups) ? 1 : 0;
+    D.work = nullptr;
+    {
+        long long fk = 0;
+        for (int i = 1; i < L; ++i) fk += r->type[i] == 1 ? 151 : (r->type[i] == 2 ? 129 : (r->type[i] == 5 ? 63 : 0));
+        D.base_flops = fk + 24LL * S + 24LL * G;   // FK, sphere + group transforms (18) and A terms (6)
+    }
     D.grp = (const float *)(b + o_grp); D.glink = (const int *)(b + o_glink);
     D.sgrp = (const int *)(b + o_sgrp); D.lpair = (const int4 *)(b + o_lpair);
     (void)flags;
@@ -619,7 +625,9 @@ gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int6
     if (n == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_q, "q is NULL");
     const DevEnv E = env->dev();
-    const size_t smem = block_smem(r->dev, env_words(E.ns, E.nb, E.nc));
+    DevRobot D = r->dev;
+    D.work = work_counter();
+    const size_t smem = block_smem(D, env_words(E.ns, E.nb, E.nc));
     const long long need = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
     gbmp_status st = GBMP_OK;
     cudaStream_t s = (cudaStream_t)stream;
@@ -630,14 +638,14 @@ gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int6
             if (st) return st;
             if (need < grid) grid = (int)need;
             ProfScope ps(GBMP_PROF_CHECK_STATES, s);
-            k_check_states<true, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, E, d_q, n, d_verdict,
+            k_check_states<true, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(D, E, d_q, n, d_verdict,
                                                                                  d_costs, d_total);
         } else {
             st = persistent_grid(k_check_states<false, SPL>, smem, r->num_sms, &grid);
             if (st) return st;
             if (need < grid) grid = (int)need;
             ProfScope ps(GBMP_PROF_CHECK_STATES, s);
-            k_check_states<false, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(r->dev, E, d_q, n, d_verdict,
+            k_check_states<false, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(D, E, d_q, n, d_verdict,
                                                                                   nullptr, nullptr);
         }
     });
@@ -690,7 +698,9 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     }
 
     const DevEnv Ev = env->dev();
-    const size_t smem = block_smem(r->dev, env_words(Ev.ns, Ev.nb, Ev.nc));
+    DevRobot D = r->dev;
+    D.work = work_counter();
+    const size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
     int grid = 0;
     const bool cull = r->dev.cull != 0;
     GBMP_SPL_SWITCH(r->dev.spl, {
@@ -708,10 +718,10 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
             GBMP_SPL_SWITCH(r->dev.spl, {
                 if (cull)
                     k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                        r->dev, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+                        D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
                 else
                     k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                        r->dev, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+                        D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
             });
         }
         GBMP_CUDA(cudaGetLastError());

@@ -54,7 +54,18 @@ struct DevRobot {
     const float *grp;
     const int *glink, *sgrp;
     const int4 *lpair;
+    // Executed-work accounting (only when `work` is non-null): work[0] += flops executed,
+    // work[1] += states evaluated.  base_flops = per-state FK + sphere + group transforms.
+    unsigned long long *work;
+    long long base_flops;
 };
+
+// Flop weights of the executed tests (multiply/add/compare = 1, FMA = 2).
+constexpr int kFlSphereX = 9;     // expanded sphere-sphere test: 4 FMA + compare
+constexpr int kFlCuboid = 33;     // 3x4 transform + clamp + squared distance + compare
+constexpr int kFlCylinder = 34;   // 3x4 transform + finite-cylinder distance + compare
+constexpr int kFlSelf = 9;        // 3 sub, 1 mul + 2 FMA, compare
+constexpr int kFlGroupPair = 11;  // group-sphere overlap test
 
 constexpr int kMaxGroups = 32;
 constexpr float kBroadMargin = 1e-3f;    // metres added to every group bounding radius
@@ -460,6 +471,16 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
     __syncwarp();
     const unsigned lt = (1u << lane) - 1u;
     bool hit = false;
+    const bool count = R.work != nullptr;
+    unsigned long long fl = (unsigned long long)R.base_flops;
+#define GBMP_CULLED_RETURN(v)                                          \
+    do {                                                               \
+        if (count && lane == 0) {                                      \
+            atomicAdd(R.work, fl);                                     \
+            atomicAdd(R.work + 1, 1ull);                               \
+        }                                                              \
+        return (v);                                                    \
+    } while (0)
 
     // --- environment spheres (expanded form, see warp_collide) ---
     const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
@@ -479,6 +500,7 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
         if (mask) { const int pos = __popc(bal & lt); w.cand[pos] = o; w.cmask[pos] = mask; }
         __syncwarp();
         const int nc = __popc(bal);
+        if (count) fl += (unsigned long long)min(kWarp, E.ns - o0) * R.G * kFlSphereX;
         for (int i = 0; i < nc; ++i) {
             const int oc = w.cand[i];
             const unsigned cm = w.cmask[i];
@@ -488,9 +510,10 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
             for (int m = 0; m < SPL; ++m) {
                 const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
                 hit |= (cm & gbit[m]) && v > A[m];
+                if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlSphereX;
             }
         }
-        if (__any_sync(kFull, hit)) return true;
+        if (__any_sync(kFull, hit)) GBMP_CULLED_RETURN(true);
     }
 
     // --- cuboids ---
@@ -513,12 +536,14 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
         if (mask) { const int pos = __popc(bal & lt); w.cand[pos] = o; w.cmask[pos] = mask; }
         __syncwarp();
         const int nc = __popc(bal);
+        if (count) fl += (unsigned long long)min(kWarp, E.nb - o0) * R.G * kFlCuboid;
         for (int i = 0; i < nc; ++i) {
             const int oc = w.cand[i];
             const unsigned cm = w.cmask[i];
             const float4 r0 = bx[5 * oc], r1 = bx[5 * oc + 1], r2 = bx[5 * oc + 2], mn = bx[5 * oc + 3], mx = bx[5 * oc + 4];
 #pragma unroll
             for (int m = 0; m < SPL; ++m) {
+                if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlCuboid;
                 if (cm & gbit[m]) {
                     const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
                     const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
@@ -528,7 +553,7 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
                 }
             }
         }
-        if (__any_sync(kFull, hit)) return true;
+        if (__any_sync(kFull, hit)) GBMP_CULLED_RETURN(true);
     }
 
     // --- cylinders ---
@@ -552,12 +577,14 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
         if (mask) { const int pos = __popc(bal & lt); w.cand[pos] = o; w.cmask[pos] = mask; }
         __syncwarp();
         const int nc = __popc(bal);
+        if (count) fl += (unsigned long long)min(kWarp, E.nc - o0) * R.G * kFlCylinder;
         for (int i = 0; i < nc; ++i) {
             const int oc = w.cand[i];
             const unsigned cm = w.cmask[i];
             const float4 r0 = cyl[4 * oc], r1 = cyl[4 * oc + 1], r2 = cyl[4 * oc + 2], pr = cyl[4 * oc + 3];
 #pragma unroll
             for (int m = 0; m < SPL; ++m) {
+                if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlCylinder;
                 if (cm & gbit[m]) {
                     const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
                     const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
@@ -569,7 +596,7 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
                 }
             }
         }
-        if (__any_sync(kFull, hit)) return true;
+        if (__any_sync(kFull, hit)) GBMP_CULLED_RETURN(true);
     }
 
     // --- self collision: group pairs whose bounding spheres overlap ---
@@ -586,20 +613,23 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
             p1 = lp.w;
         }
         unsigned bal = __ballot_sync(kFull, on);
+        if (count) fl += (unsigned long long)min(kWarp, R.NPL - k0) * kFlGroupPair;
         while (bal) {
             const int j = __ffs(bal) - 1;
             bal &= bal - 1u;
             const int q0 = __shfl_sync(kFull, p0, j), q1 = __shfl_sync(kFull, p1, j);
+            if (count) fl += (unsigned long long)(q1 - q0) * kFlSelf;
             for (int p = q0 + lane; p < q1; p += kWarp) {
                 const unsigned ij = __ldg(R.pairs + p);
                 const float thr = __ldg(R.thr + p);
                 const float4 a = w.cen[ij & 0xffffu], b = w.cen[ij >> 16];
                 hit |= sq3(a.x - b.x, a.y - b.y, a.z - b.z) < thr;
             }
-            if (__any_sync(kFull, hit)) return true;
+            if (__any_sync(kFull, hit)) GBMP_CULLED_RETURN(true);
         }
     }
-    return false;
+    GBMP_CULLED_RETURN(false);
+#undef GBMP_CULLED_RETURN
 }
 
 // Dispatch on spheres-per-lane.

@@ -64,6 +64,7 @@ struct Codegen;   // runtime-generated robot kernels (gbmp_codegen.cpp)
 // profiling is on, records CUDA events on the launching stream around it.
 constexpr int kProfFamilies = 4;
 void count_launch(int n);
+unsigned long long *work_counter();   // device [flops, states] or nullptr when counting is off
 struct ProfScope {
     int fam;
     cudaStream_t s;

@@ -52,6 +52,14 @@ void drain(ProfState &p) {
 
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+namespace {
+std::mutex g_work_mu;
+unsigned long long *g_work = nullptr;   // [flops, states] on the device
+std::atomic<bool> g_work_on{false};
+}  // namespace
+
+unsigned long long *work_counter() { return g_work_on.load() ? g_work : nullptr; }
+
 ProfScope::ProfScope(int family, cudaStream_t stream) : fam(family), s(stream) {
     count_launch(1);
     ProfState &p = prof();
@@ -115,6 +123,25 @@ gbmp_status gbmp_profile_read(int32_t family, double *ms, int64_t *launches) {
     drain(p);
     if (ms) *ms = p.ms[family];
     if (launches) *launches = p.launches[family];
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_work_counting(int32_t enable) {
+    std::lock_guard<std::mutex> lock(g_work_mu);
+    if (enable) {
+        if (!g_work) GBMP_CUDA(cudaMalloc(&g_work, 2 * sizeof(unsigned long long)));
+        GBMP_CUDA(cudaMemset(g_work, 0, 2 * sizeof(unsigned long long)));
+    }
+    g_work_on.store(enable != 0);
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_work_read(uint64_t *flops, uint64_t *states) {
+    std::lock_guard<std::mutex> lock(g_work_mu);
+    unsigned long long h[2] = {0ull, 0ull};
+    if (g_work) GBMP_CUDA(cudaMemcpy(h, g_work, sizeof h, cudaMemcpyDeviceToHost));
+    if (flops) *flops = h[0];
+    if (states) *states = h[1];
     return GBMP_OK;
 }
 
