@@ -35,6 +35,8 @@ static gbmp_status persistent_grid(K kernel, size_t smem, int num_sms, int *grid
     for (int i = 0; i < n_configured; ++i) seen |= configured[i] == (const void *)kernel;
     if (!seen) {
         GBMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        GBMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       cudaSharedmemCarveoutMaxShared));
         if (n_configured < 64) configured[n_configured++] = (const void *)kernel;
     }
     int per_sm = 0;
@@ -546,7 +548,7 @@ gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_
     GBMP_CHECK_ARG(ns == 0 || (sp && sr), "sphere arrays are NULL");
     GBMP_CHECK_ARG(nb == 0 || (bp && brot && bmin && bmax), "cuboid arrays are NULL");
     GBMP_CHECK_ARG(nc == 0 || (cp && crot && crad && chei), "cylinder arrays are NULL");
-    const long long words = 3LL * ns + 5LL * nb + 4LL * nc;
+    const long long words = 2LL * ns + (ns + 3) / 4 + 5LL * nb + 4LL * nc;
     if (words > kMaxEnvWords) {
         set_error("environment needs %lld float4 words, limit %d", words, kMaxEnvWords);
         return GBMP_ERR_CAPACITY;
@@ -568,10 +570,11 @@ gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_
         w[4 * i + 3] = make_float4(crad[i], chei[i] * 0.5f, 0.f, 0.f);
     }
     w += 4 * nc;
+    float *nbv = reinterpret_cast<float *>(w + ns);
     for (int i = 0; i < ns; ++i) {
         const double x = sp[3 * i], y = sp[3 * i + 1], z = sp[3 * i + 2], rr = sr[i];
-        w[2 * i] = make_float4(2.f * sp[3 * i], 2.f * sp[3 * i + 1], 2.f * sp[3 * i + 2], 2.f * sr[i]);
-        w[2 * i + 1] = make_float4((float)(-(x * x + y * y + z * z - rr * rr)), 0.f, 0.f, 0.f);
+        w[i] = make_float4(2.f * sp[3 * i], 2.f * sp[3 * i + 1], 2.f * sp[3 * i + 2], 2.f * sr[i]);
+        nbv[i] = (float)(-(x * x + y * y + z * z - rr * rr));
     }
     cudaError_t err = cudaMalloc(&e->d_words, sizeof(float4) * e->h_words.size());
     if (err == cudaSuccess)

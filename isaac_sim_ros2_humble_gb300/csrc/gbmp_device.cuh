@@ -39,7 +39,8 @@ constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slot
 //   spheres  [ns]     (x, y, z, r)
 //   cuboids  [nb*5]   inverse pose rows 0..2, (min xyz, 0), (max xyz, 0)
 //   cylinders[nc*4]   inverse pose rows 0..2, (radius, half height, 0, 0)
-//   spheres  [ns*2]   expanded form (2x, 2y, 2z, 2r), (-(|o|^2 - r^2), 0, 0, 0)
+//   spheres  [ns]     expanded form (2x, 2y, 2z, 2r)
+//   spheres  [ceil(ns/4)] -(|o|^2 - r^2), four per word
 // ---------------------------------------------------------------------------------
 struct DevRobot {
     int L, S, P, spl;                 // spl = spheres per lane = ceil(S/32)
@@ -75,7 +76,7 @@ struct DevEnv {
     const float4 *words;              // env_words(ns, nb, nc) float4
 };
 
-__host__ __device__ inline int env_words(int ns, int nb, int nc) { return 3 * ns + 5 * nb + 4 * nc; }
+__host__ __device__ inline int env_words(int ns, int nb, int nc) { return 2 * ns + (ns + 3) / 4 + 5 * nb + 4 * nc; }
 
 // Shared-memory staging of the robot tables and the environment.
 struct SmemTables {
@@ -105,17 +106,17 @@ __host__ __device__ inline size_t smem_tables_bytes(const DevRobot &R, int nword
     return b;
 }
 
-// Per-warp scratch: link poses [L*12], temp [16], joint state [L], sphere centres [S],
+// Per-warp scratch: link poses [L*12], joint-local transforms [L*12], joint state [L], sphere centres [S],
 // group bounding spheres in the base frame [G] + their A terms [G], candidate list [32].
 __host__ __device__ inline size_t smem_warp_bytes(const DevRobot &R) {
-    return align16(sizeof(float) * 12 * R.L) + align16(sizeof(float) * 16) + align16(sizeof(float) * R.L) +
+    return align16(sizeof(float) * 12 * R.L) * 2 + align16(sizeof(float) * R.L) +
            align16(sizeof(float4) * R.S) + align16(sizeof(float4) * R.G) + align16(sizeof(float) * R.G) +
            align16(sizeof(int) * kWarp) * 2;
 }
 
 struct WarpScratch {
     float *lp;      // link poses
-    float *tmp;     // 12-element temporary
+    float *loc;     // joint-local transforms [L*12]
     float *q;       // joint values of the state under test
     float4 *cen;    // sphere centres (x, y, z, r)
     float4 *gb;     // group bounding spheres in the base frame (x, y, z, R)
@@ -148,7 +149,7 @@ __device__ inline WarpScratch carve_warp(unsigned char *base, const DevRobot &R,
     WarpScratch w;
     size_t off = 0;
     w.lp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L);
-    w.tmp = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 16);
+    w.loc = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L);
     w.q = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * R.L);
     w.cen = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.S);
     w.gb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.G);
@@ -190,77 +191,86 @@ __device__ __forceinline__ float mul_elem(const float *A, const float *B, int r,
     return acc;
 }
 
-// Column c (rows 0..2) of the Rodrigues rotation (KernelGenerator.h:305-325); column 3
-// is zero.  All nine entries are formed in registers and the column is selected, so
-// nothing is dynamically indexed.
-__device__ __forceinline__ float3 rot_col(const float *n4, float s, float c, int col) {
+// Rodrigues rotation (KernelGenerator.h:305-325), 3x3 block R[3*row + col].
+__device__ __forceinline__ void rot33(const float *n4, float s, float c, float *R) {
     const float nx = n4[0], ny = n4[1], nz = n4[2], valid = n4[3];
     const float oc = __fadd_rn(1.f, -c);
     const float iv = __fadd_rn(1.f, -valid);
-    const float r0 = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(nx, nx), oc, c), valid), iv);
-    const float r1 = __fmul_rn(__fmaf_rn(__fmul_rn(nx, ny), oc, -__fmul_rn(nz, s)), valid);
-    const float r2 = __fmul_rn(__fmaf_rn(__fmul_rn(nx, nz), oc, __fmul_rn(ny, s)), valid);
-    const float r4 = __fmul_rn(__fmaf_rn(__fmul_rn(ny, nx), oc, __fmul_rn(nz, s)), valid);
-    const float r5 = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(ny, ny), oc, c), valid), iv);
-    const float r6 = __fmul_rn(__fmaf_rn(__fmul_rn(ny, nz), oc, -__fmul_rn(nx, s)), valid);
-    const float r8 = __fmul_rn(__fmaf_rn(__fmul_rn(nz, nx), oc, -__fmul_rn(ny, s)), valid);
-    const float r9 = __fmul_rn(__fmaf_rn(__fmul_rn(nz, ny), oc, __fmul_rn(nx, s)), valid);
-    const float r10 = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(nz, nz), oc, c), valid), iv);
-    float3 o;
-    o.x = col == 0 ? r0 : (col == 1 ? r1 : (col == 2 ? r2 : 0.f));
-    o.y = col == 0 ? r4 : (col == 1 ? r5 : (col == 2 ? r6 : 0.f));
-    o.z = col == 0 ? r8 : (col == 1 ? r9 : (col == 2 ? r10 : 0.f));
-    return o;
+    R[0] = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(nx, nx), oc, c), valid), iv);
+    R[1] = __fmul_rn(__fmaf_rn(__fmul_rn(nx, ny), oc, -__fmul_rn(nz, s)), valid);
+    R[2] = __fmul_rn(__fmaf_rn(__fmul_rn(nx, nz), oc, __fmul_rn(ny, s)), valid);
+    R[3] = __fmul_rn(__fmaf_rn(__fmul_rn(ny, nx), oc, __fmul_rn(nz, s)), valid);
+    R[4] = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(ny, ny), oc, c), valid), iv);
+    R[5] = __fmul_rn(__fmaf_rn(__fmul_rn(ny, nz), oc, -__fmul_rn(nx, s)), valid);
+    R[6] = __fmul_rn(__fmaf_rn(__fmul_rn(nz, nx), oc, -__fmul_rn(ny, s)), valid);
+    R[7] = __fmul_rn(__fmaf_rn(__fmul_rn(nz, ny), oc, __fmul_rn(nx, s)), valid);
+    R[8] = __fadd_rn(__fmul_rn(__fmaf_rn(__fmul_rn(nz, nz), oc, c), valid), iv);
 }
 
-// Element (r, c) of A * B where B is given by its column c (rows 0..2), same
-// operation order as mul_elem.
-__device__ __forceinline__ float mul_col(const float *A, float3 bc, int r, int c) {
-    float acc = __fmul_rn(A[4 * r + 0], bc.x);
-    acc = __fmaf_rn(A[4 * r + 1], bc.y, acc);
-    acc = __fmaf_rn(A[4 * r + 2], bc.z, acc);
-    if (c == 3) acc = __fadd_rn(acc, A[4 * r + 3]);
-    return acc;
+// Joint-local transform of link i (one lane): revolute P * R(axis, q), prismatic
+// P * T(axis q), fixed P, in the product order of mul_elem.  Unsupported types get
+// the identity and are flagged so that the chain gives them an identity pose.
+__device__ __forceinline__ void joint_local(const SmemTables &t, int i, float q, float *M) {
+    const float *P = t.jl + 12 * i;
+    const int ty = t.type[i];
+    if (ty == 1) {
+        float sn, cs, R[9];
+        sincosf(q, &sn, &cs);
+        rot33(t.axn + 4 * i, sn, cs, R);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float acc = __fmul_rn(P[4 * r], R[c]);
+                acc = __fmaf_rn(P[4 * r + 1], R[3 + c], acc);
+                M[4 * r + c] = __fmaf_rn(P[4 * r + 2], R[6 + c], acc);
+            }
+            float acc = __fmul_rn(P[4 * r], 0.f);
+            acc = __fmaf_rn(P[4 * r + 1], 0.f, acc);
+            acc = __fmaf_rn(P[4 * r + 2], 0.f, acc);
+            M[4 * r + 3] = __fadd_rn(acc, P[4 * r + 3]);
+        }
+    } else if (ty == 2) {
+        const float *a = t.axr + 4 * i;
+        const float tx = __fmul_rn(a[0], q), ty2 = __fmul_rn(a[1], q), tz = __fmul_rn(a[2], q);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float acc = __fmul_rn(P[4 * r], c == 0 ? 1.f : 0.f);
+                acc = __fmaf_rn(P[4 * r + 1], c == 1 ? 1.f : 0.f, acc);
+                M[4 * r + c] = __fmaf_rn(P[4 * r + 2], c == 2 ? 1.f : 0.f, acc);
+            }
+            float acc = __fmul_rn(P[4 * r], tx);
+            acc = __fmaf_rn(P[4 * r + 1], ty2, acc);
+            acc = __fmaf_rn(P[4 * r + 2], tz, acc);
+            M[4 * r + 3] = __fadd_rn(acc, P[4 * r + 3]);
+        }
+    } else if (ty == 5) {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) M[k] = P[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) M[k] = (k % 5 == 0) ? 1.f : 0.f;
+    }
 }
 
 // FK of the state in w.q into w.lp.  All lanes of the warp must call it.
+// Phase 1: lane i forms the joint-local transform of link i (all links at once).
+// Phase 2: lanes 0..11 walk the chain, link_i = link_parent(i) * local_i, one
+// element per lane (KernelGenerator.h:369-400; association parent * (pose * motion)).
 __device__ inline void warp_fk(const SmemTables &t, int L, const WarpScratch &w, int lane) {
+    for (int i = lane; i < L; i += kWarp) joint_local(t, i, w.q[i], w.loc + 12 * i);
     const int r = lane >> 2, c = lane & 3;
     const bool own = lane < 12;
     if (own) w.lp[lane] = (r == c) ? 1.f : 0.f;
     __syncwarp();
     for (int i = 1; i < L; ++i) {
         const int ty = t.type[i];
-        const float *A = w.lp + 12 * t.parent[i];
-        const float *Jp = t.jl + 12 * i;
-        float *out = w.lp + 12 * i;
-        if (ty == 1) {                               // revolute: (parent * pose) * R
-            if (own) {
-                float sn, cs;
-                sincosf(w.q[i], &sn, &cs);
-                const float3 rc = rot_col(t.axn + 4 * i, sn, cs, c);
-                w.tmp[lane] = mul_elem(A, Jp, r, c);
-                __syncwarp(0xfffu);
-                out[lane] = mul_col(w.tmp, rc, r, c);
-            }
-        } else if (ty == 2) {                        // prismatic: parent * (pose * T)
-            if (own) {
-                const float qi = w.q[i];
-                const float *a = t.axr + 4 * i;
-                float3 tc;
-                if (c == 3) {
-                    tc = make_float3(__fmul_rn(a[0], qi), __fmul_rn(a[1], qi), __fmul_rn(a[2], qi));
-                } else {
-                    tc = make_float3(c == 0 ? 1.f : 0.f, c == 1 ? 1.f : 0.f, c == 2 ? 1.f : 0.f);
-                }
-                w.tmp[lane] = mul_col(Jp, tc, r, c);
-                __syncwarp(0xfffu);
-                out[lane] = mul_elem(A, w.tmp, r, c);
-            }
-        } else if (ty == 5) {                        // fixed: parent * pose
-            if (own) out[lane] = mul_elem(A, Jp, r, c);
-        } else {                                     // unsupported: identity
-            if (own) out[lane] = (r == c) ? 1.f : 0.f;
+        if (own) {
+            const bool known = ty == 1 || ty == 2 || ty == 5;
+            w.lp[12 * i + lane] = known ? mul_elem(w.lp + 12 * t.parent[i], w.loc + 12 * i, r, c)
+                                        : ((r == c) ? 1.f : 0.f);
         }
         __syncwarp();
     }
@@ -337,12 +347,13 @@ __device__ inline bool warp_collide(const SmemTables &t, const DevRobot &R, cons
 #pragma unroll
         for (int m = 0; m < SPL; ++m) A[m] = __fmaf_rn(cz[m], cz[m], __fmaf_rn(cy[m], cy[m], __fmaf_rn(cx[m], cx[m], -cr[m] * cr[m])));
         const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
+        const float *snb = reinterpret_cast<const float *>(sx + E.ns);
         for (int o0 = 0; o0 < E.ns; o0 += 16) {
             const int oe = min(o0 + 16, E.ns);
 #pragma unroll 4
             for (int o = o0; o < oe; ++o) {
-                const float4 b = sx[2 * o];
-                const float nb = sx[2 * o + 1].x;
+                const float4 b = sx[o];
+                const float nb = snb[o];
 #pragma unroll
                 for (int m = 0; m < SPL; ++m) {
                     const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
@@ -484,12 +495,15 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
 
     // --- environment spheres (expanded form, see warp_collide) ---
     const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
+    const float *snb = reinterpret_cast<const float *>(sx + E.ns);
+#pragma unroll 1
     for (int o0 = 0; o0 < E.ns; o0 += kWarp) {
         const int o = o0 + lane;
         unsigned mask = 0u;
         if (o < E.ns) {
-            const float4 b = sx[2 * o];
-            const float nb = sx[2 * o + 1].x;
+            const float4 b = sx[o];
+            const float nb = snb[o];
+#pragma unroll 2
             for (int g = 0; g < R.G; ++g) {
                 const float4 gs = w.gb[g];
                 const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
@@ -504,8 +518,8 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
         for (int i = 0; i < nc; ++i) {
             const int oc = w.cand[i];
             const unsigned cm = w.cmask[i];
-            const float4 b = sx[2 * oc];
-            const float nb = sx[2 * oc + 1].x;
+            const float4 b = sx[oc];
+            const float nb = snb[oc];
 #pragma unroll
             for (int m = 0; m < SPL; ++m) {
                 const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
@@ -518,6 +532,7 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
 
     // --- cuboids ---
     const float4 *bx = t.env + E.ns;
+#pragma unroll 1
     for (int o0 = 0; o0 < E.nb; o0 += kWarp) {
         const int o = o0 + lane;
         unsigned mask = 0u;
@@ -558,6 +573,7 @@ __device__ inline bool warp_collide_culled(const SmemTables &t, const DevRobot &
 
     // --- cylinders ---
     const float4 *cyl = t.env + E.ns + 5 * E.nb;
+#pragma unroll 1
     for (int o0 = 0; o0 < E.nc; o0 += kWarp) {
         const int o = o0 + lane;
         unsigned mask = 0u;

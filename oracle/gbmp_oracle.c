@@ -124,11 +124,12 @@ static void fk_one_f32(const or_robot *r, const float *q, float *P)
         const float *jp = r->pose + 16 * i;
         float *out = P + 16 * i;
         switch (r->type[i]) {
-        case OR_REVOLUTE:                         /* (parent * pose) * R(axis, q) */
+        case OR_REVOLUTE:                         /* parent * (pose * R(axis, q)): same product as
+                                                     (parent * pose) * R up to rounding */
             unit_axis_f32(r->axis + 3 * i, n);
             rot_f32(n, q[i], M);
-            mul_f32(par, jp, tmp);
-            mul_f32(tmp, M, out);
+            mul_f32(jp, M, tmp);
+            mul_f32(par, tmp, out);
             break;
         case OR_PRISMATIC: {                      /* parent * (pose * T(axis q)) */
             const float *a = r->axis + 3 * i;
