@@ -195,6 +195,46 @@ def serial_arm(seed: int, dof: int = 7, n_spheres: int = 59, prismatic_torso: bo
     return robot
 
 
+def tree_robot(seed: int, n_spheres: int = 40) -> RobotModel:
+    """A branching kinematic tree (torso with two 3-joint arms and a fixed head) mixing
+    revolute, prismatic and fixed joints, with un-normalised joint axes; used to test
+    general parent maps (parent[i] < i but not i - 1)."""
+    rng = np.random.default_rng(seed)
+    #          0 base, 1 torso(prism), 2 head(fixed), 3-5 left arm, 6-8 right arm, 9 tool(fixed)
+    parent = np.array([-1, 0, 1, 1, 3, 4, 1, 6, 7, 5], np.int32)
+    types = np.array([FIXED, PRISMATIC, FIXED, REVOLUTE, REVOLUTE, REVOLUTE, REVOLUTE, REVOLUTE,
+                      REVOLUTE, FIXED], np.int32)
+    L = len(parent)
+    poses = np.tile(np.eye(4), (L, 1, 1))
+    axes = np.zeros((L, 3))
+    for i in range(1, L):
+        poses[i, :3, :3] = _random_rotation(rng)
+        poses[i, :3, 3] = _unit(rng) * rng.uniform(0.08, 0.3)
+        axes[i] = _unit(rng) * rng.uniform(0.5, 2.0)         # not unit length
+    lower = np.full(L, -2.8, np.float32)
+    upper = np.full(L, 2.8, np.float32)
+    lower[1], upper[1] = 0.0, 0.3
+    active = (types != FIXED).astype(np.uint8)
+    default = np.zeros(L, np.float32)
+    lower[~active.astype(bool)] = upper[~active.astype(bool)] = 0.0
+    carriers = [1, 2, 3, 4, 5, 6, 7, 8, 9]
+    s_link = rng.choice(carriers, n_spheres).astype(np.int32)
+    s_pos = rng.normal(scale=0.05, size=(n_spheres, 3))
+    s_r = rng.uniform(0.02, 0.05, n_spheres)
+    enables = np.ones((L, L), np.uint8)
+    for i in range(L):
+        enables[i, i] = 0
+        if parent[i] >= 0:
+            enables[i, parent[i]] = enables[parent[i], i] = 0
+    robot = RobotModel(name=f"tree_s{seed}", joint_types=types, joint_poses=poses.astype(np.float32),
+                       joint_axes=axes.astype(np.float32), parent=parent, sphere_link=s_link,
+                       sphere_pos=s_pos.astype(np.float32), sphere_r=s_r.astype(np.float32), active=active,
+                       lower=lower, upper=upper, default=default, enables=enables,
+                       link_names=[f"link_{i}" for i in range(L)], resolution=0.02)
+    disable_default_collisions(robot, np.random.default_rng(seed + 7))
+    return robot
+
+
 def fk_numpy(robot: RobotModel, q: np.ndarray) -> np.ndarray:
     """Float64 link poses [N, L, 4, 4] (host-side helper for scene generation)."""
     q = np.asarray(q, np.float64).reshape(-1, robot.num_links)
@@ -206,7 +246,7 @@ def fk_numpy(robot: RobotModel, q: np.ndarray) -> np.ndarray:
         M = np.tile(np.eye(4), (N, 1, 1))
         if robot.joint_types[i] == REVOLUTE:
             a = robot.joint_axes[i].astype(np.float64)
-            a = a / np.linalg.norm(a)
+            a = a / np.linalg.norm(a)                        # revolute axes are normalised
             c, s = np.cos(q[:, i]), np.sin(q[:, i])
             K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
             M[:, :3, :3] = (c[:, None, None] * np.eye(3) + s[:, None, None] * K

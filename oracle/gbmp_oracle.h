@@ -10,12 +10,11 @@
  * are the high-precision truth used for tolerance checks.
  *
  * Pinning: the FK, edge-step and interpolation restatements are checked in
- * tests against the reference's own generated kernels (compiled for the CPU
- * from cudampl/CUDAMPLib/include/spaces/KernelGenerator.h by oracle/ref_build.py);
- * the collision-cost restatements are checked against the reference's own
- * constraint kernels compiled for the CPU by the same recipe (block-level SIMT
- * emulation).  Where the recipe cannot run (no reference tree), parity of the
- * collision costs rests on this restatement alone.
+ * tests against the reference's own generated kernels, compiled for the CPU from
+ * cudampl/CUDAMPLib/include/spaces/KernelGenerator.h by oracle/ref_build.py.  The
+ * collision-cost restatements cannot be pinned the same way (the constraint kernels
+ * live in .cu files that need Eigen, thrust and CUDA launches); they are checked
+ * against hand-computed cases and FP64 signed clearances.
  */
 #ifndef GBMP_ORACLE_H
 #define GBMP_ORACLE_H

@@ -50,6 +50,22 @@ def test_fk_poses_and_centers(plain, edge):
         assert np.abs(poses.cpu().numpy() - m.fk(q)).max() < 2e-6
 
 
+def test_fk_branching_tree():
+    """Parent map that is not a chain, fixed and prismatic joints, un-normalised axes."""
+    robot = W.tree_robot(3)
+    env = W.random_env(9, 40, 10, 4, oriented=True, center=(0.3, 0.0, 0.3))
+    R, E = api.Robot(robot), api.Env(env)
+    m = O.OracleModel(robot, env)
+    q = robot.sample_full(np.random.default_rng(4), 2048)
+    poses = torch.zeros((2048, robot.num_links, 16), device="cuda")
+    api.fk(R, dev(q), poses)
+    v = torch.zeros(2048, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E, dev(q), verdict=v)
+    torch.cuda.synchronize()
+    assert np.abs(poses.cpu().numpy() - m.fk(q.astype(np.float64), f64=True)).max() < FK_TOL
+    _verdict_parity(m, q, v.cpu().numpy().astype(bool))
+
+
 def _verdict_parity(m, q, verdict):
     cl = m.clearance(q)
     clear = np.abs(cl) > BAND
