@@ -177,6 +177,44 @@ GBMP_API gbmp_status gbmp_steer(gbmp_robot robot, const float *d_from, const int
 GBMP_API gbmp_status gbmp_sample(gbmp_robot robot, uint64_t seed, uint64_t offset, int64_t n, float *d_q,
                         void *stream);
 
+/* ---- parallel RRT-Connect ----
+ * Replaces CPRRTC::RobotSolver (cudampl/CPRRTC/include/RobotSolver.h:84-101,
+ * cudampl/CPRRTC/src/RobotSolver.cu:348-473) and pRRTC::solve (pRRTC/src/planning/
+ * pRRTC.cu:607-766, settings pRRTC_settings.hh:3-16).  A planner owns two device-resident
+ * trees of max_nodes nodes each and a path buffer; it can be reused for many solves with
+ * the same robot (one solve at a time per planner). */
+typedef struct gbmp_planner_s *gbmp_planner;
+
+typedef struct gbmp_rrtc_settings {
+    int32_t lanes;          /* parallel extension lanes (one 4-warp block each)          */
+    int32_t max_iters;      /* iteration cap per lane                                    */
+    float range;            /* maximum extension length, L2 over active joints            */
+    float resolution;       /* edge collision-check step (<= 0: the robot's resolution)   */
+    int32_t step_rule;      /* GBMP_STEP_L2 or GBMP_STEP_LINF                             */
+    uint64_t seed;          /* Philox key; sample (lane, iteration, joint)                */
+    double time_limit_s;    /* device-side deadline (<= 0: 10 s)                          */
+} gbmp_rrtc_settings;
+
+typedef struct gbmp_rrtc_result {
+    int32_t solved;
+    int32_t status;         /* 1 solved, 2 node cap, 3 iteration cap, 4 deadline            */
+    int32_t path_len;       /* states in h_path (start first, goal last)                    */
+    float cost;             /* path length, L2 over active joints                           */
+    int32_t start_tree_size, goal_tree_size;
+    int32_t iterations;     /* largest lane iteration reached                               */
+    double kernel_ms;       /* device time of the planning launch                           */
+} gbmp_rrtc_result;
+
+GBMP_API gbmp_status gbmp_planner_create(gbmp_robot robot, int32_t max_nodes, int32_t path_cap,
+                                         gbmp_planner *out);
+GBMP_API gbmp_status gbmp_planner_destroy(gbmp_planner planner);
+/* h_start / h_goal: full joint vectors [L].  h_path: [path_cap * L] host buffer.
+ * Returns GBMP_OK when solved, GBMP_ERR_NOT_SOLVED / GBMP_ERR_TIMEOUT otherwise (the
+ * result struct is filled in every case).  Synchronous on `stream`. */
+GBMP_API gbmp_status gbmp_rrtc_solve(gbmp_planner planner, gbmp_env env, const float *h_start,
+                                     const float *h_goal, const gbmp_rrtc_settings *settings, float *h_path,
+                                     int32_t path_cap, gbmp_rrtc_result *result, void *stream);
+
 /* ---- instrumentation ----
  * With profiling enabled, CUDA events are recorded on the launching stream around
  * every launch of the named kernel families; gbmp_profile_read() waits for them and

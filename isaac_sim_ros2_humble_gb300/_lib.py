@@ -36,6 +36,17 @@ class RobotDesc(C.Structure):
                 ("default_values", C.c_void_p), ("self_enables", C.c_void_p), ("resolution", C.c_float)]
 
 
+class RrtcSettings(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("max_iters", C.c_int32), ("range", C.c_float), ("resolution", C.c_float),
+                ("step_rule", C.c_int32), ("seed", C.c_uint64), ("time_limit_s", C.c_double)]
+
+
+class RrtcResult(C.Structure):
+    _fields_ = [("solved", C.c_int32), ("status", C.c_int32), ("path_len", C.c_int32), ("cost", C.c_float),
+                ("start_tree_size", C.c_int32), ("goal_tree_size", C.c_int32), ("iterations", C.c_int32),
+                ("kernel_ms", C.c_double)]
+
+
 class Limits(C.Structure):
     _fields_ = [("max_links", C.c_int32), ("max_spheres", C.c_int32), ("max_self_pairs", C.c_int32),
                 ("max_env_words", C.c_int32)]
@@ -63,6 +74,9 @@ SIGNATURES = {
     "gbmp_nearest": [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp],
     "gbmp_steer": [_vp, _vp, _vp, _vp, _i64, _f32, _vp],
     "gbmp_sample": [_vp, _u64, _u64, _i64, _vp, _vp],
+    "gbmp_planner_create": [_vp, _i32, _i32, C.POINTER(_vp)],
+    "gbmp_planner_destroy": [_vp],
+    "gbmp_rrtc_solve": [_vp, _vp, _vp, _vp, C.POINTER(RrtcSettings), _vp, _i32, C.POINTER(RrtcResult), _vp],
     "gbmp_profile_enable": [_i32],
     "gbmp_profile_reset": [],
     "gbmp_profile_read": [_i32, C.POINTER(C.c_double), C.POINTER(C.c_int64)],

@@ -137,3 +137,47 @@ def steer(robot: Robot, q_from, q_to, max_distance: float, idx=None, stream=None
 def sample(robot: Robot, seed: int, offset: int, out, stream=None):
     n = _n(out, robot.L)
     check(_lib.load().gbmp_sample(robot.handle, seed, offset, n, ptr(out), stream_handle(stream)))
+
+
+class Planner:
+    """Device-resident RRT-Connect trees for one robot (replaces CPRRTC::RobotSolver)."""
+
+    def __init__(self, robot: Robot, max_nodes: int = 1_000_000, path_cap: int = 65536):
+        h = C.c_void_p()
+        check(_lib.load().gbmp_planner_create(robot.handle, int(max_nodes), int(path_cap), C.byref(h)))
+        self.handle = h
+        self.robot = robot
+        self.path_cap = int(path_cap)
+        self._path = np.zeros((self.path_cap, robot.L), np.float32)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().gbmp_planner_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, env: Env, start, goal, lanes: int = 1024, max_iters: int = 100000, range_: float = 0.1,
+              resolution: float = 0.0, rule: int = _lib.STEP_L2, seed: int = 0, time_limit_s: float = 10.0,
+              stream=None, raise_on_failure: bool = False):
+        """Returns (result, path): result is a dict of the C result struct, path the
+        [path_len, L] float32 waypoints (empty when not solved)."""
+        st = _lib.RrtcSettings(int(lanes), int(max_iters), float(range_), float(resolution), int(rule), int(seed),
+                               float(time_limit_s))
+        res = _lib.RrtcResult()
+        s0 = _c(start, np.float32).reshape(-1)
+        g0 = _c(goal, np.float32).reshape(-1)
+        assert s0.size == self.robot.L and g0.size == self.robot.L
+        status = _lib.load().gbmp_rrtc_solve(self.handle, env.handle, s0.ctypes.data, g0.ctypes.data, C.byref(st),
+                                             self._path.ctypes.data, self.path_cap, C.byref(res),
+                                             stream_handle(stream))
+        if status not in (_lib.OK, 6, 7) or raise_on_failure:
+            check(status)
+        out = {f: getattr(res, f) for f, _ in _lib.RrtcResult._fields_}
+        out["status_code"] = status
+        path = self._path[: res.path_len].copy() if res.solved else np.zeros((0, self.robot.L), np.float32)
+        return out, path

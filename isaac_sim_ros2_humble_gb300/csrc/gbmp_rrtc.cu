@@ -1,0 +1,509 @@
+// gbmp_rrtc.cu -- parallel RRT-Connect on the device (replaces CPRRTC::RobotSolver::solve,
+// cudampl/CPRRTC/src/RobotSolver.cu:348-473 with its kernel :507-799, and the pRRTC
+// kernel rrtc<Robot>, pRRTC/src/planning/pRRTC.cu:305-602).
+//
+// One persistent launch per solve.  Each block is one extension lane of kRrtcWarps
+// warps; per iteration a lane
+//   1. picks the tree to grow (the smaller tree gets proportionally more lanes,
+//      pRRTC.cu:348-371 balance mode 1),
+//   2. draws a Philox sample in the joint limits (counter = lane, iteration),
+//   3. finds the nearest node of that tree (block-wide argmin over the active joints),
+//   4. steers to at most `range` (pRRTC.cu:415-434),
+//   5. validates the edge with the checkMotions step rule, one warp per state
+//      (FK + self + environment collision, broad phase included),
+//   6. appends the node (atomic slot, NaN sentinel until every coordinate is written,
+//      pRRTC.cu:447-476 with the sentinel filled correctly),
+//   7. tries to connect: finds the nearest node of the other tree and extends towards
+//      it in steps of at most `range`, appending every validated step; reaching it
+//      solves the problem (RobotSolver.cu:686-794, pRRTC.cu:478-551).
+// The first lane to connect records the connection; a trace kernel then walks both
+// parent chains into the path buffer (pRRTC.cu:552-581).  Every loop is bounded: the
+// lane iteration cap, the node cap and a %globaltimer deadline end the launch with a
+// status the host reads.
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "gbmp_internal.h"
+#include "gbmp_philox.h"
+
+namespace gbmp {
+
+constexpr int kRrtcWarps = 4;
+constexpr int kRrtcThreads = kRrtcWarps * kWarp;
+
+enum : int { kStRunning = 0, kStSolved = 1, kStNodeCap = 2, kStIterCap = 3, kStDeadline = 4 };
+
+struct RrtcDev {
+    float *nodes[2];          // [cap * stride], NaN until written
+    int *parent[2];           // [cap]
+    int *size;                // [2] allocated slots per tree
+    int *state;               // [0] status, [1] winning lane, [2] tree of the new node,
+                              // [3] node in that tree, [4] node in the other tree, [5] max iteration
+    float *path;              // [path_cap * L]
+    int *path_len;            // [1], -1 if the path buffer was too small
+    int cap, stride, path_cap;
+};
+
+struct RrtcParams {
+    int lanes, max_iters, rule;
+    float range, res;
+    unsigned long long seed;
+    unsigned long long deadline_ns;   // absolute %globaltimer value
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Block-wide argmin of the squared active-joint distance from q to the written nodes
+// of one tree.  Returns the node index (or -1) to every thread.
+__device__ int block_nearest(const float *__restrict__ nodes, int size, int stride, int L,
+                             const unsigned char *act, const float *q, float *s_d, int *s_i) {
+    float best = __int_as_float(0x7f800000);
+    int bi = INT_MAX;
+    for (int i = threadIdx.x; i < size; i += blockDim.x) {
+        const float *y = nodes + (long long)i * stride;
+        float s = 0.f;
+        bool written = true;
+        for (int j = 0; j < L; ++j) {
+            const float v = __ldcg(y + j);
+            written &= v == v;
+            if (act[j]) {
+                const float d = __fadd_rn(q[j], -v);
+                s = __fmaf_rn(d, d, s);
+            }
+        }
+        if (written && (s < best || (s == best && i < bi))) { best = s; bi = i; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float ob = __shfl_xor_sync(kFull, best, off);
+        const int oi = __shfl_xor_sync(kFull, bi, off);
+        if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int warp = threadIdx.x / kWarp, lane = threadIdx.x & 31;
+    if (lane == 0) { s_d[warp] = best; s_i[warp] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kRrtcWarps; ++w)
+            if (s_d[w] < s_d[0] || (s_d[w] == s_d[0] && s_i[w] < s_i[0])) { s_d[0] = s_d[w]; s_i[0] = s_i[w]; }
+    }
+    __syncthreads();
+    const int r = s_i[0];
+    __syncthreads();
+    return r == INT_MAX ? -1 : r;
+}
+
+// Validate the edge a -> b (full joint vectors in shared memory) with the step rule of
+// checkMotions: n = floor(metric / res) + 1 states, state k = a + dir * k, the last
+// state is b; state 0 (= a, already in the tree) is skipped unless n == 1.  One warp
+// per state.  Returns true if every state is collision-free.
+template <int SPL, bool CULL>
+__device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
+                                const float *a, const float *b, float res, int rule, int *s_flag, float *s_dir,
+                                int *s_n) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x / kWarp;
+    if (threadIdx.x == 0) {
+        float d2 = 0.f, dinf = 0.f;
+        for (int j = 0; j < R.L; ++j) {
+            const float d = __fadd_rn(a[j], -b[j]);
+            d2 = __fmaf_rn(d, d, d2);
+            dinf = fmaxf(dinf, fabsf(d));
+        }
+        const float metric = rule == GBMP_STEP_LINF ? dinf : __fsqrt_rn(d2);
+        const float ratio = __fdiv_rn(metric, res);
+        *s_n = ratio < 1e6f ? (int)ratio + 1 : 1000001;
+        *s_flag = 0;
+    }
+    __syncthreads();
+    const int n = *s_n;
+    for (int j = threadIdx.x; j < R.L; j += blockDim.x) s_dir[j] = __fdiv_rn(__fadd_rn(b[j], -a[j]), (float)n);
+    __syncthreads();
+    for (int k0 = (n == 1 ? 0 : 1); k0 < n; k0 += kRrtcWarps) {
+        const int k = k0 + warp;
+        bool hit = false;
+        if (k < n) {
+            for (int j = lane; j < R.L; j += kWarp)
+                w.q[j] = (k == n - 1) ? b[j] : __fmaf_rn(s_dir[j], (float)k, a[j]);
+            __syncwarp();
+            warp_fk(t, R.L, w, lane);
+            hit = CULL ? warp_collide_culled<SPL>(t, R, E, w, lane)
+                       : warp_collide<SPL, false>(t, R, E, w, lane, nullptr);
+        }
+        if (hit && lane == 0) *s_flag = 1;
+        __syncthreads();
+        const bool any = *s_flag != 0;
+        __syncthreads();
+        if (any) return false;
+    }
+    return true;
+}
+
+// Append q to tree `tr` with parent `par`; returns the slot or -1 when the tree is full.
+__device__ int block_append(const RrtcDev &P, int tr, const float *q, int par, int L, int *s_idx) {
+    if (threadIdx.x == 0) {
+        const int idx = atomicAdd(P.size + tr, 1);
+        *s_idx = idx < P.cap ? idx : -1;
+        if (idx >= P.cap) atomicCAS(P.state, kStRunning, kStNodeCap);
+    }
+    __syncthreads();
+    const int idx = *s_idx;
+    if (idx >= 0) {
+        for (int j = threadIdx.x; j < L; j += blockDim.x) __stcg(P.nodes[tr] + (long long)idx * P.stride + j, q[j]);
+        if (threadIdx.x == 0) P.parent[tr][idx] = par;
+        __threadfence();
+    }
+    __syncthreads();
+    return idx;
+}
+
+template <int SPL, bool CULL>
+__global__ void __launch_bounds__(kRrtcThreads) k_rrtc(DevRobot R, DevEnv E, RrtcDev P, RrtcParams prm) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nwords = env_words(E.ns, E.nb, E.nc);
+    SmemTables t = carve_tables(smem, R, nwords);
+    stage_tables(R, E, t, nwords);
+    unsigned char *p = smem + smem_tables_bytes(R, nwords);
+    WarpScratch w = carve_warp(p, R, threadIdx.x / kWarp);
+    p += smem_warp_bytes(R) * kRrtcWarps;
+    float *q_s = reinterpret_cast<float *>(p);          // sample / steered node
+    float *q_a = q_s + kMaxLinks;                        // nearest node / current node
+    float *q_b = q_a + kMaxLinks;                        // connect target
+    float *q_c = q_b + kMaxLinks;                        // next connect step
+    float *s_dir = q_c + kMaxLinks;
+    float *s_d = s_dir + kMaxLinks;                      // [kRrtcWarps]
+    int *s_i = reinterpret_cast<int *>(s_d + kRrtcWarps);
+    int *s_misc = s_i + kRrtcWarps;                      // [8]
+    unsigned char *act = reinterpret_cast<unsigned char *>(s_misc + 8);
+    for (int j = threadIdx.x; j < R.L; j += blockDim.x) act[j] = R.active[j];
+    __syncthreads();
+
+    const int lane_id = blockIdx.x;
+    const int L = R.L;
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            int st = *(volatile int *)P.state;
+            if (st == kStRunning && it >= prm.max_iters) st = kStIterCap;
+            if (st == kStRunning && global_ns() > prm.deadline_ns) {
+                atomicCAS(P.state, kStRunning, kStDeadline);
+                st = kStDeadline;
+            }
+            s_misc[0] = st;
+            // tree choice: a share of the lanes proportional to the other tree's size
+            const int n0 = *(volatile int *)(P.size), n1 = *(volatile int *)(P.size + 1);
+            const float ratio = (float)n0 / (float)max(n0 + n1, 1);
+            s_misc[1] = ((float)(lane_id % prm.lanes) < (float)prm.lanes * (1.f - ratio)) ? 0 : 1;
+            s_misc[2] = min(n0, P.cap);
+            s_misc[3] = min(n1, P.cap);
+        }
+        __syncthreads();
+        if (s_misc[0] != kStRunning) {
+            if (threadIdx.x == 0 && s_misc[0] == kStIterCap) atomicCAS(P.state, kStRunning, kStIterCap);
+            break;
+        }
+        if (threadIdx.x == 0) atomicMax(P.state + 5, it + 1);
+        const int tr = s_misc[1], ot = 1 - tr;
+        const int size_t_ = tr == 0 ? s_misc[2] : s_misc[3];
+        const int size_o = tr == 0 ? s_misc[3] : s_misc[2];
+        // 2. sample
+        for (int j = threadIdx.x; j < L; j += blockDim.x) {
+            if (act[j]) {
+                const float u = philox_uniform(prm.seed, ((unsigned long long)lane_id << 32) | (unsigned)it, (unsigned)j);
+                q_s[j] = __fmaf_rn(u, __fadd_rn(R.upper[j], -R.lower[j]), R.lower[j]);
+            } else {
+                q_s[j] = R.defv[j];
+            }
+        }
+        __syncthreads();
+        // 3. nearest node in the tree being grown
+        const int nn = block_nearest(P.nodes[tr], size_t_, P.stride, L, act, q_s, s_d, s_i);
+        if (nn < 0) continue;
+        for (int j = threadIdx.x; j < L; j += blockDim.x) q_a[j] = __ldcg(P.nodes[tr] + (long long)nn * P.stride + j);
+        __syncthreads();
+        // 4. steer to at most `range` (active joints)
+        if (threadIdx.x == 0) {
+            float s = 0.f;
+            for (int j = 0; j < L; ++j)
+                if (act[j]) { const float d = __fadd_rn(q_s[j], -q_a[j]); s = __fmaf_rn(d, d, s); }
+            const float d = __fsqrt_rn(s);
+            s_d[0] = d > prm.range ? __fdiv_rn(prm.range, d) : 1.f;
+        }
+        __syncthreads();
+        const float scale = s_d[0];
+        __syncthreads();
+        for (int j = threadIdx.x; j < L; j += blockDim.x)
+            if (act[j] && scale < 1.f) q_s[j] = __fmaf_rn(scale, __fadd_rn(q_s[j], -q_a[j]), q_a[j]);
+        __syncthreads();
+        // 5. validate nn -> new
+        if (!block_edge_free<SPL, CULL>(t, R, E, w, q_a, q_s, prm.res, prm.rule, s_misc + 4, s_dir, s_misc + 5))
+            continue;
+        // 6. append
+        int cur = block_append(P, tr, q_s, nn, L, s_misc + 6);
+        if (cur < 0) break;
+        // 7. connect towards the nearest node of the other tree
+        const int tgt = block_nearest(P.nodes[ot], size_o, P.stride, L, act, q_s, s_d, s_i);
+        if (tgt < 0) continue;
+        for (int j = threadIdx.x; j < L; j += blockDim.x) {
+            q_b[j] = __ldcg(P.nodes[ot] + (long long)tgt * P.stride + j);
+            q_a[j] = q_s[j];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float s = 0.f;
+            for (int j = 0; j < L; ++j)
+                if (act[j]) { const float d = __fadd_rn(q_b[j], -q_a[j]); s = __fmaf_rn(d, d, s); }
+            const float d = __fsqrt_rn(s);
+            const float ne = ceilf(__fdiv_rn(d, prm.range));
+            s_misc[7] = ne < 1e6f ? max(1, (int)ne) : 1000000;
+        }
+        __syncthreads();
+        const int n_ext = s_misc[7];
+        __syncthreads();
+        bool connected = true;
+        for (int e = 1; e <= n_ext; ++e) {
+            if (threadIdx.x == 0) s_misc[4] = *(volatile int *)P.state;
+            __syncthreads();
+            const bool stop = s_misc[4] != kStRunning;
+            __syncthreads();
+            if (stop) { connected = false; break; }
+            for (int j = threadIdx.x; j < L; j += blockDim.x)
+                q_c[j] = (e == n_ext) ? q_b[j]
+                                      : __fmaf_rn(__fdiv_rn(__fadd_rn(q_b[j], -q_s[j]), (float)n_ext), (float)e, q_s[j]);
+            __syncthreads();
+            if (!block_edge_free<SPL, CULL>(t, R, E, w, q_a, q_c, prm.res, prm.rule, s_misc + 4, s_dir, s_misc + 5)) {
+                connected = false;
+                break;
+            }
+            if (e < n_ext) {
+                cur = block_append(P, tr, q_c, cur, L, s_misc + 6);
+                if (cur < 0) { connected = false; break; }
+                for (int j = threadIdx.x; j < L; j += blockDim.x) q_a[j] = q_c[j];
+                __syncthreads();
+            }
+        }
+        if (connected && threadIdx.x == 0) {
+            if (atomicCAS(P.state, kStRunning, kStSolved) == kStRunning) {
+                P.state[1] = lane_id;
+                P.state[2] = tr;
+                P.state[3] = cur;
+                P.state[4] = tgt;
+                __threadfence();
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_read_clock(unsigned long long *t) {
+    if (threadIdx.x == 0) *t = global_ns();
+}
+
+// Walk both parent chains into the path (start tree root first).  One thread.
+__global__ void k_rrtc_trace(RrtcDev P, int L) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (P.state[0] != kStSolved) { *P.path_len = 0; return; }
+    const int tr = P.state[2];
+    const int a = P.state[3], b = P.state[4];
+    const int na = tr == 0 ? a : b, nb = tr == 0 ? b : a;   // node in start tree, node in goal tree
+    // count
+    int len0 = 0, len1 = 0;
+    for (int i = na; i >= 0 && len0 <= P.cap; i = (P.parent[0][i] == i ? -1 : P.parent[0][i])) ++len0;
+    for (int i = nb; i >= 0 && len1 <= P.cap; i = (P.parent[1][i] == i ? -1 : P.parent[1][i])) ++len1;
+    if (len0 + len1 > P.path_cap || len0 > P.cap || len1 > P.cap) { *P.path_len = -(len0 + len1); return; }
+    int k = len0 - 1;
+    for (int i = na; i >= 0; i = (P.parent[0][i] == i ? -1 : P.parent[0][i]), --k)
+        for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[0][(long long)i * P.stride + j];
+    k = len0;
+    for (int i = nb; i >= 0; i = (P.parent[1][i] == i ? -1 : P.parent[1][i]), ++k)
+        for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[1][(long long)i * P.stride + j];
+    *P.path_len = len0 + len1;
+}
+
+#define GBMP_SPL_SWITCH2(spl, ...)                          \
+    switch (spl) {                                          \
+    case 1: { constexpr int SPL = 1; __VA_ARGS__; } break;  \
+    case 2: { constexpr int SPL = 2; __VA_ARGS__; } break;  \
+    case 3: { constexpr int SPL = 3; __VA_ARGS__; } break;  \
+    case 4: { constexpr int SPL = 4; __VA_ARGS__; } break;  \
+    case 5: { constexpr int SPL = 5; __VA_ARGS__; } break;  \
+    case 6: { constexpr int SPL = 6; __VA_ARGS__; } break;  \
+    case 7: { constexpr int SPL = 7; __VA_ARGS__; } break;  \
+    default: { constexpr int SPL = 8; __VA_ARGS__; } break; \
+    }
+
+}  // namespace gbmp
+
+using namespace gbmp;
+
+struct gbmp_planner_s {
+    gbmp_robot robot = nullptr;
+    int cap = 0, stride = 0, path_cap = 0;
+    void *block = nullptr;
+    RrtcDev dev{};
+};
+
+extern "C" {
+
+gbmp_status gbmp_planner_create(gbmp_robot r, int32_t max_nodes, int32_t path_cap, gbmp_planner *out) {
+    GBMP_CHECK_ARG(r && out, "robot/out is NULL");
+    *out = nullptr;
+    GBMP_CHECK_ARG(max_nodes >= 2 && max_nodes <= (1 << 28), "max_nodes %d outside [2, 2^28]", max_nodes);
+    GBMP_CHECK_ARG(path_cap >= 2, "path_cap < 2");
+    auto *p = new gbmp_planner_s();
+    p->robot = r;
+    p->cap = max_nodes;
+    p->stride = (r->L + 3) & ~3;
+    p->path_cap = path_cap;
+    const size_t nodes_b = align16(sizeof(float) * (size_t)max_nodes * p->stride);
+    const size_t par_b = align16(sizeof(int) * (size_t)max_nodes);
+    const size_t bytes = 2 * nodes_b + 2 * par_b + 256 + align16(sizeof(float) * (size_t)path_cap * r->L);
+    cudaError_t e = cudaMalloc(&p->block, bytes);
+    if (e != cudaSuccess) {
+        delete p;
+        set_error("planner allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+    }
+    auto *b = static_cast<unsigned char *>(p->block);
+    RrtcDev &D = p->dev;
+    D.nodes[0] = (float *)b; D.nodes[1] = (float *)(b + nodes_b);
+    D.parent[0] = (int *)(b + 2 * nodes_b); D.parent[1] = (int *)(b + 2 * nodes_b + par_b);
+    int *ints = (int *)(b + 2 * nodes_b + 2 * par_b);
+    D.size = ints; D.state = ints + 4; D.path_len = ints + 16;
+    D.path = (float *)(b + 2 * nodes_b + 2 * par_b + 256);
+    D.cap = max_nodes; D.stride = p->stride; D.path_cap = path_cap;
+    *out = p;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_planner_destroy(gbmp_planner p) {
+    if (!p) return GBMP_OK;
+    if (p->block) cudaFree(p->block);
+    delete p;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, const float *h_goal,
+                            const gbmp_rrtc_settings *s, float *h_path, int32_t path_cap, gbmp_rrtc_result *res,
+                            void *stream) {
+    GBMP_CHECK_ARG(p && env && h_start && h_goal && s && res, "NULL argument");
+    gbmp_robot r = p->robot;
+    const int L = r->L;
+    GBMP_CHECK_ARG(s->lanes >= 1 && s->lanes <= (1 << 20), "lanes %d outside [1, 2^20]", s->lanes);
+    GBMP_CHECK_ARG(s->range > 0.f && std::isfinite(s->range), "range must be > 0");
+    GBMP_CHECK_ARG(s->max_iters >= 1, "max_iters < 1");
+    GBMP_CHECK_ARG(s->step_rule == GBMP_STEP_L2 || s->step_rule == GBMP_STEP_LINF, "unknown step rule");
+    for (int j = 0; j < L; ++j)
+        GBMP_CHECK_ARG(std::isfinite(h_start[j]) && std::isfinite(h_goal[j]), "start/goal not finite");
+    memset(res, 0, sizeof *res);
+    cudaStream_t st = (cudaStream_t)stream;
+    const RrtcDev &D = p->dev;
+    // reset: NaN sentinels, counters, roots (RobotSolver.cu:361-388 with a float sentinel)
+    GBMP_CUDA(cudaMemsetAsync(D.nodes[0], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
+    GBMP_CUDA(cudaMemsetAsync(D.nodes[1], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
+    GBMP_CUDA(cudaMemsetAsync(D.size, 0, 256, st));
+    int h_init[2] = {1, 1}, h_root = 0;
+    GBMP_CUDA(cudaMemcpyAsync(D.size, h_init, sizeof h_init, cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(D.nodes[0], h_start, sizeof(float) * L, cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(D.nodes[1], h_goal, sizeof(float) * L, cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(D.parent[0], &h_root, sizeof(int), cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(D.parent[1], &h_root, sizeof(int), cudaMemcpyHostToDevice, st));
+
+    const DevEnv E = env->dev();
+    DevRobot DR = r->dev;
+    DR.work = nullptr;
+    const int nwords = env_words(E.ns, E.nb, E.nc);
+    const size_t smem = smem_tables_bytes(DR, nwords) + smem_warp_bytes(DR) * kRrtcWarps + 6 * kMaxLinks * 4 + 256;
+    RrtcParams prm;
+    prm.lanes = s->lanes;
+    prm.max_iters = s->max_iters;
+    prm.rule = s->step_rule;
+    prm.range = s->range;
+    prm.res = s->resolution > 0.f ? s->resolution : r->resolution;
+    prm.seed = s->seed;
+    // device deadline from the host clock offset: read %globaltimer through a 1-thread probe
+    unsigned long long now_ns = 0;
+    {
+        unsigned long long *d_t = (unsigned long long *)(D.state + 8);
+        {
+            ProfScope ps(GBMP_PROF_OTHER, st);
+            k_read_clock<<<1, 32, 0, st>>>(d_t);
+        }
+        GBMP_CUDA(cudaGetLastError());
+        GBMP_CUDA(cudaMemcpyAsync(&now_ns, d_t, sizeof now_ns, cudaMemcpyDeviceToHost, st));
+        GBMP_CUDA(cudaStreamSynchronize(st));
+    }
+    const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
+    prm.deadline_ns = now_ns + (unsigned long long)(lim * 1e9);
+    cudaEvent_t e0, e1;
+    GBMP_CUDA(cudaEventCreate(&e0));
+    GBMP_CUDA(cudaEventCreate(&e1));
+    GBMP_CUDA(cudaEventRecord(e0, st));
+    gbmp_status stt = GBMP_OK;
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        const bool cull = DR.cull != 0;
+        GBMP_SPL_SWITCH2(DR.spl, {
+            auto kern = cull ? k_rrtc<SPL, true> : k_rrtc<SPL, false>;
+            cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            if (ce != cudaSuccess) { set_error("%s", cudaGetErrorString(ce)); stt = GBMP_ERR_CUDA; }
+            else kern<<<s->lanes, kRrtcThreads, smem, st>>>(DR, E, D, prm);
+        });
+    }
+    if (stt) return stt;
+    GBMP_CUDA(cudaGetLastError());
+    GBMP_CUDA(cudaEventRecord(e1, st));
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        k_rrtc_trace<<<1, 32, 0, st>>>(D, L);
+    }
+    GBMP_CUDA(cudaGetLastError());
+    int h_state[6], h_size[2], h_len = 0;
+    GBMP_CUDA(cudaMemcpyAsync(h_state, D.state, sizeof h_state, cudaMemcpyDeviceToHost, st));
+    GBMP_CUDA(cudaMemcpyAsync(h_size, D.size, sizeof h_size, cudaMemcpyDeviceToHost, st));
+    GBMP_CUDA(cudaMemcpyAsync(&h_len, D.path_len, sizeof h_len, cudaMemcpyDeviceToHost, st));
+    GBMP_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    res->status = h_state[0];
+    res->solved = h_state[0] == kStSolved;
+    res->start_tree_size = std::min(h_size[0], p->cap);
+    res->goal_tree_size = std::min(h_size[1], p->cap);
+    res->iterations = h_state[5];
+    res->kernel_ms = ms;
+    res->path_len = 0;
+    if (res->solved) {
+        if (h_len < 0 || h_len > path_cap || (h_path == nullptr)) {
+            res->path_len = h_len < 0 ? -h_len : h_len;
+            set_error("path of %d states does not fit the buffer of %d", res->path_len, path_cap);
+            return GBMP_ERR_CAPACITY;
+        }
+        GBMP_CUDA(cudaMemcpy(h_path, D.path, sizeof(float) * (size_t)h_len * L, cudaMemcpyDeviceToHost));
+        res->path_len = h_len;
+        double cost = 0.0;
+        for (int k = 1; k < h_len; ++k) {
+            double s2 = 0.0;
+            for (int j = 0; j < L; ++j)
+                if (r->active[j]) {
+                    const double d = (double)h_path[k * L + j] - h_path[(k - 1) * L + j];
+                    s2 += d * d;
+                }
+            cost += std::sqrt(s2);
+        }
+        res->cost = (float)cost;
+        return GBMP_OK;
+    }
+    if (h_state[0] == kStDeadline) {
+        set_error("no path within %.3f s", lim);
+        return GBMP_ERR_TIMEOUT;
+    }
+    set_error("no path (status %d: node cap or iteration cap)", h_state[0]);
+    return GBMP_ERR_NOT_SOLVED;
+}
+
+}  // extern "C"
+

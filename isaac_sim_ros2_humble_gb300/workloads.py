@@ -388,3 +388,37 @@ def edge_workload(seed: int = 2, n_edges: int = 65536, step: float = 0.01, shard
     q_from = robot.sample_full(rng, n_edges)
     q_to = robot.sample_full(rng, n_edges)
     return robot, env, q_from, q_to
+
+
+def planning_workload(seed: int, checker, robot: Optional[RobotModel] = None, env: Optional[Environment] = None,
+                      resolution: float = 0.01, max_draws: int = 200000):
+    """Single-problem RRT-Connect: the 7-DOF arm of plain_check_workload in the shelf scene
+    (5 slabs 0.8 x 0.3 x 0.02 m spaced 0.3 m plus 40 boxes in the cells).  Start and goal
+    are collision-free configurations drawn from `seed` whose straight joint-space edge
+    collides, so the planner has to go around.  `checker(q_batch) -> bool[n]` (True =
+    collision-free) and `edge_checker(a, b) -> bool` come from the caller."""
+    robot = robot if robot is not None else serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    env = env if env is not None else shelf_env(seed)
+    rng = np.random.default_rng(10_000 + seed)
+    free_states = []
+    drawn = 0
+    while len(free_states) < 64 and drawn < max_draws:
+        q = robot.sample_full(rng, 4096)
+        drawn += 4096
+        free_states.extend(q[checker(q)])
+    if len(free_states) < 2:
+        raise RuntimeError("scene has no collision-free configurations")
+    free_states = np.asarray(free_states, np.float32)
+    return robot, env, free_states
+
+
+def pick_problem(free_states: np.ndarray, edge_free, seed: int):
+    """First (start, goal) pair of `free_states` (in a seeded order) whose direct edge
+    collides; falls back to the first pair."""
+    rng = np.random.default_rng(20_000 + seed)
+    order = rng.permutation(len(free_states))
+    for a in range(0, len(order) - 1, 2):
+        s, g = free_states[order[a]], free_states[order[a + 1]]
+        if not edge_free(s, g):
+            return s.copy(), g.copy()
+    return free_states[order[0]].copy(), free_states[order[1]].copy()
