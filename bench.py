@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
     ap.add_argument("--edges", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="edges", choices=["edges", "plan"],
+                    help="edges: the headline edge-validation batch; plan: single-problem RRT-Connect "
+                         "time-to-solution over seeded shelf problems")
+    ap.add_argument("--plan-seeds", type=int, default=100)
+    ap.add_argument("--lanes", default="1024,2048,4096,8192")
     return ap.parse_args()
 
 
@@ -157,8 +162,106 @@ def cpu_baseline(robot, env, qf, qt):
                       f"(all states, all pairs, cost mode), OpenMP, {dt:.1f} s"}
 
 
+def gpu_problem_set(n_seeds, R, robot, api, W, torch):
+    """Seeded shelf problems with collision-free start/goal whose direct edge collides,
+    selected with the GPU checker (product path)."""
+    envs, problems = {}, []
+    for seed in range(n_seeds):
+        sc = seed % 10
+        if sc not in envs:
+            env = W.shelf_env(sc)
+            envs[sc] = (env, api.Env(env))
+        env, E = envs[sc]
+
+        def checker(q, E=E):
+            v = torch.zeros(q.shape[0], dtype=torch.uint8, device="cuda")
+            api.check_states(R, E, torch.from_numpy(q).cuda(), verdict=v)
+            return v.cpu().numpy() == 0
+
+        def edge_free(a, b, E=E):
+            ok = torch.zeros(1, dtype=torch.uint8, device="cuda")
+            api.check_edges(R, E, torch.from_numpy(a[None].copy()).cuda(), torch.from_numpy(b[None].copy()).cuda(),
+                            PLAN_RES, RULE, ok)
+            return bool(ok.item())
+
+        _, _, free = W.planning_workload(seed, checker, robot=robot, env=env)
+        start, goal = W.pick_problem(free, edge_free, seed)
+        problems.append((seed, sc, start, goal))
+    return envs, problems
+
+
+PLAN_RES = 0.01
+PLAN_RANGE = 0.1
+
+
+def run_plan(args):
+    """Single-problem parallel RRT-Connect: time to first solution over seeded shelf
+    problems (7-DOF arm, 5 slabs + 40 boxes), for several lane counts."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    import oracle as O
+    from isaac_sim_ros2_humble_gb300 import api, workloads as W
+    torch.cuda.set_device(0)
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    R = api.Robot(robot)
+    envs, problems = gpu_problem_set(args.plan_seeds, R, robot, api, W, torch)
+    planner = api.Planner(R, max_nodes=1_000_000, path_cap=65536)
+    lanes_list = [int(x) for x in args.lanes.split(",")]
+    per_lanes = {}
+    for lanes in lanes_list:
+        for seed, sc, start, goal in problems[: max(args.warmup, 1)]:
+            planner.solve(envs[sc][1], start, goal, lanes=lanes, range_=PLAN_RANGE, resolution=PLAN_RES, rule=RULE,
+                          seed=seed)
+        ms, costs, ok, kms = [], [], 0, []
+        for seed, sc, start, goal in problems:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res, path = planner.solve(envs[sc][1], start, goal, lanes=lanes, range_=PLAN_RANGE, resolution=PLAN_RES,
+                                      rule=RULE, seed=seed, time_limit_s=10.0)
+            ms.append((time.perf_counter() - t0) * 1e3)
+            kms.append(res["kernel_ms"])
+            if res["solved"]:
+                ok += 1
+                costs.append(res["cost"])
+        per_lanes[lanes] = {"p50_ms": float(np.percentile(ms, 50)), "p95_ms": float(np.percentile(ms, 95)),
+                            "p99_ms": float(np.percentile(ms, 99)), "mean_ms": float(np.mean(ms)),
+                            "kernel_p50_ms": float(np.percentile(kms, 50)), "success": ok / len(problems),
+                            "path_length_mean": float(np.mean(costs)) if costs else None,
+                            "path_length_p50": float(np.percentile(costs, 50)) if costs else None}
+    best = min(per_lanes, key=lambda k: per_lanes[k]["p50_ms"])
+    line = {"metric": "plan p50 latency", "value": per_lanes[best]["p50_ms"], "unit": "ms",
+            "n_gpus": 1, "steps": len(problems), "warmup": args.warmup, "ms_per_step": per_lanes[best]["mean_ms"],
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded shelf scenes)",
+            "config": {"workload": f"rrtc_shelf_7dof_{len(problems)}_seeds", "best_lanes": best,
+                       "range": PLAN_RANGE, "resolution": PLAN_RES, "step_rule": "linf", "max_nodes": 1_000_000,
+                       "per_lanes": per_lanes}}
+    if not args.no_cpu_baseline:
+        k = min(10, len(problems))
+        t_cpu, c_cpu, s_cpu = [], [], 0
+        for seed, sc, start, goal in problems[:k]:
+            m = O.OracleModel(robot, envs[sc][0])
+            t0 = time.perf_counter()
+            r_, p_ = O.rrtc(m, start, goal, range_=PLAN_RANGE, res=PLAN_RES, rule=RULE, seed=seed,
+                            max_nodes=200_000, max_iters=200_000)
+            t_cpu.append((time.perf_counter() - t0) * 1e3)
+            s_cpu += r_["solved"]
+            if r_["solved"]:
+                c_cpu.append(r_["cost"])
+        line["cpu_baseline"] = {"value": float(np.percentile(t_cpu, 50)), "unit": "ms", "cores": 1, "kind": "port",
+                                "sample": f"first {k} problems, sequential RRT-Connect with the same primitives "
+                                          f"(oracle), success {s_cpu}/{k}, path length mean "
+                                          f"{float(np.mean(c_cpu)) if c_cpu else None}"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "plan":
+        return run_plan(args)
     if args.impl == "reference":
         return run_reference(args)
     import torch

@@ -630,3 +630,151 @@ void or_steer(const float *from, float *to, int64_t n, int32_t J, float max_dist
         }
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Sequential RRT-Connect with the planner's primitives (the loop of          */
+/* cudampl/CPRRTC/src/RobotSolver.cu:562-796 and pRRTC/src/planning/          */
+/* pRRTC.cu:340-601 run by one thread): Philox sample (counter iteration,      */
+/* lane 0), nearest node by squared active-joint distance, steer to `range`,   */
+/* edge validation with the checkMotions step rule (state 0 skipped unless     */
+/* n == 1), append, greedy connect in ceil(d / range) steps.  The smaller tree */
+/* grows.  Returns 1 when solved; the path runs from start to goal.            */
+/* ------------------------------------------------------------------------- */
+static int state_collides(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs,
+                          const float *thr, const float *q, float *P, float *C)
+{
+    fk_one_f32(r, q, P);
+    centers_one_f32(r, P, C);
+    if (self_cost(C, np, pairs, thr) != 0.f) return 1;
+    if (env_sphere_cost(r, e, C) != 0.f) return 1;
+    if (env_cuboid_cost(r, e, C) != 0.f) return 1;
+    return env_cylinder_cost(r, e, C) != 0.f;
+}
+
+static int edge_free(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs, const float *thr,
+                     const float *a, const float *b, float res, int32_t rule, float *P, float *C, float *dir,
+                     float *st)
+{
+    const int J = r->L;
+    int32_t n = or_edge_steps(a, b, J, res, rule, dir, NULL);
+    for (int32_t k = (n == 1 ? 0 : 1); k < n; ++k) {
+        or_edge_state(a, b, dir, J, n, k, st);
+        if (state_collides(r, e, np, pairs, thr, st, P, C)) return 0;
+    }
+    return 1;
+}
+
+static int32_t tree_nearest(const float *nodes, int32_t size, int32_t J, const uint8_t *active, const float *q)
+{
+    float best = INFINITY;
+    int32_t bi = -1;
+    for (int32_t i = 0; i < size; ++i) {
+        float s = 0.f;
+        for (int j = 0; j < J; ++j)
+            if (active[j]) {
+                float d = q[j] - nodes[(int64_t)i * J + j];
+                s = fmaf(d, d, s);
+            }
+        if (s < best) { best = s; bi = i; }
+    }
+    return bi;
+}
+
+static float active_dist(const float *a, const float *b, int32_t J, const uint8_t *active)
+{
+    float s = 0.f;
+    for (int j = 0; j < J; ++j)
+        if (active[j]) { float d = b[j] - a[j]; s = fmaf(d, d, s); }
+    return sqrtf(s);
+}
+
+int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs, const float *thr,
+                const float *start, const float *goal, const uint8_t *active, const float *lower,
+                const float *upper, const float *defv, float range, float res, int32_t rule, uint64_t seed,
+                int32_t max_nodes, int32_t max_iters, float *path, int32_t path_cap, int32_t *path_len,
+                float *cost, int32_t *iters, int32_t *tree_sizes)
+{
+    const int J = r->L;
+    float *nodes[2];
+    int32_t *par[2], size[2] = {1, 1};
+    for (int t = 0; t < 2; ++t) {
+        nodes[t] = (float *)malloc(sizeof(float) * (size_t)max_nodes * J);
+        par[t] = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_nodes);
+    }
+    memcpy(nodes[0], start, sizeof(float) * J);
+    memcpy(nodes[1], goal, sizeof(float) * J);
+    par[0][0] = 0; par[1][0] = 0;
+    float *P = (float *)malloc(sizeof(float) * 16 * J), *C = (float *)malloc(sizeof(float) * 3 * (r->S + 1));
+    float *dir = (float *)malloc(sizeof(float) * J), *st = (float *)malloc(sizeof(float) * J);
+    float *qs = (float *)malloc(sizeof(float) * J), *qn = (float *)malloc(sizeof(float) * J);
+    float *qa = (float *)malloc(sizeof(float) * J), *qb = (float *)malloc(sizeof(float) * J);
+    float *qc = (float *)malloc(sizeof(float) * J);
+    int32_t solved = 0, ca = -1, cb = -1, tr_win = 0, it;
+    for (it = 0; it < max_iters && !solved; ++it) {
+        int tr = size[0] <= size[1] ? 0 : 1, ot = 1 - tr;
+        for (int j = 0; j < J; ++j) {
+            if (!active[j]) { qs[j] = defv[j]; continue; }
+            uint64_t ctr = (uint64_t)it;
+            uint32_t c4[4] = {(uint32_t)ctr, (uint32_t)(ctr >> 32), (uint32_t)j, 0u};
+            philox(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
+            float u = (float)(c4[0] >> 8) * (1.0f / 16777216.0f);
+            qs[j] = fmaf(u, upper[j] - lower[j], lower[j]);
+        }
+        int32_t nn = tree_nearest(nodes[tr], size[tr], J, active, qs);
+        memcpy(qn, nodes[tr] + (int64_t)nn * J, sizeof(float) * J);
+        float d = active_dist(qn, qs, J, active);
+        if (d > range) {
+            float sc = range / d;
+            for (int j = 0; j < J; ++j) if (active[j]) qs[j] = fmaf(sc, qs[j] - qn[j], qn[j]);
+        }
+        if (!edge_free(r, e, np, pairs, thr, qn, qs, res, rule, P, C, dir, st)) continue;
+        if (size[tr] >= max_nodes) break;
+        int32_t cur = size[tr]++;
+        memcpy(nodes[tr] + (int64_t)cur * J, qs, sizeof(float) * J);
+        par[tr][cur] = nn;
+        int32_t tgt = tree_nearest(nodes[ot], size[ot], J, active, qs);
+        memcpy(qb, nodes[ot] + (int64_t)tgt * J, sizeof(float) * J);
+        memcpy(qa, qs, sizeof(float) * J);
+        float dd = active_dist(qs, qb, J, active);
+        int32_t n_ext = (int32_t)ceilf(dd / range);
+        if (n_ext < 1) n_ext = 1;
+        int ok = 1;
+        for (int32_t k = 1; k <= n_ext && ok; ++k) {
+            for (int j = 0; j < J; ++j) qc[j] = (k == n_ext) ? qb[j] : fmaf((qb[j] - qs[j]) / (float)n_ext, (float)k, qs[j]);
+            if (!edge_free(r, e, np, pairs, thr, qa, qc, res, rule, P, C, dir, st)) { ok = 0; break; }
+            if (k < n_ext) {
+                if (size[tr] >= max_nodes) { ok = 0; break; }
+                int32_t nx = size[tr]++;
+                memcpy(nodes[tr] + (int64_t)nx * J, qc, sizeof(float) * J);
+                par[tr][nx] = cur;
+                cur = nx;
+                memcpy(qa, qc, sizeof(float) * J);
+            }
+        }
+        if (ok) { solved = 1; ca = cur; cb = tgt; tr_win = tr; }
+    }
+    *iters = it;
+    tree_sizes[0] = size[0];
+    tree_sizes[1] = size[1];
+    *path_len = 0;
+    *cost = 0.f;
+    if (solved) {
+        int32_t n0 = tr_win == 0 ? ca : cb, n1 = tr_win == 0 ? cb : ca;
+        int32_t l0 = 0, l1 = 0;
+        for (int32_t i = n0;; i = par[0][i]) { ++l0; if (i == 0) break; }
+        for (int32_t i = n1;; i = par[1][i]) { ++l1; if (i == 0) break; }
+        if (l0 + l1 <= path_cap) {
+            int32_t k = l0 - 1;
+            for (int32_t i = n0;; i = par[0][i], --k) { memcpy(path + (int64_t)k * J, nodes[0] + (int64_t)i * J, sizeof(float) * J); if (i == 0) break; }
+            k = l0;
+            for (int32_t i = n1;; i = par[1][i], ++k) { memcpy(path + (int64_t)k * J, nodes[1] + (int64_t)i * J, sizeof(float) * J); if (i == 0) break; }
+            *path_len = l0 + l1;
+            double c = 0.0;
+            for (int32_t q = 1; q < l0 + l1; ++q) c += active_dist(path + (int64_t)(q - 1) * J, path + (int64_t)q * J, J, active);
+            *cost = (float)c;
+        }
+    }
+    for (int t = 0; t < 2; ++t) { free(nodes[t]); free(par[t]); }
+    free(P); free(C); free(dir); free(st); free(qs); free(qn); free(qa); free(qb); free(qc);
+    return solved;
+}

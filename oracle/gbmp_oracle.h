@@ -92,6 +92,12 @@ void or_steer(const float *from, float *to, int64_t n, int32_t J, float max_dist
 void or_sample(const float *lower, const float *upper, const uint8_t *active, const float *defv,
                int32_t J, uint64_t seed, uint64_t offset, int64_t n, float *q);
 
+int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs, const float *thr,
+                const float *start, const float *goal, const uint8_t *active, const float *lower,
+                const float *upper, const float *defv, float range, float res, int32_t rule, uint64_t seed,
+                int32_t max_nodes, int32_t max_iters, float *path, int32_t path_cap, int32_t *path_len,
+                float *cost, int32_t *iters, int32_t *tree_sizes);
+
 int32_t or_num_threads(void);
 
 #ifdef __cplusplus

@@ -64,6 +64,10 @@ def lib():
                                  _i32p, C.c_int32]
         L.or_steer.argtypes = [_f32p, _f32p, C.c_int64, C.c_int32, C.c_float]
         L.or_sample.argtypes = [_f32p, _f32p, _u8p, _f32p, C.c_int32, C.c_uint64, C.c_uint64, C.c_int64, _f32p]
+        L.or_rrtc.argtypes = [vp, vp, C.c_int32, _i32p, _f32p, _f32p, _f32p, _u8p, _f32p, _f32p, _f32p,
+                              C.c_float, C.c_float, C.c_int32, C.c_uint64, C.c_int32, C.c_int32, _f32p, C.c_int32,
+                              C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32), _i32p]
+        L.or_rrtc.restype = C.c_int32
         L.or_num_threads.restype = C.c_int32
         _lib = L
     return _lib
@@ -186,6 +190,23 @@ class OracleModel:
         lib().or_check_motions(C.byref(self.r), C.byref(self.e), self.npairs, self.pairs, self.thr_sq,
                                f, t, E, res, rule, int(early_exit), ok, hit, ns, ln, nthreads)
         return ok.astype(bool), hit, ns, ln
+
+
+def rrtc(model, start, goal, range_=0.1, res=0.01, rule=STEP_LINF, seed=0, max_nodes=200000,
+         max_iters=200000, path_cap=65536):
+    """Sequential RRT-Connect (one thread) with the planner's primitives."""
+    rb = model.robot
+    path = np.zeros((path_cap, model.L), np.float32)
+    pl, it = C.c_int32(), C.c_int32()
+    cost = C.c_float()
+    sizes = np.zeros(2, np.int32)
+    ok = lib().or_rrtc(C.byref(model.r), C.byref(model.e), model.npairs, model.pairs, model.thr_sq,
+                       _c(start, np.float32), _c(goal, np.float32), _c(rb.active, np.uint8),
+                       _c(rb.lower, np.float32), _c(rb.upper, np.float32), _c(rb.default, np.float32),
+                       range_, res, rule, seed, max_nodes, max_iters, path, path_cap, C.byref(pl), C.byref(cost),
+                       C.byref(it), sizes)
+    return {"solved": int(ok), "path_len": pl.value, "cost": cost.value, "iterations": it.value,
+            "tree_sizes": sizes.tolist()}, path[: pl.value].copy()
 
 
 def nearest(tree, queries, active=None, cand=None, nthreads=0):
