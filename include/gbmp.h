@@ -215,6 +215,33 @@ GBMP_API gbmp_status gbmp_rrtc_solve(gbmp_planner planner, gbmp_env env, const f
                                      const float *h_goal, const gbmp_rrtc_settings *settings, float *h_path,
                                      int32_t path_cap, gbmp_rrtc_result *result, void *stream);
 
+/* ---- batched planning ----
+ * Many heterogeneous problems (different robots, scenes, start/goal) in one persistent
+ * launch: block b serves problem b % n as lane b / n.  The reference has no batched
+ * form; each result equals what the same problem gives on its own up to the lane
+ * interleaving (the first connection found wins).  With use_graph the whole solve
+ * (table upload, reset, planning, trace, result copy) is a captured CUDA graph that is
+ * replayed while the shape (n, lanes, settings, launch footprint) stays the same.
+ * h_paths: [n * path_cap * max_links] floats; problem i's path starts at
+ * i * path_cap * max_links with its robot's L floats per state. */
+typedef struct gbmp_batch_planner_s *gbmp_batch_planner;
+
+typedef struct gbmp_rrtc_problem {
+    gbmp_robot robot;
+    gbmp_env env;
+    const float *start;     /* host [L] */
+    const float *goal;      /* host [L] */
+    uint64_t seed;
+} gbmp_rrtc_problem;
+
+GBMP_API gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, int32_t max_links,
+                                               int32_t path_cap, gbmp_batch_planner *out);
+GBMP_API gbmp_status gbmp_batch_planner_destroy(gbmp_batch_planner planner);
+GBMP_API gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner planner, int32_t n, const gbmp_rrtc_problem *problems,
+                                           const gbmp_rrtc_settings *settings, int32_t lanes_per_problem,
+                                           int32_t use_graph, gbmp_rrtc_result *results, float *h_paths,
+                                           void *stream);
+
 /* ---- instrumentation ----
  * With profiling enabled, CUDA events are recorded on the launching stream around
  * every launch of the named kernel families; gbmp_profile_read() waits for them and

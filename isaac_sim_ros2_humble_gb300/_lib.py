@@ -47,6 +47,11 @@ class RrtcResult(C.Structure):
                 ("kernel_ms", C.c_double)]
 
 
+class RrtcProblem(C.Structure):
+    _fields_ = [("robot", C.c_void_p), ("env", C.c_void_p), ("start", C.c_void_p), ("goal", C.c_void_p),
+                ("seed", C.c_uint64)]
+
+
 class Limits(C.Structure):
     _fields_ = [("max_links", C.c_int32), ("max_spheres", C.c_int32), ("max_self_pairs", C.c_int32),
                 ("max_env_words", C.c_int32)]
@@ -77,6 +82,10 @@ SIGNATURES = {
     "gbmp_planner_create": [_vp, _i32, _i32, C.POINTER(_vp)],
     "gbmp_planner_destroy": [_vp],
     "gbmp_rrtc_solve": [_vp, _vp, _vp, _vp, C.POINTER(RrtcSettings), _vp, _i32, C.POINTER(RrtcResult), _vp],
+    "gbmp_batch_planner_create": [_i32, _i32, _i32, _i32, C.POINTER(_vp)],
+    "gbmp_batch_planner_destroy": [_vp],
+    "gbmp_rrtc_solve_batch": [_vp, _i32, C.POINTER(RrtcProblem), C.POINTER(RrtcSettings), _i32, _i32,
+                              C.POINTER(RrtcResult), _vp, _vp],
     "gbmp_profile_enable": [_i32],
     "gbmp_profile_reset": [],
     "gbmp_profile_read": [_i32, C.POINTER(C.c_double), C.POINTER(C.c_int64)],

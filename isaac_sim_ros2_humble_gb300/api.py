@@ -181,3 +181,54 @@ class Planner:
         out["status_code"] = status
         path = self._path[: res.path_len].copy() if res.solved else np.zeros((0, self.robot.L), np.float32)
         return out, path
+
+
+class BatchPlanner:
+    """Many heterogeneous RRT-Connect problems per launch (see gbmp_rrtc_solve_batch)."""
+
+    def __init__(self, max_problems: int = 256, max_nodes: int = 32768, max_links: int = 16,
+                 path_cap: int = 4096):
+        h = C.c_void_p()
+        check(_lib.load().gbmp_batch_planner_create(int(max_problems), int(max_nodes), int(max_links),
+                                                    int(path_cap), C.byref(h)))
+        self.handle = h
+        self.max_problems, self.max_links, self.path_cap = int(max_problems), int(max_links), int(path_cap)
+        self._paths = np.zeros((self.max_problems, self.path_cap, self.max_links), np.float32)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().gbmp_batch_planner_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, problems, lanes_per_problem: int = 8, use_graph: bool = True, max_iters: int = 100000,
+              range_: float = 0.1, resolution: float = 0.0, rule: int = _lib.STEP_L2, time_limit_s: float = 10.0,
+              stream=None):
+        """problems: list of (Robot, Env, start[L], goal[L], seed).  Returns a list of
+        (result dict, path [path_len, L])."""
+        n = len(problems)
+        arr = (_lib.RrtcProblem * n)()
+        keep = []
+        for i, (R, E, s0, g0, seed) in enumerate(problems):
+            a, b = _c(s0, np.float32).reshape(-1), _c(g0, np.float32).reshape(-1)
+            keep += [a, b]
+            arr[i] = _lib.RrtcProblem(R.handle.value, E.handle.value, a.ctypes.data, b.ctypes.data, int(seed))
+        st = _lib.RrtcSettings(0, int(max_iters), float(range_), float(resolution), int(rule), 0, float(time_limit_s))
+        res = (_lib.RrtcResult * n)()
+        paths = self._paths[:n]
+        check(_lib.load().gbmp_rrtc_solve_batch(self.handle, n, arr, C.byref(st), int(lanes_per_problem),
+                                                int(bool(use_graph)), res, paths.ctypes.data,
+                                                stream_handle(stream)))
+        out = []
+        flat = self._paths.reshape(self.max_problems, -1)
+        for i in range(n):
+            r = {f: getattr(res[i], f) for f, _ in _lib.RrtcResult._fields_}
+            L = problems[i][0].L
+            p = flat[i, : r["path_len"] * L].reshape(-1, L).copy() if r["solved"] else np.zeros((0, L), np.float32)
+            out.append((r, p))
+        return out

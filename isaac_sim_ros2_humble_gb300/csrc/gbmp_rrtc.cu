@@ -49,7 +49,8 @@ struct RrtcParams {
     int lanes, max_iters, rule;
     float range, res;
     unsigned long long seed;
-    unsigned long long deadline_ns;   // absolute %globaltimer value
+    unsigned long long deadline_ns;   // absolute %globaltimer value, or
+    const unsigned long long *deadline_ptr;   // read from device memory when non-null
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -160,8 +161,11 @@ __device__ int block_append(const RrtcDev &P, int tr, const float *q, int par, i
     return idx;
 }
 
+// One extension lane of one problem (the body of both the single-problem and the
+// batched planning kernels).  All threads of the block call it.
 template <int SPL, bool CULL>
-__global__ void __launch_bounds__(kRrtcThreads) k_rrtc(DevRobot R, DevEnv E, RrtcDev P, RrtcParams prm) {
+__device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, const RrtcParams &prm,
+                          const int lane_id) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
@@ -181,13 +185,12 @@ __global__ void __launch_bounds__(kRrtcThreads) k_rrtc(DevRobot R, DevEnv E, Rrt
     for (int j = threadIdx.x; j < R.L; j += blockDim.x) act[j] = R.active[j];
     __syncthreads();
 
-    const int lane_id = blockIdx.x;
     const int L = R.L;
     for (int it = 0;; ++it) {
         if (threadIdx.x == 0) {
             int st = *(volatile int *)P.state;
             if (st == kStRunning && it >= prm.max_iters) st = kStIterCap;
-            if (st == kStRunning && global_ns() > prm.deadline_ns) {
+            if (st == kStRunning && global_ns() > (prm.deadline_ptr ? *prm.deadline_ptr : prm.deadline_ns)) {
                 atomicCAS(P.state, kStRunning, kStDeadline);
                 st = kStDeadline;
             }
@@ -297,6 +300,84 @@ __global__ void __launch_bounds__(kRrtcThreads) k_rrtc(DevRobot R, DevEnv E, Rrt
     }
 }
 
+template <int SPL, bool CULL>
+__global__ void __launch_bounds__(kRrtcThreads) k_rrtc(DevRobot R, DevEnv E, RrtcDev P, RrtcParams prm) {
+    rrtc_lane<SPL, CULL>(R, E, P, prm, blockIdx.x);
+}
+
+// A problem of a batched launch: its robot, scene, trees and Philox key.
+struct BatchProblem {
+    DevRobot R;
+    DevEnv E;
+    RrtcDev P;
+    unsigned long long seed;
+    const float *start, *goal;      // device copies of the roots
+    int prev[2];                    // slots used by the previous solve (to reset)
+};
+
+// Batched planning: block b serves problem b % n as lane b / n, so every problem gets
+// lanes from the first wave of resident blocks.  The problem's descriptors are copied
+// into shared memory once.
+template <int SPL, bool CULL>
+__global__ void __launch_bounds__(kRrtcThreads) k_rrtc_batch(const BatchProblem *__restrict__ probs, int n,
+                                                            int lanes_per_problem, RrtcParams prm) {
+    __shared__ DevRobot sR;
+    __shared__ DevEnv sE;
+    __shared__ RrtcDev sP;
+    __shared__ unsigned long long sSeed;
+    const int p = blockIdx.x % n;
+    if (threadIdx.x == 0) {
+        sR = probs[p].R;
+        sE = probs[p].E;
+        sP = probs[p].P;
+        sSeed = probs[p].seed;
+    }
+    __syncthreads();
+    RrtcParams q = prm;
+    q.lanes = lanes_per_problem;
+    q.seed = sSeed;
+    rrtc_lane<SPL, CULL>(sR, sE, sP, q, blockIdx.x / n);
+}
+
+// Reset of every problem of a batch: NaN sentinels over the slots the previous solve
+// used, roots from the staged start / goal, counters to zero.
+__global__ void k_rrtc_batch_reset(BatchProblem *__restrict__ probs, int n, unsigned long long *deadline,
+                                   unsigned long long limit_ns) {
+    const int p = blockIdx.y;
+    if (p == 0 && blockIdx.x == 0 && threadIdx.x == 0) *deadline = global_ns() + limit_ns;
+    if (p >= n) return;
+    BatchProblem &b = probs[p];
+    const int L = b.R.L;
+    for (int t = 0; t < 2; ++t) {
+        const long long words = (long long)max(b.prev[t], 1) * b.P.stride;
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < words;
+             i += (long long)gridDim.x * blockDim.x)
+            b.P.nodes[t][i] = __int_as_float(0xffffffff);
+    }
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        for (int j = threadIdx.x; j < L; j += blockDim.x) {
+            b.P.nodes[0][j] = b.start[j];
+            b.P.nodes[1][j] = b.goal[j];
+        }
+        if (threadIdx.x == 0) {
+            b.P.parent[0][0] = 0;
+            b.P.parent[1][0] = 0;
+            b.P.size[0] = 1;
+            b.P.size[1] = 1;
+            for (int k = 0; k < 12; ++k) b.P.state[k] = 0;
+        }
+    }
+}
+
+// Record the used slots for the next reset.
+__global__ void k_rrtc_batch_finish(BatchProblem *__restrict__ probs, int n) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    probs[p].prev[0] = min(probs[p].P.size[0], probs[p].P.cap);
+    probs[p].prev[1] = min(probs[p].P.size[1], probs[p].P.cap);
+}
+
 __global__ void k_read_clock(unsigned long long *t) {
     if (threadIdx.x == 0) *t = global_ns();
 }
@@ -320,6 +401,42 @@ __global__ void k_rrtc_trace(RrtcDev P, int L) {
     for (int i = nb; i >= 0; i = (P.parent[1][i] == i ? -1 : P.parent[1][i]), ++k)
         for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[1][(long long)i * P.stride + j];
     *P.path_len = len0 + len1;
+}
+
+__global__ void k_rrtc_batch_trace(const BatchProblem *__restrict__ probs, int n, int *__restrict__ summary) {
+    const int p = blockIdx.x;
+    if (p >= n) return;
+    if (threadIdx.x == 0) {
+        const RrtcDev &P = probs[p].P;
+        // reuse the single-problem trace (one thread)
+        const int L = probs[p].R.L;
+        if (P.state[0] != kStSolved) {
+            *P.path_len = 0;
+        } else {
+            const int tr = P.state[2], a = P.state[3], b = P.state[4];
+            const int na = tr == 0 ? a : b, nb = tr == 0 ? b : a;
+            int len0 = 0, len1 = 0;
+            for (int i = na; i >= 0 && len0 <= P.cap; i = (P.parent[0][i] == i ? -1 : P.parent[0][i])) ++len0;
+            for (int i = nb; i >= 0 && len1 <= P.cap; i = (P.parent[1][i] == i ? -1 : P.parent[1][i])) ++len1;
+            if (len0 + len1 > P.path_cap || len0 > P.cap || len1 > P.cap) {
+                *P.path_len = -(len0 + len1);
+            } else {
+                int k = len0 - 1;
+                for (int i = na; i >= 0; i = (P.parent[0][i] == i ? -1 : P.parent[0][i]), --k)
+                    for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[0][(long long)i * P.stride + j];
+                k = len0;
+                for (int i = nb; i >= 0; i = (P.parent[1][i] == i ? -1 : P.parent[1][i]), ++k)
+                    for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[1][(long long)i * P.stride + j];
+                *P.path_len = len0 + len1;
+            }
+        }
+        int *o = summary + 8 * p;
+        o[0] = P.state[0];
+        o[1] = *P.path_len;
+        o[2] = min(P.size[0], P.cap);
+        o[3] = min(P.size[1], P.cap);
+        o[4] = P.state[5];
+    }
 }
 
 #define GBMP_SPL_SWITCH2(spl, ...)                          \
@@ -437,6 +554,7 @@ gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, 
     }
     const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
     prm.deadline_ns = now_ns + (unsigned long long)(lim * 1e9);
+    prm.deadline_ptr = nullptr;
     cudaEvent_t e0, e1;
     GBMP_CUDA(cudaEventCreate(&e0));
     GBMP_CUDA(cudaEventCreate(&e1));
@@ -507,3 +625,267 @@ gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, 
 
 }  // extern "C"
 
+
+// ---------------------------------------------------------------------------------
+// Batched planning (many heterogeneous problems in one persistent launch).
+// ---------------------------------------------------------------------------------
+struct gbmp_batch_planner_s {
+    int max_problems = 0, cap = 0, max_links = 0, path_cap = 0, stride = 0;
+    void *pool = nullptr;                 // per-problem trees, parents, ints, paths
+    size_t per_problem = 0;
+    BatchProblem *d_table = nullptr;      // device problem table
+    BatchProblem *h_table = nullptr;      // pinned host mirror
+    float *d_roots = nullptr, *h_roots = nullptr;   // [max_problems * 2 * max_links]
+    int *d_summary = nullptr, *h_summary = nullptr; // [max_problems * 8]
+    unsigned long long *d_deadline = nullptr;
+    std::vector<int> prev;                // 2 per problem
+    // captured graph and its key
+    cudaGraphExec_t exec = nullptr;
+    long long key[8] = {0};
+    std::mutex mu;
+};
+
+static gbmp_status batch_launch(gbmp_batch_planner b, int n, int lpp, const RrtcParams &prm, int spl, bool cull,
+                                size_t smem, double limit_s, cudaStream_t st) {
+    GBMP_CUDA(cudaMemcpyAsync(b->d_table, b->h_table, sizeof(BatchProblem) * n, cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(b->d_roots, b->h_roots, sizeof(float) * (size_t)n * 2 * b->max_links,
+                              cudaMemcpyHostToDevice, st));
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        k_rrtc_batch_reset<<<dim3(8, n), 256, 0, st>>>(b->d_table, n, b->d_deadline,
+                                                      (unsigned long long)(limit_s * 1e9));
+    }
+    GBMP_CUDA(cudaGetLastError());
+    gbmp_status stt = GBMP_OK;
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        GBMP_SPL_SWITCH2(spl, {
+            auto kern = cull ? k_rrtc_batch<SPL, true> : k_rrtc_batch<SPL, false>;
+            cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            if (ce != cudaSuccess) { set_error("%s", cudaGetErrorString(ce)); stt = GBMP_ERR_CUDA; }
+            else kern<<<n * lpp, kRrtcThreads, smem, st>>>(b->d_table, n, lpp, prm);
+        });
+    }
+    if (stt) return stt;
+    GBMP_CUDA(cudaGetLastError());
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        k_rrtc_batch_trace<<<n, 32, 0, st>>>(b->d_table, n, b->d_summary);
+    }
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        k_rrtc_batch_finish<<<(n + 127) / 128, 128, 0, st>>>(b->d_table, n);
+    }
+    GBMP_CUDA(cudaGetLastError());
+    GBMP_CUDA(cudaMemcpyAsync(b->h_summary, b->d_summary, sizeof(int) * 8 * n, cudaMemcpyDeviceToHost, st));
+    return GBMP_OK;
+}
+
+extern "C" {
+
+gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, int32_t max_links, int32_t path_cap,
+                                      gbmp_batch_planner *out) {
+    GBMP_CHECK_ARG(out, "out is NULL");
+    *out = nullptr;
+    GBMP_CHECK_ARG(max_problems >= 1 && max_problems <= 65535, "max_problems %d outside [1, 65535]", max_problems);
+    GBMP_CHECK_ARG(max_nodes >= 2 && max_nodes <= (1 << 24), "max_nodes %d outside [2, 2^24]", max_nodes);
+    GBMP_CHECK_ARG(max_links >= 1 && max_links <= kMaxLinks, "max_links %d outside [1, %d]", max_links, kMaxLinks);
+    GBMP_CHECK_ARG(path_cap >= 2, "path_cap < 2");
+    auto *b = new gbmp_batch_planner_s();
+    b->max_problems = max_problems;
+    b->cap = max_nodes;
+    b->max_links = max_links;
+    b->path_cap = path_cap;
+    b->stride = (max_links + 3) & ~3;
+    const size_t nodes_b = align16(sizeof(float) * (size_t)max_nodes * b->stride);
+    const size_t par_b = align16(sizeof(int) * (size_t)max_nodes);
+    b->per_problem = 2 * nodes_b + 2 * par_b + 256 + align16(sizeof(float) * (size_t)path_cap * max_links);
+    cudaError_t e = cudaMalloc(&b->pool, b->per_problem * max_problems);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(BatchProblem) * max_problems);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_table, sizeof(BatchProblem) * max_problems);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_roots, sizeof(float) * (size_t)max_problems * 2 * max_links);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_roots, sizeof(float) * (size_t)max_problems * 2 * max_links);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_summary, sizeof(int) * 8 * max_problems);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_summary, sizeof(int) * 8 * max_problems);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_deadline, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        set_error("batch planner allocation failed: %s", cudaGetErrorString(e));
+        gbmp_batch_planner_destroy(b);
+        return e == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+    }
+    // every tree starts fully reset once
+    e = cudaMemset(b->pool, 0xff, b->per_problem * max_problems);
+    if (e != cudaSuccess) {
+        set_error("batch planner reset failed: %s", cudaGetErrorString(e));
+        gbmp_batch_planner_destroy(b);
+        return GBMP_ERR_CUDA;
+    }
+    b->prev.assign(2 * max_problems, 1);
+    *out = b;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_batch_planner_destroy(gbmp_batch_planner b) {
+    if (!b) return GBMP_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->pool) cudaFree(b->pool);
+    if (b->d_table) cudaFree(b->d_table);
+    if (b->h_table) cudaFreeHost(b->h_table);
+    if (b->d_roots) cudaFree(b->d_roots);
+    if (b->h_roots) cudaFreeHost(b->h_roots);
+    if (b->d_summary) cudaFree(b->d_summary);
+    if (b->h_summary) cudaFreeHost(b->h_summary);
+    if (b->d_deadline) cudaFree(b->d_deadline);
+    delete b;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rrtc_problem *problems,
+                                  const gbmp_rrtc_settings *s, int32_t lanes_per_problem, int32_t use_graph,
+                                  gbmp_rrtc_result *results, float *h_paths, void *stream) {
+    GBMP_CHECK_ARG(b && problems && s && results, "NULL argument");
+    GBMP_CHECK_ARG(n >= 1 && n <= b->max_problems, "n %d outside [1, %d]", n, b->max_problems);
+    GBMP_CHECK_ARG(lanes_per_problem >= 1 && lanes_per_problem <= 4096, "lanes_per_problem outside [1, 4096]");
+    GBMP_CHECK_ARG((long long)n * lanes_per_problem <= (1LL << 30), "too many blocks");
+    GBMP_CHECK_ARG(s->range > 0.f && s->max_iters >= 1, "bad settings");
+    GBMP_CHECK_ARG(s->step_rule == GBMP_STEP_L2 || s->step_rule == GBMP_STEP_LINF, "unknown step rule");
+    std::lock_guard<std::mutex> lock(b->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    int spl = 1;
+    bool cull = true;
+    size_t smem = 0;
+    auto *pool = static_cast<unsigned char *>(b->pool);
+    const size_t nodes_b = align16(sizeof(float) * (size_t)b->cap * b->stride);
+    const size_t par_b = align16(sizeof(int) * (size_t)b->cap);
+    for (int i = 0; i < n; ++i) {
+        const gbmp_rrtc_problem &pr = problems[i];
+        GBMP_CHECK_ARG(pr.robot && pr.env && pr.start && pr.goal, "problem %d has a NULL field", i);
+        GBMP_CHECK_ARG(pr.robot->L <= b->max_links, "problem %d: %d links > max_links %d", i, pr.robot->L,
+                       b->max_links);
+        const DevRobot &R = pr.robot->dev;
+        const DevEnv E = pr.env->dev();
+        spl = std::max(spl, R.spl);
+        cull = cull && R.cull;
+        smem = std::max(smem, smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) + smem_warp_bytes(R) * kRrtcWarps +
+                                  6 * kMaxLinks * 4 + 256);
+        BatchProblem &bp = b->h_table[i];
+        bp.R = R;
+        bp.R.work = nullptr;
+        bp.E = E;
+        unsigned char *base = pool + b->per_problem * i;
+        bp.P.nodes[0] = (float *)base;
+        bp.P.nodes[1] = (float *)(base + nodes_b);
+        bp.P.parent[0] = (int *)(base + 2 * nodes_b);
+        bp.P.parent[1] = (int *)(base + 2 * nodes_b + par_b);
+        int *ints = (int *)(base + 2 * nodes_b + 2 * par_b);
+        bp.P.size = ints;
+        bp.P.state = ints + 4;
+        bp.P.path_len = ints + 16;
+        bp.P.path = (float *)(base + 2 * nodes_b + 2 * par_b + 256);
+        bp.P.cap = b->cap;
+        bp.P.stride = b->stride;
+        bp.P.path_cap = b->path_cap;
+        bp.seed = pr.seed;
+        bp.start = b->d_roots + (size_t)i * 2 * b->max_links;
+        bp.goal = bp.start + b->max_links;
+        bp.prev[0] = b->prev[2 * i];
+        bp.prev[1] = b->prev[2 * i + 1];
+        for (int j = 0; j < pr.robot->L; ++j) {
+            GBMP_CHECK_ARG(std::isfinite(pr.start[j]) && std::isfinite(pr.goal[j]), "problem %d: start/goal not finite", i);
+            b->h_roots[(size_t)i * 2 * b->max_links + j] = pr.start[j];
+            b->h_roots[(size_t)i * 2 * b->max_links + b->max_links + j] = pr.goal[j];
+        }
+    }
+    RrtcParams prm;
+    prm.lanes = lanes_per_problem;
+    prm.max_iters = s->max_iters;
+    prm.rule = s->step_rule;
+    prm.range = s->range;
+    prm.res = s->resolution > 0.f ? s->resolution : problems[0].robot->resolution;
+    prm.seed = 0;
+    prm.deadline_ns = 0;
+    prm.deadline_ptr = b->d_deadline;
+    const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
+    cudaEvent_t e0, e1;
+    GBMP_CUDA(cudaEventCreate(&e0));
+    GBMP_CUDA(cudaEventCreate(&e1));
+    GBMP_CUDA(cudaEventRecord(e0, st));
+    if (use_graph) {
+        const long long key[8] = {n, lanes_per_problem, (long long)smem, spl, cull, s->max_iters,
+                                  (long long)(lim * 1e6), (long long)(prm.range * 1e6) ^ ((long long)(prm.res * 1e9) << 20)};
+        if (!b->exec || memcmp(key, b->key, sizeof key) != 0) {
+            if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+            cudaStream_t cap_st;
+            GBMP_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
+            GBMP_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
+            gbmp_status bs = batch_launch(b, n, lanes_per_problem, prm, spl, cull, smem, lim, cap_st);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(cap_st, &g);
+            cudaStreamDestroy(cap_st);
+            if (bs) { if (g) cudaGraphDestroy(g); return bs; }
+            if (ce != cudaSuccess) { set_error("graph capture failed: %s", cudaGetErrorString(ce)); return GBMP_ERR_CUDA; }
+            ce = cudaGraphInstantiate(&b->exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) { set_error("graph instantiate failed: %s", cudaGetErrorString(ce)); return GBMP_ERR_CUDA; }
+            memcpy(b->key, key, sizeof key);
+        }
+        count_launch(4);
+        GBMP_CUDA(cudaGraphLaunch(b->exec, st));
+    } else {
+        gbmp_status bs = batch_launch(b, n, lanes_per_problem, prm, spl, cull, smem, lim, st);
+        if (bs) return bs;
+    }
+    GBMP_CUDA(cudaEventRecord(e1, st));
+    GBMP_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int max_len = 0;
+    for (int i = 0; i < n; ++i) {
+        const int *o = b->h_summary + 8 * i;
+        gbmp_rrtc_result &r = results[i];
+        memset(&r, 0, sizeof r);
+        r.status = o[0];
+        r.solved = o[0] == kStSolved && o[1] > 0;
+        r.path_len = o[1] > 0 ? o[1] : 0;
+        r.start_tree_size = o[2];
+        r.goal_tree_size = o[3];
+        r.iterations = o[4];
+        r.kernel_ms = ms;
+        b->prev[2 * i] = std::max(o[2], 1);
+        b->prev[2 * i + 1] = std::max(o[3], 1);
+        max_len = std::max(max_len, r.path_len);
+    }
+    if (h_paths && max_len > 0) {
+        // one pitched copy: rows of max_len * L floats from every problem's path buffer
+        const size_t pitch_src = b->per_problem;
+        const size_t row = sizeof(float) * (size_t)max_len * b->max_links;
+        const size_t pitch_dst = sizeof(float) * (size_t)b->path_cap * b->max_links;
+        if (row <= pitch_dst) {
+            GBMP_CUDA(cudaMemcpy2DAsync(h_paths, pitch_dst, b->h_table[0].P.path, pitch_src, row, n,
+                                        cudaMemcpyDeviceToHost, st));
+            GBMP_CUDA(cudaStreamSynchronize(st));
+        }
+        for (int i = 0; i < n; ++i) {
+            gbmp_rrtc_result &r = results[i];
+            if (!r.solved) continue;
+            const int L = problems[i].robot->L;
+            const float *pth = h_paths + (size_t)i * b->path_cap * b->max_links;
+            double cost = 0.0;
+            for (int k = 1; k < r.path_len; ++k) {
+                double s2 = 0.0;
+                for (int j = 0; j < L; ++j)
+                    if (problems[i].robot->active[j]) {
+                        const double d = (double)pth[k * L + j] - pth[(k - 1) * L + j];
+                        s2 += d * d;
+                    }
+                cost += std::sqrt(s2);
+            }
+            r.cost = (float)cost;
+        }
+    }
+    return GBMP_OK;
+}
+
+}  // extern "C"

@@ -422,3 +422,23 @@ def pick_problem(free_states: np.ndarray, edge_free, seed: int):
         if not edge_free(s, g):
             return s.copy(), g.copy()
     return free_states[order[0]].copy(), free_states[order[1]].copy()
+
+
+def uneven_batch_models(seed: int, n: int = 256):
+    """Robots and scenes of the uneven batch: DOF U{6..9} (8 and 9 with a prismatic
+    torso), link spheres U[30, 120], obstacles U[10, 500] split 76 / 19 / 5 % into
+    spheres / oriented boxes / cylinders (the 256 : 64 : 16 proportions)."""
+    rng = np.random.default_rng(30_000 + seed)
+    out = []
+    for i in range(n):
+        dof = int(rng.integers(6, 10))
+        S = int(rng.integers(30, 121))
+        O = int(rng.integers(10, 501))
+        nb = int(round(O * 64 / 336))
+        nc = int(round(O * 16 / 336))
+        ns = O - nb - nc
+        robot = serial_arm(40_000 + 7 * seed + i, dof=dof, n_spheres=S, prismatic_torso=dof >= 8,
+                           name=f"arm{dof}_b{i}", resolution=0.01)
+        env = random_env(50_000 + 7 * seed + i, ns, nb, nc, oriented=True)
+        out.append((robot, env))
+    return out
