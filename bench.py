@@ -269,7 +269,15 @@ def run_batch(args):
     from isaac_sim_ros2_humble_gb300 import api, workloads as W
     torch.cuda.set_device(0)
     n = 256
-    models = W.uneven_batch_models(0, n=n)
+
+    def feasible(robot, env):
+        R_, E_ = api.Robot(robot), api.Env(env)
+        q = robot.sample_full(np.random.default_rng(0), 2000)
+        v = torch.zeros(q.shape[0], dtype=torch.uint8, device="cuda")
+        api.check_states(R_, E_, torch.from_numpy(q).cuda(), verdict=v)
+        return float((v == 0).float().mean().item()) >= 0.02
+
+    models = W.uneven_batch_models(0, n=n, feasible=feasible)
     problems = []
     for i, (robot, env) in enumerate(models):
         R, E = api.Robot(robot), api.Env(env)

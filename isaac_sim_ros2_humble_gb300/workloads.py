@@ -424,10 +424,14 @@ def pick_problem(free_states: np.ndarray, edge_free, seed: int):
     return free_states[order[0]].copy(), free_states[order[1]].copy()
 
 
-def uneven_batch_models(seed: int, n: int = 256):
+def uneven_batch_models(seed: int, n: int = 256, feasible=None):
     """Robots and scenes of the uneven batch: DOF U{6..9} (8 and 9 with a prismatic
     torso), link spheres U[30, 120], obstacles U[10, 500] split 76 / 19 / 5 % into
-    spheres / oriented boxes / cylinders (the 256 : 64 : 16 proportions)."""
+    spheres / oriented boxes / cylinders (the 256 : 64 : 16 proportions).  The obstacle
+    cube grows with the count so that the density stays near that of a 120-obstacle
+    scene.  `feasible(robot, env) -> bool`, if given, rejects a scene (for example one
+    without collision-free configurations) and the next scene seed of that problem is
+    tried, up to 16 times."""
     rng = np.random.default_rng(30_000 + seed)
     out = []
     for i in range(n):
@@ -439,6 +443,39 @@ def uneven_batch_models(seed: int, n: int = 256):
         ns = O - nb - nc
         robot = serial_arm(40_000 + 7 * seed + i, dof=dof, n_spheres=S, prismatic_torso=dof >= 8,
                            name=f"arm{dof}_b{i}", resolution=0.01)
-        env = random_env(50_000 + 7 * seed + i, ns, nb, nc, oriented=True)
+        size = 1.2 * max(1.0, (O / 120.0) ** (1.0 / 3.0))
+        for attempt in range(16):
+            k = 50_000 + 7 * seed + i + 100_003 * attempt
+            env = random_env(k, ns, nb, nc, oriented=True, size=size,
+                             center=(SCENE_CENTER[0] + (size - 1.2) / 2, 0.0, SCENE_CENTER[2]))
+            env = prune_blocking_obstacles(robot, env, np.random.default_rng(k + 10_000))
+            if feasible is None or feasible(robot, env):
+                break
         out.append((robot, env))
     return out
+
+
+def prune_blocking_obstacles(robot: RobotModel, env: Environment, rng: np.random.Generator,
+                             samples: int = 256, always: float = 0.9) -> Environment:
+    """Drop obstacles whose bounding sphere meets the robot in at least `always` of
+    random configurations (obstacles sitting in the permanently swept volume around the
+    base would make every configuration collide)."""
+    q = robot.sample_full(rng, samples)
+    C = sphere_centers_numpy(robot, q)                                   # [N,S,3]
+    r = robot.sphere_r.astype(np.float64)
+
+    def blocked(pos, rad):
+        if len(pos) == 0:
+            return np.zeros(0, bool)
+        d = np.linalg.norm(C[:, :, None, :] - pos[None, None].astype(np.float64), axis=-1)   # [N,S,O]
+        hit = (d < (r[None, :, None] + rad[None, None])).any(1)
+        return hit.mean(0) >= always
+
+    bs = blocked(env.sphere_pos, env.sphere_r.astype(np.float64))
+    bh = np.linalg.norm(np.maximum(np.abs(env.box_min), np.abs(env.box_max)), axis=1) if len(env.box_pos) else np.zeros(0)
+    bb = blocked(env.box_pos, bh)
+    ch = np.hypot(env.cyl_radius, env.cyl_height / 2) if len(env.cyl_pos) else np.zeros(0)
+    bc = blocked(env.cyl_pos, ch)
+    return Environment(env.sphere_pos[~bs], env.sphere_r[~bs], env.box_pos[~bb], env.box_rot[~bb],
+                       env.box_min[~bb], env.box_max[~bb], env.cyl_pos[~bc], env.cyl_rot[~bc],
+                       env.cyl_radius[~bc], env.cyl_height[~bc])

@@ -15,7 +15,11 @@ RES, RULE = 0.01, _lib.STEP_LINF
 
 @pytest.fixture(scope="module")
 def batch():
-    models = W.uneven_batch_models(1, n=24)
+    def feasible(robot, env):
+        q = robot.sample_full(np.random.default_rng(0), 1000)
+        return (O.OracleModel(robot, env).check_states(q)[1] == 0).mean() >= 0.02
+
+    models = W.uneven_batch_models(1, n=24, feasible=feasible)
     probs, oracles = [], []
     for i, (robot, env) in enumerate(models):
         m = O.OracleModel(robot, env)
