@@ -565,8 +565,11 @@ gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, 
         const bool cull = DR.cull != 0;
         GBMP_SPL_SWITCH2(DR.spl, {
             auto kern = cull ? k_rrtc<SPL, true> : k_rrtc<SPL, false>;
-            cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-            if (ce != cudaSuccess) { set_error("%s", cudaGetErrorString(ce)); stt = GBMP_ERR_CUDA; }
+            cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (ce != cudaSuccess) {
+                set_error("planning kernel needs %zu bytes of shared memory: %s", smem, cudaGetErrorString(ce));
+                stt = ce == cudaErrorInvalidValue ? GBMP_ERR_CAPACITY : GBMP_ERR_CUDA;
+            }
             else kern<<<s->lanes, kRrtcThreads, smem, st>>>(DR, E, D, prm);
         });
     }
@@ -661,8 +664,11 @@ static gbmp_status batch_launch(gbmp_batch_planner b, int n, int lpp, const Rrtc
         ProfScope ps(GBMP_PROF_OTHER, st);
         GBMP_SPL_SWITCH2(spl, {
             auto kern = cull ? k_rrtc_batch<SPL, true> : k_rrtc_batch<SPL, false>;
-            cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-            if (ce != cudaSuccess) { set_error("%s", cudaGetErrorString(ce)); stt = GBMP_ERR_CUDA; }
+            cudaError_t ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (ce != cudaSuccess) {
+                set_error("planning kernel needs %zu bytes of shared memory: %s", smem, cudaGetErrorString(ce));
+                stt = ce == cudaErrorInvalidValue ? GBMP_ERR_CAPACITY : GBMP_ERR_CUDA;
+            }
             else kern<<<n * lpp, kRrtcThreads, smem, st>>>(b->d_table, n, lpp, prm);
         });
     }
