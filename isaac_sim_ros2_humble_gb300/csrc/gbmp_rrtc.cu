@@ -198,7 +198,10 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
             // tree choice: a share of the lanes proportional to the other tree's size
             const int n0 = *(volatile int *)(P.size), n1 = *(volatile int *)(P.size + 1);
             const float ratio = (float)n0 / (float)max(n0 + n1, 1);
-            s_misc[1] = ((float)(lane_id % prm.lanes) < (float)prm.lanes * (1.f - ratio)) ? 0 : 1;
+            // lanes hashed to [0, 1) (Fibonacci hashing) grow tree 0 below 1 - ratio, so the
+            // smaller tree gets the larger share of lanes whatever the lane count
+            const float h = (float)(((unsigned)lane_id * 2654435769u) >> 8) * (1.0f / 16777216.0f);
+            s_misc[1] = h < 1.f - ratio ? 0 : 1;
             s_misc[2] = min(n0, P.cap);
             s_misc[3] = min(n1, P.cap);
         }
@@ -320,23 +323,44 @@ struct BatchProblem {
 // into shared memory once.
 template <int SPL, bool CULL>
 __global__ void __launch_bounds__(kRrtcThreads) k_rrtc_batch(const BatchProblem *__restrict__ probs, int n,
-                                                            int lanes_per_problem, RrtcParams prm) {
+                                                            int lanes_per_problem, RrtcParams prm, int *rr) {
     __shared__ DevRobot sR;
     __shared__ DevEnv sE;
     __shared__ RrtcDev sP;
     __shared__ unsigned long long sSeed;
-    const int p = blockIdx.x % n;
-    if (threadIdx.x == 0) {
-        sR = probs[p].R;
-        sE = probs[p].E;
-        sP = probs[p].P;
-        sSeed = probs[p].seed;
+    __shared__ int sLane, sNext;
+    int p = blockIdx.x % n;
+    // A block stays with a problem until it ends (solved, capped or deadline), then
+    // migrates to a problem that is still running, so the lanes of easy problems end up
+    // helping the hard ones.  Each stay ends a problem, so there are at most n hops.
+    for (int hop = 0; hop <= n; ++hop) {
+        if (threadIdx.x == 0) {
+            sR = probs[p].R;
+            sE = probs[p].E;
+            sP = probs[p].P;
+            sSeed = probs[p].seed;
+            sLane = atomicAdd(probs[p].P.state + 6, 1);
+        }
+        __syncthreads();
+        RrtcParams q = prm;
+        q.lanes = lanes_per_problem;
+        q.seed = sSeed;
+        rrtc_lane<SPL, CULL>(sR, sE, sP, q, sLane);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int next = -1;
+            const int start = (int)((unsigned)atomicAdd(rr, 1) % (unsigned)n);
+            for (int k = 0; k < n; ++k) {
+                const int c = (start + k) % n;
+                if (*(volatile int *)probs[c].P.state == kStRunning) { next = c; break; }
+            }
+            sNext = next;
+        }
+        __syncthreads();
+        if (sNext < 0) break;
+        p = sNext;
+        __syncthreads();
     }
-    __syncthreads();
-    RrtcParams q = prm;
-    q.lanes = lanes_per_problem;
-    q.seed = sSeed;
-    rrtc_lane<SPL, CULL>(sR, sE, sP, q, blockIdx.x / n);
 }
 
 // Reset of every problem of a batch: NaN sentinels over the slots the previous solve
@@ -640,7 +664,7 @@ struct gbmp_batch_planner_s {
     BatchProblem *h_table = nullptr;      // pinned host mirror
     float *d_roots = nullptr, *h_roots = nullptr;   // [max_problems * 2 * max_links]
     int *d_summary = nullptr, *h_summary = nullptr; // [max_problems * 8]
-    unsigned long long *d_deadline = nullptr;
+    unsigned long long *d_deadline = nullptr;   // [0] deadline, [1] round-robin counter
     std::vector<int> prev;                // 2 per problem
     // captured graph and its key
     cudaGraphExec_t exec = nullptr;
@@ -669,7 +693,7 @@ static gbmp_status batch_launch(gbmp_batch_planner b, int n, int lpp, const Rrtc
                 set_error("planning kernel needs %zu bytes of shared memory: %s", smem, cudaGetErrorString(ce));
                 stt = ce == cudaErrorInvalidValue ? GBMP_ERR_CAPACITY : GBMP_ERR_CUDA;
             }
-            else kern<<<n * lpp, kRrtcThreads, smem, st>>>(b->d_table, n, lpp, prm);
+            else kern<<<n * lpp, kRrtcThreads, smem, st>>>(b->d_table, n, lpp, prm, (int *)(b->d_deadline + 1));
         });
     }
     if (stt) return stt;
@@ -713,7 +737,7 @@ gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, i
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_roots, sizeof(float) * (size_t)max_problems * 2 * max_links);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_summary, sizeof(int) * 8 * max_problems);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_summary, sizeof(int) * 8 * max_problems);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_deadline, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_deadline, 2 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         set_error("batch planner allocation failed: %s", cudaGetErrorString(e));
         gbmp_batch_planner_destroy(b);
