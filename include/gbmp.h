@@ -242,6 +242,66 @@ GBMP_API gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner planner, int32_t n
                                            int32_t use_graph, gbmp_rrtc_result *results, float *h_paths,
                                            void *stream);
 
+/* ---- continuous-batching request server ----
+ * No counterpart in the reference (its callers run one request at a time).  Robots and
+ * environments are registered once and stay resident; FK+collision requests are
+ * batched as they arrive (grouped by robot and environment, one launch per group,
+ * batches overlapping on `num_streams` streams) and admitted while the in-flight
+ * device bytes stay within hbm_budget_bytes; plan requests are solved in batched,
+ * graph-captured launches by `plan_workers` threads with device-resident trees.
+ * Host buffers passed to submit must stay valid until gbmp_server_wait returns. */
+typedef struct gbmp_server_s *gbmp_server;
+
+typedef struct gbmp_server_config {
+    int32_t num_streams;          /* concurrent check batches                       */
+    int64_t hbm_budget_bytes;     /* device bytes of in-flight check batches        */
+    int64_t max_batch_states;     /* states per check batch                         */
+    int32_t plan_workers;         /* threads solving plan batches (0: no planning)  */
+    int32_t plan_batch;           /* problems per plan batch                        */
+    int32_t plan_lanes;           /* lanes per problem                              */
+    int32_t planner_max_nodes;    /* nodes per tree per problem                     */
+    int32_t plan_path_cap;        /* path buffer per problem (states)               */
+    int32_t plan_max_iters;
+    float plan_range;
+    float plan_resolution;
+    int32_t step_rule;
+    double plan_time_limit_s;
+} gbmp_server_config;
+
+typedef struct gbmp_request_info {
+    gbmp_status status;
+    int32_t solved;
+    int32_t path_len;
+    float cost;
+    double latency_ms;            /* submit to completion                            */
+    double queue_ms;              /* submit to dispatch                              */
+} gbmp_request_info;
+
+typedef struct gbmp_server_metrics {
+    int64_t completed, batches, plan_batches, states_checked, budget_in_use;
+    double check_p50_ms, check_p95_ms, check_p99_ms;
+    double plan_p50_ms, plan_p95_ms, plan_p99_ms;
+    double elapsed_s;
+} gbmp_server_metrics;
+
+GBMP_API gbmp_status gbmp_server_create(const gbmp_server_config *config, gbmp_server *out);
+GBMP_API gbmp_status gbmp_server_add_robot(gbmp_server server, gbmp_robot robot, int32_t *robot_id);
+GBMP_API gbmp_status gbmp_server_add_env(gbmp_server server, gbmp_env env, int32_t *env_id);
+GBMP_API gbmp_status gbmp_server_start(gbmp_server server);
+/* h_q [n * L] (L of the robot); h_verdict [n] receives 1 for colliding states. */
+GBMP_API gbmp_status gbmp_server_submit_check(gbmp_server server, int32_t robot_id, int32_t env_id, const float *h_q,
+                                              int64_t n, uint8_t *h_verdict, int64_t *ticket);
+/* h_path [path_cap * L] receives the path (start first) when solved. */
+GBMP_API gbmp_status gbmp_server_submit_plan(gbmp_server server, int32_t robot_id, int32_t env_id,
+                                             const float *h_start, const float *h_goal, uint64_t seed, float *h_path,
+                                             int32_t path_cap, int64_t *ticket);
+/* Blocks until the request finishes (or timeout_s passes: GBMP_ERR_TIMEOUT, the ticket
+ * stays valid); info->status is the request's own status. */
+GBMP_API gbmp_status gbmp_server_wait(gbmp_server server, int64_t ticket, double timeout_s, gbmp_request_info *info);
+GBMP_API gbmp_status gbmp_server_stats(gbmp_server server, gbmp_server_metrics *out);
+/* Stops the worker threads after the batches in flight finish. */
+GBMP_API gbmp_status gbmp_server_destroy(gbmp_server server);
+
 /* ---- instrumentation ----
  * With profiling enabled, CUDA events are recorded on the launching stream around
  * every launch of the named kernel families; gbmp_profile_read() waits for them and

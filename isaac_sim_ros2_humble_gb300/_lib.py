@@ -52,6 +52,26 @@ class RrtcProblem(C.Structure):
                 ("seed", C.c_uint64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("num_streams", C.c_int32), ("hbm_budget_bytes", C.c_int64), ("max_batch_states", C.c_int64),
+                ("plan_workers", C.c_int32), ("plan_batch", C.c_int32), ("plan_lanes", C.c_int32),
+                ("planner_max_nodes", C.c_int32), ("plan_path_cap", C.c_int32), ("plan_max_iters", C.c_int32),
+                ("plan_range", C.c_float), ("plan_resolution", C.c_float), ("step_rule", C.c_int32),
+                ("plan_time_limit_s", C.c_double)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("solved", C.c_int32), ("path_len", C.c_int32), ("cost", C.c_float),
+                ("latency_ms", C.c_double), ("queue_ms", C.c_double)]
+
+
+class ServerMetrics(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("plan_batches", C.c_int64),
+                ("states_checked", C.c_int64), ("budget_in_use", C.c_int64), ("check_p50_ms", C.c_double),
+                ("check_p95_ms", C.c_double), ("check_p99_ms", C.c_double), ("plan_p50_ms", C.c_double),
+                ("plan_p95_ms", C.c_double), ("plan_p99_ms", C.c_double), ("elapsed_s", C.c_double)]
+
+
 class Limits(C.Structure):
     _fields_ = [("max_links", C.c_int32), ("max_spheres", C.c_int32), ("max_self_pairs", C.c_int32),
                 ("max_env_words", C.c_int32)]
@@ -86,6 +106,15 @@ SIGNATURES = {
     "gbmp_batch_planner_destroy": [_vp],
     "gbmp_rrtc_solve_batch": [_vp, _i32, C.POINTER(RrtcProblem), C.POINTER(RrtcSettings), _i32, _i32,
                               C.POINTER(RrtcResult), _vp, _vp],
+    "gbmp_server_create": [C.POINTER(ServerConfig), C.POINTER(_vp)],
+    "gbmp_server_add_robot": [_vp, _vp, _i32p],
+    "gbmp_server_add_env": [_vp, _vp, _i32p],
+    "gbmp_server_start": [_vp],
+    "gbmp_server_submit_check": [_vp, _i32, _i32, _vp, _i64, _vp, C.POINTER(C.c_int64)],
+    "gbmp_server_submit_plan": [_vp, _i32, _i32, _vp, _vp, _u64, _vp, _i32, C.POINTER(C.c_int64)],
+    "gbmp_server_wait": [_vp, _i64, C.c_double, C.POINTER(RequestInfo)],
+    "gbmp_server_stats": [_vp, C.POINTER(ServerMetrics)],
+    "gbmp_server_destroy": [_vp],
     "gbmp_profile_enable": [_i32],
     "gbmp_profile_reset": [],
     "gbmp_profile_read": [_i32, C.POINTER(C.c_double), C.POINTER(C.c_int64)],

@@ -232,3 +232,79 @@ class BatchPlanner:
             p = flat[i, : r["path_len"] * L].reshape(-1, L).copy() if r["solved"] else np.zeros((0, L), np.float32)
             out.append((r, p))
         return out
+
+
+class Server:
+    """Continuous-batching request server (gbmp_server_*): resident robots and scenes,
+    FK+collision requests batched as they arrive, plan requests solved in batched
+    launches.  Host arrays passed to submit_* are kept alive until wait() returns."""
+
+    def __init__(self, num_streams: int = 4, hbm_budget_bytes: int = 1 << 30, max_batch_states: int = 1 << 20,
+                 plan_workers: int = 1, plan_batch: int = 64, plan_lanes: int = 8, planner_max_nodes: int = 32768,
+                 plan_path_cap: int = 4096, plan_max_iters: int = 100000, plan_range: float = 0.1,
+                 plan_resolution: float = 0.01, step_rule: int = _lib.STEP_LINF, plan_time_limit_s: float = 10.0):
+        cfg = _lib.ServerConfig(num_streams, hbm_budget_bytes, max_batch_states, plan_workers, plan_batch, plan_lanes,
+                                planner_max_nodes, plan_path_cap, plan_max_iters, plan_range, plan_resolution,
+                                step_rule, plan_time_limit_s)
+        h = C.c_void_p()
+        check(_lib.load().gbmp_server_create(C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self.robots, self.envs = [], []
+        self._live = {}
+
+    def add_robot(self, robot: Robot) -> int:
+        i = C.c_int32()
+        check(_lib.load().gbmp_server_add_robot(self.handle, robot.handle, C.byref(i)))
+        self.robots.append(robot)
+        return i.value
+
+    def add_env(self, env: Env) -> int:
+        i = C.c_int32()
+        check(_lib.load().gbmp_server_add_env(self.handle, env.handle, C.byref(i)))
+        self.envs.append(env)
+        return i.value
+
+    def start(self):
+        check(_lib.load().gbmp_server_start(self.handle))
+
+    def submit_check(self, robot_id: int, env_id: int, q: np.ndarray, verdict: np.ndarray) -> int:
+        q = np.ascontiguousarray(q, np.float32)
+        assert verdict.dtype == np.uint8 and verdict.flags.c_contiguous and verdict.size >= q.shape[0]
+        t = C.c_int64()
+        check(_lib.load().gbmp_server_submit_check(self.handle, robot_id, env_id, q.ctypes.data, q.shape[0],
+                                                   verdict.ctypes.data, C.byref(t)))
+        self._live[t.value] = (q, verdict)
+        return t.value
+
+    def submit_plan(self, robot_id: int, env_id: int, start, goal, seed: int, path: np.ndarray) -> int:
+        s0, g0 = _c(start, np.float32).reshape(-1), _c(goal, np.float32).reshape(-1)
+        t = C.c_int64()
+        check(_lib.load().gbmp_server_submit_plan(self.handle, robot_id, env_id, s0.ctypes.data, g0.ctypes.data,
+                                                  int(seed), path.ctypes.data, path.shape[0], C.byref(t)))
+        self._live[t.value] = (s0, g0, path)
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 60.0):
+        info = _lib.RequestInfo()
+        st = _lib.load().gbmp_server_wait(self.handle, ticket, float(timeout_s), C.byref(info))
+        if st == 6:
+            return None
+        check(st)
+        self._live.pop(ticket, None)
+        return {f: getattr(info, f) for f, _ in _lib.RequestInfo._fields_}
+
+    def stats(self):
+        m = _lib.ServerMetrics()
+        check(_lib.load().gbmp_server_stats(self.handle, C.byref(m)))
+        return {f: getattr(m, f) for f, _ in _lib.ServerMetrics._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().gbmp_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,511 @@
+// gbmp_server.cu -- continuous-batching request server over resident robots,
+// environments and planner trees.  The reference has no serving layer; callers of
+// the reference run checkStates / solve one request at a time on the default stream
+// (cudampl/CUDAMPLib/src/spaces/SingleArmSpace.cu:1572-1602,
+// cudampl/CPRRTC/src/RobotSolver.cu:348-473).
+//
+// Design
+//  * Robots and environments are registered once and stay resident.
+//  * FK+collision requests go to the check queue.  A scheduler thread repeatedly
+//    takes every pending check request that fits the HBM budget and the batch cap,
+//    groups them by (robot, environment), packs their joint states into one pinned
+//    staging buffer, and issues per group one H2D copy, one gbmp_check_states launch
+//    and one D2H copy on the next of `num_streams` streams.  Batches on different
+//    streams overlap on the device; a completion thread waits for each batch's event,
+//    scatters verdicts to the requests and returns the budget, so requests that arrive
+//    while others run are admitted as soon as memory frees up.
+//  * Plan requests go to the plan queue; `plan_workers` threads each own a batch
+//    planner (device-resident trees) and solve everything pending in one batched,
+//    graph-captured launch, so plan batches overlap with check batches and with each
+//    other.
+//  * Every request records submit, start and finish times; the server keeps latency
+//    percentiles.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <thread>
+
+#include "gbmp_internal.h"
+
+using gbmp::align16;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    int64_t id = 0;
+    int kind = 0;                     // 0 check, 1 plan
+    int robot = 0, env = 0;
+    const float *q = nullptr;         // check: host [n * L]
+    int64_t n = 0;
+    uint8_t *verdict = nullptr;       // check: host [n]
+    const float *start = nullptr, *goal = nullptr;
+    uint64_t seed = 0;
+    float *path = nullptr;
+    int32_t path_cap = 0;
+    size_t bytes = 0;                 // device bytes reserved while in flight
+    Clock::time_point t_submit, t_start, t_done;
+    gbmp_status status = GBMP_OK;
+    int32_t solved = 0, path_len = 0;
+    float cost = 0.f;
+    bool done = false;
+};
+
+struct Batch {
+    std::vector<std::shared_ptr<Request>> reqs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    float *d_q = nullptr;
+    uint8_t *d_v = nullptr;
+    float *h_q = nullptr;
+    uint8_t *h_v = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gbmp_server_s {
+    gbmp_server_config cfg{};
+    std::vector<gbmp_robot> robots;
+    std::vector<gbmp_env> envs;
+    std::vector<cudaStream_t> streams;
+    int next_stream = 0;
+    int device = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done, cv_plan, cv_complete;
+    std::deque<std::shared_ptr<Request>> check_q, plan_q;
+    std::deque<Batch> in_flight;
+    std::map<int64_t, std::shared_ptr<Request>> tickets;
+    int64_t next_id = 1;
+    size_t budget_used = 0;
+    bool stop = false;
+    gbmp_status fatal = GBMP_OK;
+
+    std::vector<double> lat_check, lat_plan;    // ms
+    int64_t completed = 0, batches = 0, plan_batches = 0, states_checked = 0;
+    Clock::time_point t0 = Clock::now();
+
+    std::thread sched, completer;
+    std::vector<std::thread> planners;
+};
+
+namespace {
+
+void finish_request(gbmp_server_s *s, const std::shared_ptr<Request> &r) {
+    r->t_done = Clock::now();
+    r->done = true;
+    const double ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    (r->kind == 0 ? s->lat_check : s->lat_plan).push_back(ms);
+    ++s->completed;
+}
+
+// Scheduler: forms check batches from everything pending that fits the budget.
+void scheduler_loop(gbmp_server_s *s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        s->cv_sched.wait(lk, [&] { return s->stop || (!s->check_q.empty() && s->fatal == GBMP_OK); });
+        if (s->stop) return;
+        // admit requests in arrival order while they fit the budget and the batch cap
+        std::vector<std::shared_ptr<Request>> take;
+        size_t bytes = 0;
+        int64_t states = 0;
+        while (!s->check_q.empty()) {
+            auto &r = s->check_q.front();
+            const bool first = take.empty();
+            if (!first && states + r->n > s->cfg.max_batch_states) break;
+            if (s->budget_used + bytes + r->bytes > (size_t)s->cfg.hbm_budget_bytes) {
+                if (first && s->in_flight.empty()) {
+                    // a single request larger than the whole budget can never be admitted
+                    r->status = GBMP_ERR_CAPACITY;
+                    finish_request(s, r);
+                    s->check_q.pop_front();
+                    s->cv_complete.notify_all();
+                    continue;
+                }
+                break;
+            }
+            bytes += r->bytes;
+            states += r->n;
+            take.push_back(r);
+            s->check_q.pop_front();
+        }
+        if (take.empty()) {
+            // wait for memory to free up
+            s->cv_sched.wait(lk, [&] { return s->stop || s->in_flight.empty() || s->budget_used == 0; });
+            continue;
+        }
+        s->budget_used += bytes;
+        const int si = s->next_stream;
+        s->next_stream = (s->next_stream + 1) % (int)s->streams.size();
+        lk.unlock();
+
+        Batch b;
+        b.reqs = take;
+        b.stream = s->streams[si];
+        b.bytes = bytes;
+        gbmp_status st = GBMP_OK;
+        const auto now = Clock::now();
+        for (auto &r : take) r->t_start = now;
+        // group by (robot, env): consecutive runs in a sorted order
+        std::stable_sort(b.reqs.begin(), b.reqs.end(), [](const std::shared_ptr<Request> &a,
+                                                          const std::shared_ptr<Request> &c) {
+            return a->robot != c->robot ? a->robot < c->robot : a->env < c->env;
+        });
+        // packing: the states of all requests back to back (floats), verdicts back to back
+        // (bytes); requests of one (robot, env) group are adjacent, so a group is one launch
+        size_t qfloats = 0, vbytes = 0;
+        for (auto &r : b.reqs) {
+            qfloats += (size_t)r->n * s->robots[r->robot]->L;
+            vbytes += (size_t)r->n;
+        }
+        const size_t qbytes = align16(sizeof(float) * qfloats);
+        cudaError_t ce = cudaMalloc(&b.d_q, qbytes + align16(vbytes));
+        if (ce == cudaSuccess) ce = cudaMallocHost(&b.h_q, qbytes + align16(vbytes));
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
+        if (ce != cudaSuccess) st = ce == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+        if (st == GBMP_OK) {
+            b.d_v = reinterpret_cast<uint8_t *>(b.d_q) + qbytes;
+            b.h_v = reinterpret_cast<uint8_t *>(b.h_q) + qbytes;
+            size_t off = 0;
+            for (auto &r : b.reqs) {
+                const size_t nf = (size_t)r->n * s->robots[r->robot]->L;
+                memcpy(b.h_q + off, r->q, sizeof(float) * nf);
+                off += nf;
+            }
+            ce = cudaMemcpyAsync(b.d_q, b.h_q, sizeof(float) * qfloats, cudaMemcpyHostToDevice, b.stream);
+            if (ce != cudaSuccess) st = GBMP_ERR_CUDA;
+            size_t qoff = 0, voff = 0;
+            for (size_t i = 0; i < b.reqs.size() && st == GBMP_OK;) {
+                const size_t q0 = qoff, v0 = voff;
+                int64_t n = 0;
+                size_t j = i;
+                while (j < b.reqs.size() && b.reqs[j]->robot == b.reqs[i]->robot && b.reqs[j]->env == b.reqs[i]->env) {
+                    n += b.reqs[j]->n;
+                    qoff += (size_t)b.reqs[j]->n * s->robots[b.reqs[j]->robot]->L;
+                    voff += (size_t)b.reqs[j]->n;
+                    ++j;
+                }
+                st = gbmp_check_states(s->robots[b.reqs[i]->robot], s->envs[b.reqs[i]->env], b.d_q + q0, n,
+                                       GBMP_CHECK_VERDICT, b.d_v + v0, nullptr, nullptr, b.stream);
+                i = j;
+            }
+            if (st == GBMP_OK) {
+                ce = cudaMemcpyAsync(b.h_v, b.d_v, vbytes, cudaMemcpyDeviceToHost, b.stream);
+                if (ce == cudaSuccess) ce = cudaEventRecord(b.done, b.stream);
+                if (ce != cudaSuccess) st = GBMP_ERR_CUDA;
+            }
+        }
+        lk.lock();
+        if (st != GBMP_OK) {
+            for (auto &r : b.reqs) {
+                r->status = st;
+                finish_request(s, r);
+            }
+            s->budget_used -= bytes;
+            if (b.d_q) cudaFree(b.d_q);
+            if (b.h_q) cudaFreeHost(b.h_q);
+            if (b.done) cudaEventDestroy(b.done);
+            s->cv_complete.notify_all();
+            continue;
+        }
+        s->states_checked += states;
+        ++s->batches;
+        s->in_flight.push_back(b);
+        s->cv_done.notify_one();
+    }
+}
+
+// Completion: waits for batches in issue order, scatters verdicts, frees the budget.
+void completion_loop(gbmp_server_s *s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        s->cv_done.wait(lk, [&] { return s->stop || !s->in_flight.empty(); });
+        if (s->in_flight.empty() && s->stop) return;
+        Batch b = s->in_flight.front();
+        lk.unlock();
+        cudaError_t ce = cudaEventSynchronize(b.done);
+        size_t voff = 0;
+        for (auto &r : b.reqs) {
+            if (ce == cudaSuccess) memcpy(r->verdict, b.h_v + voff, (size_t)r->n);
+            voff += (size_t)r->n;
+        }
+        cudaFree(b.d_q);
+        cudaFreeHost(b.h_q);
+        cudaEventDestroy(b.done);
+        lk.lock();
+        s->in_flight.pop_front();
+        for (auto &r : b.reqs) {
+            r->status = ce == cudaSuccess ? GBMP_OK : GBMP_ERR_CUDA;
+            finish_request(s, r);
+        }
+        s->budget_used -= b.bytes;
+        s->cv_sched.notify_all();
+        s->cv_complete.notify_all();
+    }
+}
+
+// Plan worker: solves every pending plan request in one batched launch.
+void plan_loop(gbmp_server_s *s, int worker) {
+    cudaSetDevice(s->device);
+    gbmp_batch_planner bp = nullptr;
+    cudaStream_t st = nullptr;
+    int max_links = 1;
+    for (auto r : s->robots) max_links = std::max(max_links, r->L);
+    gbmp_status cs = gbmp_batch_planner_create(s->cfg.plan_batch, s->cfg.planner_max_nodes, max_links,
+                                               s->cfg.plan_path_cap, &bp);
+    if (cs == GBMP_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) cs = GBMP_ERR_CUDA;
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (cs != GBMP_OK) s->fatal = cs;
+    (void)worker;
+    while (true) {
+        s->cv_plan.wait(lk, [&] { return s->stop || !s->plan_q.empty(); });
+        if (s->stop) break;
+        std::vector<std::shared_ptr<Request>> take;
+        while (!s->plan_q.empty() && (int)take.size() < s->cfg.plan_batch) {
+            take.push_back(s->plan_q.front());
+            s->plan_q.pop_front();
+        }
+        ++s->plan_batches;
+        lk.unlock();
+        const auto now = Clock::now();
+        std::vector<gbmp_rrtc_problem> probs(take.size());
+        for (size_t i = 0; i < take.size(); ++i) {
+            take[i]->t_start = now;
+            probs[i] = {s->robots[take[i]->robot], s->envs[take[i]->env], take[i]->start, take[i]->goal, take[i]->seed};
+        }
+        gbmp_rrtc_settings set{};
+        set.lanes = s->cfg.plan_lanes;
+        set.max_iters = s->cfg.plan_max_iters;
+        set.range = s->cfg.plan_range;
+        set.resolution = s->cfg.plan_resolution;
+        set.step_rule = s->cfg.step_rule;
+        set.time_limit_s = s->cfg.plan_time_limit_s;
+        std::vector<gbmp_rrtc_result> res(take.size());
+        std::vector<float> paths((size_t)take.size() * s->cfg.plan_path_cap * max_links);
+        gbmp_status ps = cs != GBMP_OK ? cs
+                                       : gbmp_rrtc_solve_batch(bp, (int)take.size(), probs.data(), &set,
+                                                               s->cfg.plan_lanes, 1, res.data(), paths.data(), st);
+        for (size_t i = 0; i < take.size(); ++i) {
+            auto &r = take[i];
+            r->status = ps;
+            if (ps == GBMP_OK) {
+                r->solved = res[i].solved;
+                r->cost = res[i].cost;
+                const int L = s->robots[r->robot]->L;
+                const int len = res[i].solved ? res[i].path_len : 0;
+                r->path_len = len;
+                if (len > r->path_cap) {
+                    r->status = GBMP_ERR_CAPACITY;
+                } else if (len > 0 && r->path) {
+                    memcpy(r->path, paths.data() + i * (size_t)s->cfg.plan_path_cap * max_links, sizeof(float) * len * L);
+                }
+                if (!r->solved && r->status == GBMP_OK) r->status = GBMP_ERR_NOT_SOLVED;
+            }
+        }
+        lk.lock();
+        for (auto &r : take) finish_request(s, r);
+        s->cv_complete.notify_all();
+    }
+    lk.unlock();
+    if (bp) gbmp_batch_planner_destroy(bp);
+    if (st) cudaStreamDestroy(st);
+}
+
+double pct(std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double idx = p / 100.0 * (v.size() - 1);
+    const size_t lo = (size_t)idx, hi = std::min(lo + 1, v.size() - 1);
+    return v[lo] + (idx - lo) * (v[hi] - v[lo]);
+}
+
+}  // namespace
+
+using namespace gbmp;
+
+extern "C" {
+
+gbmp_status gbmp_server_create(const gbmp_server_config *cfg, gbmp_server *out) {
+    GBMP_CHECK_ARG(cfg && out, "NULL argument");
+    *out = nullptr;
+    GBMP_CHECK_ARG(cfg->num_streams >= 1 && cfg->num_streams <= 64, "num_streams outside [1, 64]");
+    GBMP_CHECK_ARG(cfg->hbm_budget_bytes > 0, "hbm_budget_bytes <= 0");
+    GBMP_CHECK_ARG(cfg->max_batch_states >= 1, "max_batch_states < 1");
+    GBMP_CHECK_ARG(cfg->plan_workers >= 0 && cfg->plan_workers <= 16, "plan_workers outside [0, 16]");
+    GBMP_CHECK_ARG(cfg->plan_workers == 0 || (cfg->plan_batch >= 1 && cfg->planner_max_nodes >= 2 &&
+                                              cfg->plan_lanes >= 1 && cfg->plan_path_cap >= 2 &&
+                                              cfg->plan_range > 0.f && cfg->plan_max_iters >= 1),
+                   "bad planner configuration");
+    auto *s = new gbmp_server_s();
+    s->cfg = *cfg;
+    cudaGetDevice(&s->device);
+    for (int i = 0; i < cfg->num_streams; ++i) {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            set_error("stream creation failed");
+            gbmp_server_destroy(s);
+            return GBMP_ERR_CUDA;
+        }
+        s->streams.push_back(st);
+    }
+    *out = s;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_add_robot(gbmp_server s, gbmp_robot r, int32_t *id) {
+    GBMP_CHECK_ARG(s && r && id, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    GBMP_CHECK_ARG(!s->sched.joinable(), "resources must be registered before gbmp_server_start");
+    s->robots.push_back(r);
+    *id = (int32_t)s->robots.size() - 1;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_add_env(gbmp_server s, gbmp_env e, int32_t *id) {
+    GBMP_CHECK_ARG(s && e && id, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    GBMP_CHECK_ARG(!s->sched.joinable(), "resources must be registered before gbmp_server_start");
+    s->envs.push_back(e);
+    *id = (int32_t)s->envs.size() - 1;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_start(gbmp_server s) {
+    GBMP_CHECK_ARG(s, "server is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    GBMP_CHECK_ARG(!s->sched.joinable(), "server already started");
+    GBMP_CHECK_ARG(!s->robots.empty() && !s->envs.empty(), "register robots and environments first");
+    s->t0 = Clock::now();
+    s->sched = std::thread(scheduler_loop, s);
+    s->completer = std::thread(completion_loop, s);
+    for (int i = 0; i < s->cfg.plan_workers; ++i) s->planners.emplace_back(plan_loop, s, i);
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_submit_check(gbmp_server s, int32_t robot, int32_t env, const float *h_q, int64_t n,
+                                     uint8_t *h_verdict, int64_t *ticket) {
+    GBMP_CHECK_ARG(s && h_q && h_verdict && ticket, "NULL argument");
+    GBMP_CHECK_ARG(n >= 1, "n < 1");
+    std::lock_guard<std::mutex> lk(s->mu);
+    GBMP_CHECK_ARG(robot >= 0 && robot < (int)s->robots.size(), "unknown robot %d", robot);
+    GBMP_CHECK_ARG(env >= 0 && env < (int)s->envs.size(), "unknown environment %d", env);
+    GBMP_CHECK_ARG(s->sched.joinable() && !s->stop, "server not running");
+    auto r = std::make_shared<Request>();
+    r->id = s->next_id++;
+    r->kind = 0;
+    r->robot = robot;
+    r->env = env;
+    r->q = h_q;
+    r->n = n;
+    r->verdict = h_verdict;
+    r->bytes = align16(sizeof(float) * n * s->robots[robot]->L) + align16((size_t)n);
+    r->t_submit = Clock::now();
+    s->tickets[r->id] = r;
+    s->check_q.push_back(r);
+    *ticket = r->id;
+    s->cv_sched.notify_one();
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_submit_plan(gbmp_server s, int32_t robot, int32_t env, const float *h_start,
+                                    const float *h_goal, uint64_t seed, float *h_path, int32_t path_cap,
+                                    int64_t *ticket) {
+    GBMP_CHECK_ARG(s && h_start && h_goal && ticket, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    GBMP_CHECK_ARG(s->cfg.plan_workers > 0, "server has no plan workers");
+    GBMP_CHECK_ARG(robot >= 0 && robot < (int)s->robots.size(), "unknown robot %d", robot);
+    GBMP_CHECK_ARG(env >= 0 && env < (int)s->envs.size(), "unknown environment %d", env);
+    GBMP_CHECK_ARG(s->sched.joinable() && !s->stop, "server not running");
+    auto r = std::make_shared<Request>();
+    r->id = s->next_id++;
+    r->kind = 1;
+    r->robot = robot;
+    r->env = env;
+    r->start = h_start;
+    r->goal = h_goal;
+    r->seed = seed;
+    r->path = h_path;
+    r->path_cap = path_cap;
+    r->t_submit = Clock::now();
+    s->tickets[r->id] = r;
+    s->plan_q.push_back(r);
+    *ticket = r->id;
+    s->cv_plan.notify_one();
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_wait(gbmp_server s, int64_t ticket, double timeout_s, gbmp_request_info *info) {
+    GBMP_CHECK_ARG(s, "server is NULL");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    GBMP_CHECK_ARG(it != s->tickets.end(), "unknown ticket %lld", (long long)ticket);
+    auto r = it->second;
+    const auto deadline = Clock::now() + std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 1e9);
+    if (!s->cv_complete.wait_until(lk, deadline, [&] { return r->done; })) {
+        set_error("request %lld not finished within %.3f s", (long long)ticket, timeout_s);
+        return GBMP_ERR_TIMEOUT;
+    }
+    if (info) {
+        info->status = r->status;
+        info->solved = r->solved;
+        info->path_len = r->path_len;
+        info->cost = r->cost;
+        info->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+        info->queue_ms = std::chrono::duration<double, std::milli>(r->t_start - r->t_submit).count();
+    }
+    s->tickets.erase(it);
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_stats(gbmp_server s, gbmp_server_metrics *out) {
+    GBMP_CHECK_ARG(s && out, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    memset(out, 0, sizeof *out);
+    out->completed = s->completed;
+    out->batches = s->batches;
+    out->plan_batches = s->plan_batches;
+    out->states_checked = s->states_checked;
+    out->check_p50_ms = pct(s->lat_check, 50);
+    out->check_p95_ms = pct(s->lat_check, 95);
+    out->check_p99_ms = pct(s->lat_check, 99);
+    out->plan_p50_ms = pct(s->lat_plan, 50);
+    out->plan_p95_ms = pct(s->lat_plan, 95);
+    out->plan_p99_ms = pct(s->lat_plan, 99);
+    out->elapsed_s = std::chrono::duration<double>(Clock::now() - s->t0).count();
+    out->budget_in_use = (int64_t)s->budget_used;
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_server_destroy(gbmp_server s) {
+    if (!s) return GBMP_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_sched.notify_all();
+    s->cv_done.notify_all();
+    s->cv_plan.notify_all();
+    if (s->sched.joinable()) s->sched.join();
+    if (s->completer.joinable()) s->completer.join();
+    for (auto &t : s->planners) t.join();
+    for (auto &b : s->in_flight) {
+        cudaEventSynchronize(b.done);
+        cudaFree(b.d_q);
+        cudaFreeHost(b.h_q);
+        cudaEventDestroy(b.done);
+    }
+    for (auto st : s->streams) cudaStreamDestroy(st);
+    delete s;
+    return GBMP_OK;
+}
+
+}  // extern "C"
