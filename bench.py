@@ -51,11 +51,13 @@ def parse():
     ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
     ap.add_argument("--edges", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="edges", choices=["edges", "plan", "batch"],
+    ap.add_argument("--workload", default="edges", choices=["edges", "plan", "batch", "serve"],
                     help="edges: the headline edge-validation batch; plan: single-problem RRT-Connect "
                          "time-to-solution over seeded shelf problems")
     ap.add_argument("--plan-seeds", type=int, default=100)
     ap.add_argument("--lanes", default="1024,2048,4096,8192")
+    ap.add_argument("--rates", default="200,1000,2000", help="serve: Poisson arrival rates (req/s)")
+    ap.add_argument("--duration", type=float, default=3.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
 
 
@@ -348,8 +350,133 @@ def run_batch(args):
     return 0
 
 
+def run_serve(args):
+    """Serving: Poisson request stream over 4 resident robots (6-9 DOF) and 16 resident
+    scenes (50-500 obstacles); 70 % FK+collision requests of log-uniform 1-65,536 states,
+    30 % RRT-Connect plan requests.  The continuous-batching server against the plain
+    per-request path (one request at a time, in arrival order)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import threading
+    import torch
+    from isaac_sim_ros2_humble_gb300 import _lib, api, workloads as W
+    torch.cuda.set_device(0)
+    robots = [W.serial_arm(80 + i, dof=6 + i, n_spheres=40 + 25 * i, prismatic_torso=i >= 2, resolution=0.01)
+              for i in range(4)]
+    envs = [W.random_env(90 + k, *(lambda O: (O - round(O * 80 / 336), round(O * 64 / 336), round(O * 16 / 336)))
+                         (50 + 30 * k), oriented=True) for k in range(16)]
+    R = [api.Robot(r) for r in robots]
+    E = [api.Env(e) for e in envs]
+    rng = np.random.default_rng(5)
+    pools = [r.sample_full(rng, 65536) for r in robots]
+    free = {}
+    for i in range(4):
+        for k in range(16):
+            v = torch.zeros(4096, dtype=torch.uint8, device="cuda")
+            api.check_states(R[i], E[k], torch.from_numpy(pools[i][:4096]).cuda(), verdict=v)
+            f = pools[i][:4096][v.cpu().numpy() == 0]
+            free[(i, k)] = f if len(f) >= 2 else None
+
+    def make_stream(rate, seed):
+        g = np.random.default_rng(seed)
+        t, out = 0.0, []
+        while t < args.duration:
+            t += g.exponential(1.0 / rate)
+            i, k = int(g.integers(4)), int(g.integers(16))
+            if g.random() < 0.7 or free[(i, k)] is None:
+                n = int(min(65536, np.exp(g.uniform(0, np.log(65536)))))
+                off = int(g.integers(0, 65536 - n + 1))
+                out.append((t, "check", i, k, (off, n)))
+            else:
+                f = free[(i, k)]
+                a, b = g.choice(len(f), 2, replace=False)
+                out.append((t, "plan", i, k, (f[a], f[b], int(g.integers(1 << 30)))))
+        return out
+
+    def run_served(stream):
+        srv = api.Server(num_streams=4, hbm_budget_bytes=8 << 30, max_batch_states=1 << 21, plan_workers=2,
+                         plan_batch=64, plan_lanes=16, planner_max_nodes=32768, plan_path_cap=4096,
+                         plan_range=PLAN_RANGE, plan_resolution=PLAN_RES, step_rule=RULE)
+        for r in R:
+            srv.add_robot(r)
+        for e in E:
+            srv.add_env(e)
+        srv.start()
+        tickets = []
+        t0 = time.perf_counter()
+        for (ta, kind, i, k, d) in stream:
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            if kind == "check":
+                off, n = d
+                out = np.zeros(n, np.uint8)
+                tickets.append(("check", srv.submit_check(i, k, pools[i][off:off + n], out)))
+            else:
+                path = np.zeros((4096, robots[i].num_links), np.float32)
+                tickets.append(("plan", srv.submit_plan(i, k, d[0], d[1], d[2], path)))
+        lat = {"check": [], "plan": []}
+        for kind, t in tickets:
+            info = srv.wait(t, 120.0)
+            lat[kind].append(info["latency_ms"])
+        el = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        return lat, el, st
+
+    def run_plain(stream):
+        planners = [api.Planner(r, max_nodes=32768, path_cap=4096) for r in R]
+        lat = {"check": [], "plan": []}
+        t0 = time.perf_counter()
+        for (ta, kind, i, k, d) in stream:
+            now = time.perf_counter() - t0
+            if now < ta:
+                time.sleep(ta - now)
+            if kind == "check":
+                off, n = d
+                q = torch.from_numpy(pools[i][off:off + n]).cuda(non_blocking=False)
+                v = torch.zeros(n, dtype=torch.uint8, device="cuda")
+                api.check_states(R[i], E[k], q, verdict=v)
+                v.cpu()
+            else:
+                planners[i].solve(E[k], d[0], d[1], lanes=1024, range_=PLAN_RANGE, resolution=PLAN_RES, rule=RULE,
+                                  seed=d[2])
+            lat[kind].append((time.perf_counter() - t0 - ta) * 1e3)
+        return lat, time.perf_counter() - t0
+
+    pct = lambda v, p: float(np.percentile(v, p)) if len(v) else None
+    per_rate = {}
+    for rate in [float(x) for x in args.rates.split(",")]:
+        stream = make_stream(rate, int(rate))
+        run_served(make_stream(rate, 1)[: 50])          # warm-up
+        lat_s, el_s, st = run_served(stream)
+        lat_p, el_p = run_plain(stream)
+        all_s = lat_s["check"] + lat_s["plan"]
+        all_p = lat_p["check"] + lat_p["plan"]
+        per_rate[str(int(rate))] = {
+            "requests": len(stream), "served_throughput_rps": len(stream) / el_s,
+            "plain_throughput_rps": len(stream) / el_p,
+            "served": {"p50_ms": pct(all_s, 50), "p95_ms": pct(all_s, 95), "p99_ms": pct(all_s, 99),
+                       "check_p99_ms": pct(lat_s["check"], 99), "plan_p99_ms": pct(lat_s["plan"], 99)},
+            "plain": {"p50_ms": pct(all_p, 50), "p95_ms": pct(all_p, 95), "p99_ms": pct(all_p, 99),
+                      "check_p99_ms": pct(lat_p["check"], 99), "plan_p99_ms": pct(lat_p["plan"], 99)},
+            "check_batches": st["batches"], "plan_batches": st["plan_batches"]}
+    top = per_rate[max(per_rate, key=lambda k: float(k))]
+    line = {"metric": "served p99 latency", "value": top["served"]["p99_ms"], "unit": "ms", "n_gpus": 1,
+            "steps": sum(v["requests"] for v in per_rate.values()), "warmup": 50,
+            "ms_per_step": top["served"]["p50_ms"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded Poisson stream)",
+            "config": {"workload": "serving_4robots_16scenes_70check_30plan", "duration_s": args.duration,
+                       "per_rate": per_rate}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "serve":
+        return run_serve(args)
     if args.workload == "plan":
         return run_plan(args)
     if args.workload == "batch":
