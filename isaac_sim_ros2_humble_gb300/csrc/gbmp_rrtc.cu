@@ -20,6 +20,7 @@
 // parent chains into the path buffer (pRRTC.cu:552-581).  Every loop is bounded: the
 // lane iteration cap, the node cap and a %globaltimer deadline end the launch with a
 // status the host reads.
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -666,9 +667,14 @@ struct gbmp_batch_planner_s {
     int *d_summary = nullptr, *h_summary = nullptr; // [max_problems * 8]
     unsigned long long *d_deadline = nullptr;   // [0] deadline, [1] round-robin counter
     std::vector<int> prev;                // 2 per problem
-    // captured graph and its key
-    cudaGraphExec_t exec = nullptr;
-    long long key[8] = {0};
+    // captured graphs by launch shape (a few shapes, least recently used evicted)
+    struct Captured {
+        long long key[8];
+        cudaGraphExec_t exec;
+        long long used;
+    };
+    std::vector<Captured> graphs;
+    long long use_clock = 0;
     std::mutex mu;
 };
 
@@ -757,7 +763,7 @@ gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, i
 
 gbmp_status gbmp_batch_planner_destroy(gbmp_batch_planner b) {
     if (!b) return GBMP_OK;
-    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
     if (b->pool) cudaFree(b->pool);
     if (b->d_table) cudaFree(b->d_table);
     if (b->h_table) cudaFreeHost(b->h_table);
@@ -843,8 +849,17 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
     if (use_graph) {
         const long long key[8] = {n, lanes_per_problem, (long long)smem, spl, cull, s->max_iters,
                                   (long long)(lim * 1e6), (long long)(prm.range * 1e6) ^ ((long long)(prm.res * 1e9) << 20)};
-        if (!b->exec || memcmp(key, b->key, sizeof key) != 0) {
-            if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+        cudaGraphExec_t exec = nullptr;
+        for (auto &g : b->graphs)
+            if (memcmp(key, g.key, sizeof key) == 0) { exec = g.exec; g.used = ++b->use_clock; }
+        if (!exec) {
+            if (b->graphs.size() >= 8) {
+                auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                            [](const gbmp_batch_planner_s::Captured &x,
+                                               const gbmp_batch_planner_s::Captured &y) { return x.used < y.used; });
+                cudaGraphExecDestroy(lru->exec);
+                b->graphs.erase(lru);
+            }
             cudaStream_t cap_st;
             GBMP_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
             GBMP_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
@@ -854,13 +869,17 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
             cudaStreamDestroy(cap_st);
             if (bs) { if (g) cudaGraphDestroy(g); return bs; }
             if (ce != cudaSuccess) { set_error("graph capture failed: %s", cudaGetErrorString(ce)); return GBMP_ERR_CUDA; }
-            ce = cudaGraphInstantiate(&b->exec, g, 0);
+            ce = cudaGraphInstantiate(&exec, g, 0);
             cudaGraphDestroy(g);
             if (ce != cudaSuccess) { set_error("graph instantiate failed: %s", cudaGetErrorString(ce)); return GBMP_ERR_CUDA; }
-            memcpy(b->key, key, sizeof key);
+            gbmp_batch_planner_s::Captured c;
+            memcpy(c.key, key, sizeof key);
+            c.exec = exec;
+            c.used = ++b->use_clock;
+            b->graphs.push_back(c);
         }
         count_launch(4);
-        GBMP_CUDA(cudaGraphLaunch(b->exec, st));
+        GBMP_CUDA(cudaGraphLaunch(exec, st));
     } else {
         gbmp_status bs = batch_launch(b, n, lanes_per_problem, prm, spl, cull, smem, lim, st);
         if (bs) return bs;

@@ -57,14 +57,20 @@ struct Request {
     bool done = false;
 };
 
-struct Batch {
-    std::vector<std::shared_ptr<Request>> reqs;
+// A batch slot: stream, completion event and staging buffers allocated once at start,
+// so that nothing in the request path allocates or frees device or pinned memory
+// (cudaFree and cudaFreeHost synchronise with the whole device and would serialise
+// the check batches behind running plan batches).
+struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    float *d_q = nullptr;
-    uint8_t *d_v = nullptr;
-    float *h_q = nullptr;
-    uint8_t *h_v = nullptr;
+    float *d_q = nullptr, *h_q = nullptr;   // [cap_states * max_L]
+    uint8_t *d_v = nullptr, *h_v = nullptr; // [cap_states]
+};
+
+struct Batch {
+    std::vector<std::shared_ptr<Request>> reqs;
+    int slot = -1;
     size_t bytes = 0;
 };
 
@@ -75,7 +81,10 @@ struct gbmp_server_s {
     std::vector<gbmp_robot> robots;
     std::vector<gbmp_env> envs;
     std::vector<cudaStream_t> streams;
-    int next_stream = 0;
+    std::vector<Slot> slots;
+    std::vector<int> free_slots;
+    int64_t cap_states = 0;                 // states per slot
+    int max_L = 0;
     int device = 0;
 
     std::mutex mu;
@@ -106,103 +115,82 @@ void finish_request(gbmp_server_s *s, const std::shared_ptr<Request> &r) {
     ++s->completed;
 }
 
-// Scheduler: forms check batches from everything pending that fits the budget.
+// Scheduler: forms check batches from everything pending that fits a free slot and
+// the budget, then stages, launches and hands the batch to the completion thread.
 void scheduler_loop(gbmp_server_s *s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     while (true) {
-        s->cv_sched.wait(lk, [&] { return s->stop || (!s->check_q.empty() && s->fatal == GBMP_OK); });
+        s->cv_sched.wait(lk, [&] {
+            return s->stop || (!s->check_q.empty() && !s->free_slots.empty() && s->fatal == GBMP_OK);
+        });
         if (s->stop) return;
-        // admit requests in arrival order while they fit the budget and the batch cap
         std::vector<std::shared_ptr<Request>> take;
         size_t bytes = 0;
         int64_t states = 0;
         while (!s->check_q.empty()) {
             auto &r = s->check_q.front();
-            const bool first = take.empty();
-            if (!first && states + r->n > s->cfg.max_batch_states) break;
-            if (s->budget_used + bytes + r->bytes > (size_t)s->cfg.hbm_budget_bytes) {
-                if (first && s->in_flight.empty()) {
-                    // a single request larger than the whole budget can never be admitted
-                    r->status = GBMP_ERR_CAPACITY;
-                    finish_request(s, r);
-                    s->check_q.pop_front();
-                    s->cv_complete.notify_all();
-                    continue;
-                }
-                break;
+            if (r->n > s->cap_states) {
+                // larger than a slot (the budget split over the streams): never admissible
+                r->status = GBMP_ERR_CAPACITY;
+                finish_request(s, r);
+                s->check_q.pop_front();
+                s->cv_complete.notify_all();
+                continue;
             }
+            if (states + r->n > s->cap_states) break;
+            if (s->budget_used + bytes + r->bytes > (size_t)s->cfg.hbm_budget_bytes) break;
             bytes += r->bytes;
             states += r->n;
             take.push_back(r);
             s->check_q.pop_front();
         }
-        if (take.empty()) {
-            // wait for memory to free up
-            s->cv_sched.wait(lk, [&] { return s->stop || s->in_flight.empty() || s->budget_used == 0; });
-            continue;
-        }
+        if (take.empty()) continue;
         s->budget_used += bytes;
-        const int si = s->next_stream;
-        s->next_stream = (s->next_stream + 1) % (int)s->streams.size();
+        const int si = s->free_slots.back();
+        s->free_slots.pop_back();
         lk.unlock();
 
+        Slot &sl = s->slots[si];
         Batch b;
         b.reqs = take;
-        b.stream = s->streams[si];
+        b.slot = si;
         b.bytes = bytes;
-        gbmp_status st = GBMP_OK;
         const auto now = Clock::now();
         for (auto &r : take) r->t_start = now;
-        // group by (robot, env): consecutive runs in a sorted order
+        // group by (robot, env): requests of a group become adjacent, one launch per group
         std::stable_sort(b.reqs.begin(), b.reqs.end(), [](const std::shared_ptr<Request> &a,
                                                           const std::shared_ptr<Request> &c) {
             return a->robot != c->robot ? a->robot < c->robot : a->env < c->env;
         });
-        // packing: the states of all requests back to back (floats), verdicts back to back
-        // (bytes); requests of one (robot, env) group are adjacent, so a group is one launch
         size_t qfloats = 0, vbytes = 0;
         for (auto &r : b.reqs) {
+            memcpy(sl.h_q + qfloats, r->q, sizeof(float) * (size_t)r->n * s->robots[r->robot]->L);
             qfloats += (size_t)r->n * s->robots[r->robot]->L;
             vbytes += (size_t)r->n;
         }
-        const size_t qbytes = align16(sizeof(float) * qfloats);
-        cudaError_t ce = cudaMalloc(&b.d_q, qbytes + align16(vbytes));
-        if (ce == cudaSuccess) ce = cudaMallocHost(&b.h_q, qbytes + align16(vbytes));
-        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
-        if (ce != cudaSuccess) st = ce == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
-        if (st == GBMP_OK) {
-            b.d_v = reinterpret_cast<uint8_t *>(b.d_q) + qbytes;
-            b.h_v = reinterpret_cast<uint8_t *>(b.h_q) + qbytes;
-            size_t off = 0;
-            for (auto &r : b.reqs) {
-                const size_t nf = (size_t)r->n * s->robots[r->robot]->L;
-                memcpy(b.h_q + off, r->q, sizeof(float) * nf);
-                off += nf;
+        gbmp_status st = GBMP_OK;
+        if (cudaMemcpyAsync(sl.d_q, sl.h_q, sizeof(float) * qfloats, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess)
+            st = GBMP_ERR_CUDA;
+        size_t qoff = 0, voff = 0;
+        for (size_t i = 0; i < b.reqs.size() && st == GBMP_OK;) {
+            const size_t q0 = qoff, v0 = voff;
+            int64_t n = 0;
+            size_t j = i;
+            while (j < b.reqs.size() && b.reqs[j]->robot == b.reqs[i]->robot && b.reqs[j]->env == b.reqs[i]->env) {
+                n += b.reqs[j]->n;
+                qoff += (size_t)b.reqs[j]->n * s->robots[b.reqs[j]->robot]->L;
+                voff += (size_t)b.reqs[j]->n;
+                ++j;
             }
-            ce = cudaMemcpyAsync(b.d_q, b.h_q, sizeof(float) * qfloats, cudaMemcpyHostToDevice, b.stream);
-            if (ce != cudaSuccess) st = GBMP_ERR_CUDA;
-            size_t qoff = 0, voff = 0;
-            for (size_t i = 0; i < b.reqs.size() && st == GBMP_OK;) {
-                const size_t q0 = qoff, v0 = voff;
-                int64_t n = 0;
-                size_t j = i;
-                while (j < b.reqs.size() && b.reqs[j]->robot == b.reqs[i]->robot && b.reqs[j]->env == b.reqs[i]->env) {
-                    n += b.reqs[j]->n;
-                    qoff += (size_t)b.reqs[j]->n * s->robots[b.reqs[j]->robot]->L;
-                    voff += (size_t)b.reqs[j]->n;
-                    ++j;
-                }
-                st = gbmp_check_states(s->robots[b.reqs[i]->robot], s->envs[b.reqs[i]->env], b.d_q + q0, n,
-                                       GBMP_CHECK_VERDICT, b.d_v + v0, nullptr, nullptr, b.stream);
-                i = j;
-            }
-            if (st == GBMP_OK) {
-                ce = cudaMemcpyAsync(b.h_v, b.d_v, vbytes, cudaMemcpyDeviceToHost, b.stream);
-                if (ce == cudaSuccess) ce = cudaEventRecord(b.done, b.stream);
-                if (ce != cudaSuccess) st = GBMP_ERR_CUDA;
-            }
+            st = gbmp_check_states(s->robots[b.reqs[i]->robot], s->envs[b.reqs[i]->env], sl.d_q + q0, n,
+                                   GBMP_CHECK_VERDICT, sl.d_v + v0, nullptr, nullptr, sl.stream);
+            i = j;
         }
+        if (st == GBMP_OK &&
+            (cudaMemcpyAsync(sl.h_v, sl.d_v, vbytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
+             cudaEventRecord(sl.done, sl.stream) != cudaSuccess))
+            st = GBMP_ERR_CUDA;
         lk.lock();
         if (st != GBMP_OK) {
             for (auto &r : b.reqs) {
@@ -210,9 +198,7 @@ void scheduler_loop(gbmp_server_s *s) {
                 finish_request(s, r);
             }
             s->budget_used -= bytes;
-            if (b.d_q) cudaFree(b.d_q);
-            if (b.h_q) cudaFreeHost(b.h_q);
-            if (b.done) cudaEventDestroy(b.done);
+            s->free_slots.push_back(si);
             s->cv_complete.notify_all();
             continue;
         }
@@ -223,7 +209,8 @@ void scheduler_loop(gbmp_server_s *s) {
     }
 }
 
-// Completion: waits for batches in issue order, scatters verdicts, frees the budget.
+// Completion: waits for batches in issue order, scatters verdicts, frees the slot
+// and the budget.
 void completion_loop(gbmp_server_s *s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
@@ -231,23 +218,22 @@ void completion_loop(gbmp_server_s *s) {
         s->cv_done.wait(lk, [&] { return s->stop || !s->in_flight.empty(); });
         if (s->in_flight.empty() && s->stop) return;
         Batch b = s->in_flight.front();
+        s->in_flight.pop_front();
         lk.unlock();
-        cudaError_t ce = cudaEventSynchronize(b.done);
+        Slot &sl = s->slots[b.slot];
+        const cudaError_t ce = cudaEventSynchronize(sl.done);
         size_t voff = 0;
         for (auto &r : b.reqs) {
-            if (ce == cudaSuccess) memcpy(r->verdict, b.h_v + voff, (size_t)r->n);
+            if (ce == cudaSuccess) memcpy(r->verdict, sl.h_v + voff, (size_t)r->n);
             voff += (size_t)r->n;
         }
-        cudaFree(b.d_q);
-        cudaFreeHost(b.h_q);
-        cudaEventDestroy(b.done);
         lk.lock();
-        s->in_flight.pop_front();
         for (auto &r : b.reqs) {
             r->status = ce == cudaSuccess ? GBMP_OK : GBMP_ERR_CUDA;
             finish_request(s, r);
         }
         s->budget_used -= b.bytes;
+        s->free_slots.push_back(b.slot);
         s->cv_sched.notify_all();
         s->cv_complete.notify_all();
     }
@@ -263,6 +249,7 @@ void plan_loop(gbmp_server_s *s, int worker) {
     gbmp_status cs = gbmp_batch_planner_create(s->cfg.plan_batch, s->cfg.planner_max_nodes, max_links,
                                                s->cfg.plan_path_cap, &bp);
     if (cs == GBMP_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) cs = GBMP_ERR_CUDA;
+    std::vector<float> paths;
     std::unique_lock<std::mutex> lk(s->mu);
     if (cs != GBMP_OK) s->fatal = cs;
     (void)worker;
@@ -290,7 +277,8 @@ void plan_loop(gbmp_server_s *s, int worker) {
         set.step_rule = s->cfg.step_rule;
         set.time_limit_s = s->cfg.plan_time_limit_s;
         std::vector<gbmp_rrtc_result> res(take.size());
-        std::vector<float> paths((size_t)take.size() * s->cfg.plan_path_cap * max_links);
+        if (paths.size() < (size_t)take.size() * s->cfg.plan_path_cap * max_links)
+            paths.resize((size_t)s->cfg.plan_batch * s->cfg.plan_path_cap * max_links);
         gbmp_status ps = cs != GBMP_OK ? cs
                                        : gbmp_rrtc_solve_batch(bp, (int)take.size(), probs.data(), &set,
                                                                s->cfg.plan_lanes, 1, res.data(), paths.data(), st);
@@ -384,6 +372,30 @@ gbmp_status gbmp_server_start(gbmp_server s) {
     std::lock_guard<std::mutex> lk(s->mu);
     GBMP_CHECK_ARG(!s->sched.joinable(), "server already started");
     GBMP_CHECK_ARG(!s->robots.empty() && !s->envs.empty(), "register robots and environments first");
+    s->max_L = 1;
+    for (auto r : s->robots) s->max_L = std::max(s->max_L, r->L);
+    const int64_t per_state = 4LL * s->max_L + 1;
+    s->cap_states = std::min<int64_t>(s->cfg.max_batch_states,
+                                      s->cfg.hbm_budget_bytes / ((int64_t)s->streams.size() * per_state));
+    GBMP_CHECK_ARG(s->cap_states >= 1, "hbm_budget_bytes too small for one state per stream");
+    for (size_t i = 0; i < s->streams.size(); ++i) {
+        Slot sl;
+        sl.stream = s->streams[i];
+        const size_t qb = align16(sizeof(float) * (size_t)s->cap_states * s->max_L);
+        cudaError_t ce = cudaMalloc(&sl.d_q, qb + align16((size_t)s->cap_states));
+        if (ce == cudaSuccess) ce = cudaMallocHost(&sl.h_q, qb + align16((size_t)s->cap_states));
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (ce != cudaSuccess) {
+            if (sl.d_q) cudaFree(sl.d_q);
+            if (sl.h_q) cudaFreeHost(sl.h_q);
+            set_error("server slot allocation failed: %s", cudaGetErrorString(ce));
+            return ce == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+        }
+        sl.d_v = reinterpret_cast<uint8_t *>(sl.d_q) + qb;
+        sl.h_v = reinterpret_cast<uint8_t *>(sl.h_q) + qb;
+        s->slots.push_back(sl);
+        s->free_slots.push_back((int)i);
+    }
     s->t0 = Clock::now();
     s->sched = std::thread(scheduler_loop, s);
     s->completer = std::thread(completion_loop, s);
@@ -497,11 +509,11 @@ gbmp_status gbmp_server_destroy(gbmp_server s) {
     if (s->sched.joinable()) s->sched.join();
     if (s->completer.joinable()) s->completer.join();
     for (auto &t : s->planners) t.join();
-    for (auto &b : s->in_flight) {
-        cudaEventSynchronize(b.done);
-        cudaFree(b.d_q);
-        cudaFreeHost(b.h_q);
-        cudaEventDestroy(b.done);
+    for (auto &sl : s->slots) {
+        cudaEventSynchronize(sl.done);
+        cudaEventDestroy(sl.done);
+        cudaFree(sl.d_q);
+        cudaFreeHost(sl.h_q);
     }
     for (auto st : s->streams) cudaStreamDestroy(st);
     delete s;
