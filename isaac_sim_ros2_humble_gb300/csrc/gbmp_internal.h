@@ -75,6 +75,20 @@ struct ProfScope {
     ProfScope &operator=(const ProfScope &) = delete;
 };
 
+// Batched planning in two halves (gbmp_rrtc.cu), used by the request server to hand
+// results out as each problem of a launch ends: batch_begin queues the launch on `st`,
+// batch_flag reads problem i's host-mapped completion word (0 running, path length + 1
+// when solved, -status otherwise), batch_copy_path copies a finished problem's path
+// while the launch continues, batch_end waits and fills every result.  The caller
+// holds batch_mutex(b) from begin to end.
+gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *problems, const gbmp_rrtc_settings *s,
+                        int lanes_per_problem, int use_graph, cudaStream_t st);
+int batch_flag(gbmp_batch_planner b, int i);
+gbmp_status batch_copy_path(gbmp_batch_planner b, int i, int L, int len, float *h_path, cudaStream_t st);
+gbmp_status batch_end(gbmp_batch_planner b, const gbmp_rrtc_problem *problems, gbmp_rrtc_result *results,
+                      float *h_paths, cudaStream_t st);
+std::mutex &batch_mutex(gbmp_batch_planner b);
+
 }  // namespace gbmp
 
 struct gbmp_robot_s {

@@ -44,6 +44,8 @@ struct RrtcDev {
     float *path;              // [path_cap * L]
     int *path_len;            // [1], -1 if the path buffer was too small
     int cap, stride, path_cap;
+    volatile int *flag;       // host-mapped completion word (batched solves) or null:
+                              // path length + 1 when solved, -status when ended without a path
 };
 
 struct RrtcParams {
@@ -160,6 +162,36 @@ __device__ int block_append(const RrtcDev &P, int tr, const float *q, int par, i
     }
     __syncthreads();
     return idx;
+}
+
+// Walk both parent chains into the path (start tree root first); one thread.  Returns
+// the number of states, or minus the required size when the buffer is too small.
+__device__ int trace_path(const RrtcDev &P, int L) {
+    const int tr = P.state[2];
+    const int a = P.state[3], b = P.state[4];
+    const int na = tr == 0 ? a : b, nb = tr == 0 ? b : a;
+    int len0 = 0, len1 = 0;
+    for (int i = na; i >= 0 && len0 <= P.cap; i = (P.parent[0][i] == i ? -1 : P.parent[0][i])) ++len0;
+    for (int i = nb; i >= 0 && len1 <= P.cap; i = (P.parent[1][i] == i ? -1 : P.parent[1][i])) ++len1;
+    if (len0 + len1 > P.path_cap || len0 > P.cap || len1 > P.cap) return -(len0 + len1);
+    int k = len0 - 1;
+    for (int i = na; i >= 0; i = (P.parent[0][i] == i ? -1 : P.parent[0][i]), --k)
+        for (int j = 0; j < L; ++j) P.path[k * L + j] = __ldcg(P.nodes[0] + (long long)i * P.stride + j);
+    k = len0;
+    for (int i = nb; i >= 0; i = (P.parent[1][i] == i ? -1 : P.parent[1][i]), ++k)
+        for (int j = 0; j < L; ++j) P.path[k * L + j] = __ldcg(P.nodes[1] + (long long)i * P.stride + j);
+    return len0 + len1;
+}
+
+// Publish the end of a problem to the host-mapped completion word once (state[10]
+// elects the writer).
+__device__ void publish_end(const RrtcDev &P, int value) {
+    if (!P.flag) return;
+    if (atomicCAS(P.state + 10, 0, 1) == 0) {
+        __threadfence_system();
+        *P.flag = value;
+        __threadfence_system();
+    }
 }
 
 // One extension lane of one problem (the body of both the single-problem and the
@@ -298,6 +330,13 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
                 P.state[3] = cur;
                 P.state[4] = tgt;
                 __threadfence();
+                if (P.flag) {
+                    // the winner traces at once so the host can take this result while the
+                    // launch continues for other problems
+                    const int len = trace_path(P, L);
+                    *P.path_len = len;
+                    publish_end(P, len > 0 ? len + 1 : -5);
+                }
             }
         }
         __syncthreads();
@@ -341,6 +380,7 @@ __global__ void __launch_bounds__(kRrtcThreads) k_rrtc_batch(const BatchProblem 
             sP = probs[p].P;
             sSeed = probs[p].seed;
             sLane = atomicAdd(probs[p].P.state + 6, 1);
+            atomicAdd(probs[p].P.state + 7, 1);
         }
         __syncthreads();
         RrtcParams q = prm;
@@ -348,6 +388,14 @@ __global__ void __launch_bounds__(kRrtcThreads) k_rrtc_batch(const BatchProblem 
         q.seed = sSeed;
         rrtc_lane<SPL, CULL>(sR, sE, sP, q, sLane);
         __syncthreads();
+        if (threadIdx.x == 0) {
+            // the last lane to leave an ended, unsolved problem publishes its end
+            __threadfence();
+            if (atomicSub(sP.state + 7, 1) == 1) {
+                const int stt = *(volatile int *)sP.state;
+                if (stt != kStRunning && stt != kStSolved) publish_end(sP, -stt);
+            }
+        }
         if (threadIdx.x == 0) {
             int next = -1;
             const int start = (int)((unsigned)atomicAdd(rr, 1) % (unsigned)n);
@@ -665,6 +713,10 @@ struct gbmp_batch_planner_s {
     BatchProblem *h_table = nullptr;      // pinned host mirror
     float *d_roots = nullptr, *h_roots = nullptr;   // [max_problems * 2 * max_links]
     int *d_summary = nullptr, *h_summary = nullptr; // [max_problems * 8]
+    int *h_flags = nullptr, *d_flags = nullptr;     // host-mapped completion words [max_problems]
+    // launch in progress (between batch_begin and batch_end)
+    int cur_n = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     unsigned long long *d_deadline = nullptr;   // [0] deadline, [1] round-robin counter
     std::vector<int> prev;                // 2 per problem
     // captured graphs by launch shape (a few shapes, least recently used evicted)
@@ -744,6 +796,10 @@ gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, i
     if (e == cudaSuccess) e = cudaMalloc(&b->d_summary, sizeof(int) * 8 * max_problems);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_summary, sizeof(int) * 8 * max_problems);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_deadline, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaHostAlloc(&b->h_flags, sizeof(int) * max_problems, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&b->d_flags, b->h_flags, 0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     if (e != cudaSuccess) {
         set_error("batch planner allocation failed: %s", cudaGetErrorString(e));
         gbmp_batch_planner_destroy(b);
@@ -772,6 +828,9 @@ gbmp_status gbmp_batch_planner_destroy(gbmp_batch_planner b) {
     if (b->d_summary) cudaFree(b->d_summary);
     if (b->h_summary) cudaFreeHost(b->h_summary);
     if (b->d_deadline) cudaFree(b->d_deadline);
+    if (b->h_flags) cudaFreeHost(b->h_flags);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
     delete b;
     return GBMP_OK;
 }
@@ -780,13 +839,23 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
                                   const gbmp_rrtc_settings *s, int32_t lanes_per_problem, int32_t use_graph,
                                   gbmp_rrtc_result *results, float *h_paths, void *stream) {
     GBMP_CHECK_ARG(b && problems && s && results, "NULL argument");
+    std::lock_guard<std::mutex> lock(b->mu);
+    gbmp_status st = gbmp::batch_begin(b, n, problems, s, lanes_per_problem, use_graph, (cudaStream_t)stream);
+    if (st) return st;
+    return gbmp::batch_end(b, problems, results, h_paths, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace gbmp {
+
+gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *problems, const gbmp_rrtc_settings *s,
+                        int lanes_per_problem, int use_graph, cudaStream_t st) {
     GBMP_CHECK_ARG(n >= 1 && n <= b->max_problems, "n %d outside [1, %d]", n, b->max_problems);
     GBMP_CHECK_ARG(lanes_per_problem >= 1 && lanes_per_problem <= 4096, "lanes_per_problem outside [1, 4096]");
     GBMP_CHECK_ARG((long long)n * lanes_per_problem <= (1LL << 30), "too many blocks");
     GBMP_CHECK_ARG(s->range > 0.f && s->max_iters >= 1, "bad settings");
     GBMP_CHECK_ARG(s->step_rule == GBMP_STEP_L2 || s->step_rule == GBMP_STEP_LINF, "unknown step rule");
-    std::lock_guard<std::mutex> lock(b->mu);
-    cudaStream_t st = (cudaStream_t)stream;
     int spl = 1;
     bool cull = true;
     size_t smem = 0;
@@ -821,6 +890,7 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
         bp.P.cap = b->cap;
         bp.P.stride = b->stride;
         bp.P.path_cap = b->path_cap;
+        bp.P.flag = b->d_flags + i;
         bp.seed = pr.seed;
         bp.start = b->d_roots + (size_t)i * 2 * b->max_links;
         bp.goal = bp.start + b->max_links;
@@ -831,6 +901,7 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
             b->h_roots[(size_t)i * 2 * b->max_links + j] = pr.start[j];
             b->h_roots[(size_t)i * 2 * b->max_links + b->max_links + j] = pr.goal[j];
         }
+        b->h_flags[i] = 0;
     }
     RrtcParams prm;
     prm.lanes = lanes_per_problem;
@@ -842,10 +913,8 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
     prm.deadline_ns = 0;
     prm.deadline_ptr = b->d_deadline;
     const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
-    cudaEvent_t e0, e1;
-    GBMP_CUDA(cudaEventCreate(&e0));
-    GBMP_CUDA(cudaEventCreate(&e1));
-    GBMP_CUDA(cudaEventRecord(e0, st));
+    b->cur_n = n;
+    GBMP_CUDA(cudaEventRecord(b->ev0, st));
     if (use_graph) {
         const long long key[8] = {n, lanes_per_problem, (long long)smem, spl, cull, s->max_iters,
                                   (long long)(lim * 1e6), (long long)(prm.range * 1e6) ^ ((long long)(prm.res * 1e9) << 20)};
@@ -884,12 +953,25 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
         gbmp_status bs = batch_launch(b, n, lanes_per_problem, prm, spl, cull, smem, lim, st);
         if (bs) return bs;
     }
-    GBMP_CUDA(cudaEventRecord(e1, st));
+    GBMP_CUDA(cudaEventRecord(b->ev1, st));
+    return GBMP_OK;
+}
+
+int batch_flag(gbmp_batch_planner b, int i) { return *(volatile int *)(b->h_flags + i); }
+
+gbmp_status batch_copy_path(gbmp_batch_planner b, int i, int L, int len, float *h_path, cudaStream_t st) {
+    const float *src = b->h_table[i].P.path;
+    GBMP_CUDA(cudaMemcpyAsync(h_path, src, sizeof(float) * (size_t)len * L, cudaMemcpyDeviceToHost, st));
+    GBMP_CUDA(cudaStreamSynchronize(st));
+    return GBMP_OK;
+}
+
+gbmp_status batch_end(gbmp_batch_planner b, const gbmp_rrtc_problem *problems, gbmp_rrtc_result *results,
+                      float *h_paths, cudaStream_t st) {
+    const int n = b->cur_n;
     GBMP_CUDA(cudaStreamSynchronize(st));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     int max_len = 0;
     for (int i = 0; i < n; ++i) {
         const int *o = b->h_summary + 8 * i;
@@ -907,7 +989,7 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
         max_len = std::max(max_len, r.path_len);
     }
     if (h_paths && max_len > 0) {
-        // one pitched copy: rows of max_len * L floats from every problem's path buffer
+        // one pitched copy: rows of max_len * max_links floats from every problem's path buffer
         const size_t pitch_src = b->per_problem;
         const size_t row = sizeof(float) * (size_t)max_len * b->max_links;
         const size_t pitch_dst = sizeof(float) * (size_t)b->path_cap * b->max_links;
@@ -937,4 +1019,7 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
     return GBMP_OK;
 }
 
-}  // extern "C"
+std::mutex &batch_mutex(gbmp_batch_planner b) { return b->mu; }
+
+}  // namespace gbmp
+

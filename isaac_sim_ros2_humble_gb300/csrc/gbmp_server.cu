@@ -22,6 +22,7 @@
 //    percentiles.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -239,20 +240,37 @@ void completion_loop(gbmp_server_s *s) {
     }
 }
 
-// Plan worker: solves every pending plan request in one batched launch.
+// Plan worker: solves everything pending in one batched launch and hands each result
+// out as soon as its problem ends (host-mapped completion words), while the launch
+// continues for the others.
 void plan_loop(gbmp_server_s *s, int worker) {
     cudaSetDevice(s->device);
     gbmp_batch_planner bp = nullptr;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, cst = nullptr;
     int max_links = 1;
     for (auto r : s->robots) max_links = std::max(max_links, r->L);
     gbmp_status cs = gbmp_batch_planner_create(s->cfg.plan_batch, s->cfg.planner_max_nodes, max_links,
                                                s->cfg.plan_path_cap, &bp);
-    if (cs == GBMP_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) cs = GBMP_ERR_CUDA;
-    std::vector<float> paths;
+    if (cs == GBMP_OK && (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+                          cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking) != cudaSuccess))
+        cs = GBMP_ERR_CUDA;
     std::unique_lock<std::mutex> lk(s->mu);
     if (cs != GBMP_OK) s->fatal = cs;
     (void)worker;
+    auto path_cost = [&](const std::shared_ptr<Request> &r, int len) {
+        const gbmp_robot rb = s->robots[r->robot];
+        double c = 0.0;
+        for (int k = 1; k < len; ++k) {
+            double s2 = 0.0;
+            for (int j = 0; j < rb->L; ++j)
+                if (rb->active[j]) {
+                    const double d = (double)r->path[k * rb->L + j] - r->path[(k - 1) * rb->L + j];
+                    s2 += d * d;
+                }
+            c += std::sqrt(s2);
+        }
+        return (float)c;
+    };
     while (true) {
         s->cv_plan.wait(lk, [&] { return s->stop || !s->plan_q.empty(); });
         if (s->stop) break;
@@ -263,9 +281,10 @@ void plan_loop(gbmp_server_s *s, int worker) {
         }
         ++s->plan_batches;
         lk.unlock();
+        const int n = (int)take.size();
         const auto now = Clock::now();
-        std::vector<gbmp_rrtc_problem> probs(take.size());
-        for (size_t i = 0; i < take.size(); ++i) {
+        std::vector<gbmp_rrtc_problem> probs(n);
+        for (int i = 0; i < n; ++i) {
             take[i]->t_start = now;
             probs[i] = {s->robots[take[i]->robot], s->envs[take[i]->env], take[i]->start, take[i]->goal, take[i]->seed};
         }
@@ -276,36 +295,72 @@ void plan_loop(gbmp_server_s *s, int worker) {
         set.resolution = s->cfg.plan_resolution;
         set.step_rule = s->cfg.step_rule;
         set.time_limit_s = s->cfg.plan_time_limit_s;
-        std::vector<gbmp_rrtc_result> res(take.size());
-        if (paths.size() < (size_t)take.size() * s->cfg.plan_path_cap * max_links)
-            paths.resize((size_t)s->cfg.plan_batch * s->cfg.plan_path_cap * max_links);
-        gbmp_status ps = cs != GBMP_OK ? cs
-                                       : gbmp_rrtc_solve_batch(bp, (int)take.size(), probs.data(), &set,
-                                                               s->cfg.plan_lanes, 1, res.data(), paths.data(), st);
-        for (size_t i = 0; i < take.size(); ++i) {
+        std::vector<char> done(n, 0);
+        gbmp_status ps = cs != GBMP_OK ? cs : gbmp::batch_begin(bp, n, probs.data(), &set, s->cfg.plan_lanes, 1, st);
+        // hand out results as problems end
+        auto deliver = [&](int i, int flag) {
             auto &r = take[i];
-            r->status = ps;
-            if (ps == GBMP_OK) {
-                r->solved = res[i].solved;
-                r->cost = res[i].cost;
-                const int L = s->robots[r->robot]->L;
-                const int len = res[i].solved ? res[i].path_len : 0;
-                r->path_len = len;
-                if (len > r->path_cap) {
+            if (flag > 0) {
+                const int len = flag - 1;
+                if (len > r->path_cap || !r->path) {
                     r->status = GBMP_ERR_CAPACITY;
-                } else if (len > 0 && r->path) {
-                    memcpy(r->path, paths.data() + i * (size_t)s->cfg.plan_path_cap * max_links, sizeof(float) * len * L);
+                    r->path_len = len;
+                } else {
+                    r->status = gbmp::batch_copy_path(bp, i, s->robots[r->robot]->L, len, r->path, cst);
+                    r->solved = r->status == GBMP_OK;
+                    r->path_len = len;
+                    r->cost = path_cost(r, len);
                 }
-                if (!r->solved && r->status == GBMP_OK) r->status = GBMP_ERR_NOT_SOLVED;
+            } else {
+                r->status = flag == -4 ? GBMP_ERR_TIMEOUT : (flag == -5 ? GBMP_ERR_CAPACITY : GBMP_ERR_NOT_SOLVED);
             }
+            std::lock_guard<std::mutex> g(s->mu);
+            finish_request(s, r);
+            s->cv_complete.notify_all();
+        };
+        if (ps == GBMP_OK) {
+            int left = n;
+            while (left > 0) {
+                for (int i = 0; i < n; ++i)
+                    if (!done[i]) {
+                        const int f = gbmp::batch_flag(bp, i);
+                        if (f != 0) {
+                            done[i] = 1;
+                            --left;
+                            deliver(i, f);
+                        }
+                    }
+                if (left == 0 || cudaStreamQuery(st) != cudaErrorNotReady) break;
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            }
+            std::vector<gbmp_rrtc_result> res(n);
+            ps = gbmp::batch_end(bp, probs.data(), res.data(), nullptr, st);
+            for (int i = 0; i < n; ++i) {
+                if (done[i]) continue;
+                done[i] = 1;
+                if (ps == GBMP_OK && res[i].solved) deliver(i, res[i].path_len + 1);
+                else if (ps == GBMP_OK) deliver(i, -res[i].status);
+                else {
+                    take[i]->status = ps;
+                    std::lock_guard<std::mutex> g(s->mu);
+                    finish_request(s, take[i]);
+                    s->cv_complete.notify_all();
+                }
+            }
+        } else {
+            std::lock_guard<std::mutex> g(s->mu);
+            for (auto &r : take) {
+                r->status = ps;
+                finish_request(s, r);
+            }
+            s->cv_complete.notify_all();
         }
         lk.lock();
-        for (auto &r : take) finish_request(s, r);
-        s->cv_complete.notify_all();
     }
     lk.unlock();
     if (bp) gbmp_batch_planner_destroy(bp);
     if (st) cudaStreamDestroy(st);
+    if (cst) cudaStreamDestroy(cst);
 }
 
 double pct(std::vector<double> v, double p) {
