@@ -251,7 +251,9 @@ void plan_loop(gbmp_server_s *s, int worker) {
     for (auto r : s->robots) max_links = std::max(max_links, r->L);
     gbmp_status cs = gbmp_batch_planner_create(s->cfg.plan_batch, s->cfg.planner_max_nodes, max_links,
                                                s->cfg.plan_path_cap, &bp);
-    if (cs == GBMP_OK && (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    if (cs == GBMP_OK && (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, lo_prio) != cudaSuccess ||
                           cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking) != cudaSuccess))
         cs = GBMP_ERR_CUDA;
     std::unique_lock<std::mutex> lk(s->mu);
@@ -296,7 +298,10 @@ void plan_loop(gbmp_server_s *s, int worker) {
         set.step_rule = s->cfg.step_rule;
         set.time_limit_s = s->cfg.plan_time_limit_s;
         std::vector<char> done(n, 0);
-        gbmp_status ps = cs != GBMP_OK ? cs : gbmp::batch_begin(bp, n, probs.data(), &set, s->cfg.plan_lanes, 1, st);
+        // small batches get more lanes per problem (up to 1024 blocks per launch), large
+        // ones at least plan_lanes
+        const int lpp = std::max(s->cfg.plan_lanes, std::min(1024, 1024 / n));
+        gbmp_status ps = cs != GBMP_OK ? cs : gbmp::batch_begin(bp, n, probs.data(), &set, lpp, 0, st);
         // hand out results as problems end
         auto deliver = [&](int i, int flag) {
             auto &r = take[i];
@@ -391,9 +396,13 @@ gbmp_status gbmp_server_create(const gbmp_server_config *cfg, gbmp_server *out) 
     auto *s = new gbmp_server_s();
     s->cfg = *cfg;
     cudaGetDevice(&s->device);
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     for (int i = 0; i < cfg->num_streams; ++i) {
         cudaStream_t st;
-        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        // check batches are short: give them the highest priority so their blocks are
+        // scheduled ahead of the long planning launches
+        if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, hi_prio) != cudaSuccess) {
             set_error("stream creation failed");
             gbmp_server_destroy(s);
             return GBMP_ERR_CUDA;
