@@ -155,6 +155,28 @@ GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const floa
                              int64_t n_edges, float resolution, int32_t step_rule, uint8_t *d_ok,
                              int32_t *d_first_hit, float *d_length, int32_t *d_num_steps, void *stream);
 
+/* gbmp_check_edges without any allocation: same arguments, kernels and results, but its
+ * working memory is a fixed 5 MiB device array inside the library (one per device)
+ * instead of a buffer grown with cudaMalloc.  No counterpart in the reference, whose
+ * checkMotions allocates and frees its state buffers on every call.
+ * For callers that must not allocate device memory: a control loop with a latency bound
+ * (cudaMalloc / cudaFree can block and cudaFree synchronises the device), a process whose
+ * device memory is fully reserved up front, or code that runs while memory is exhausted.
+ * Limits: n_edges <= 65536 and n_edges * num_links <= 1,048,576; larger calls return
+ * GBMP_ERR_CAPACITY with a message and do nothing (use gbmp_check_edges or split them).
+ * The scratch's wave counters must start at zero: every call zeroes them on `stream`
+ * before its first kernel; all other scratch is written before it is read.
+ * Calls on one device share the scratch: calls whose work overlaps on the device (other
+ * streams, other host threads) race and give wrong results; order them on one stream or
+ * synchronise between them.  Different devices do not share it.
+ * The first call on each device (n_edges = 0 is enough) looks up the scratch's device
+ * address with that device current; a caller that captures streams makes that first
+ * call before it begins a capture.  Stream-synchronising like gbmp_check_edges. */
+GBMP_API gbmp_status gbmp_check_edges_noalloc(gbmp_robot robot, gbmp_env env, const float *d_from,
+                                     const float *d_to, int64_t n_edges, float resolution,
+                                     int32_t step_rule, uint8_t *d_ok, int32_t *d_first_hit,
+                                     float *d_length, int32_t *d_num_steps, void *stream);
+
 /* Nearest neighbour, replacing SingleArmStateManager::find_the_nearest_neighbors
  * (SingleArmStates.cu:1265-1431).  d_tree [M*L]; candidate indices d_cand [n_cand]
  * (NULL = all M nodes); d_queries [Q*L]; d_out [Q] index of the nearest candidate by

@@ -96,6 +96,7 @@ SIGNATURES = {
     "gbmp_fk": [_vp, _vp, _i64, _vp, _vp, _vp],
     "gbmp_check_states": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp],
     "gbmp_check_edges": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
+    "gbmp_check_edges_noalloc": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
     "gbmp_nearest": [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp],
     "gbmp_steer": [_vp, _vp, _vp, _vp, _i64, _f32, _vp],
     "gbmp_sample": [_vp, _u64, _u64, _i64, _vp, _vp],

@@ -745,3 +745,148 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Edge validation without allocation.  The scratch of gbmp_check_edges lives in one
+// file-scope device array instead of the robot's growable buffer:
+//   [0, 4 Ei)            nsteps[E]      int   written by k_edge_setup
+//   [4 Ei, 8 Ei)         first_hit[E]   int   written by k_edge_setup
+//   [8 Ei, 12 Ei)        liveA[E]       int   written by k_edge_setup
+//   [12 Ei, 16 Ei)       liveB[E]       int   written by k_edge_compact
+//   [16 Ei, +4 D)        dir[E*L]       float written by k_edge_setup
+//   [.., +4 (W+2))       ctr[W+2]       int   MUST START AT ZERO: zeroed on the stream
+//                                             at the start of every call
+// with Ei = kNoAllocMaxEdges, D = kNoAllocMaxDirFloats, W = kMaxWaves.  The array is
+// shared by every call on a device, so calls that overlap on the device race.
+// ---------------------------------------------------------------------------------
+namespace gbmp {
+
+constexpr long long kNoAllocMaxEdges = 65536;
+constexpr long long kNoAllocMaxDirFloats = 1LL << 20;   // n_edges * links
+constexpr size_t kNoAllocEdgeInts = sizeof(int) * kNoAllocMaxEdges;
+constexpr size_t kNoAllocDirOffset = 4 * kNoAllocEdgeInts;
+constexpr size_t kNoAllocCtrOffset = kNoAllocDirOffset + sizeof(float) * kNoAllocMaxDirFloats;
+constexpr size_t kNoAllocBytes = (kNoAllocCtrOffset + sizeof(int) * (kMaxWaves + 2) + 255) & ~size_t(255);
+static_assert(kNoAllocDirOffset % 256 == 0 && kNoAllocCtrOffset % 256 == 0, "scratch regions stay aligned");
+
+static __device__ __align__(256) unsigned char g_edge_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+
+// Device address of g_edge_scratch on the current device, looked up once per device.
+static gbmp_status noalloc_scratch(unsigned char **out) {
+    static std::mutex mu;
+    static unsigned char *addr[kNoAllocMaxDevices] = {};
+    int dev = 0;
+    GBMP_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("device %d is beyond the %d devices the allocation-free scratch is tracked for", dev,
+                  kNoAllocMaxDevices);
+        return GBMP_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        GBMP_CUDA(cudaGetSymbolAddress(&p, g_edge_scratch));
+        if (!p) {
+            set_error("cudaGetSymbolAddress gave no address for the edge scratch on device %d", dev);
+            return GBMP_ERR_CUDA;
+        }
+        addr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = addr[dev];
+    return GBMP_OK;
+}
+
+}  // namespace gbmp
+
+extern "C" {
+
+gbmp_status gbmp_check_edges_noalloc(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to,
+                                     int64_t E, float res, int32_t rule, uint8_t *d_ok, int32_t *d_first_hit,
+                                     float *d_length, int32_t *d_num_steps, void *stream) {
+    GBMP_CHECK_ARG(r && env, "robot/env is NULL");
+    GBMP_CHECK_ARG(rule == GBMP_STEP_L2 || rule == GBMP_STEP_LINF, "unknown step rule %d", rule);
+    GBMP_CHECK_ARG(E >= 0, "edge count %lld < 0", (long long)E);
+    if (E > kNoAllocMaxEdges || E * (long long)r->L > kNoAllocMaxDirFloats) {
+        set_error("%lld edges x %d links exceed the allocation-free scratch (at most %lld edges and %lld "
+                  "edges x links); use gbmp_check_edges or split the call",
+                  (long long)E, r->L, kNoAllocMaxEdges, kNoAllocMaxDirFloats);
+        return GBMP_ERR_CAPACITY;
+    }
+    unsigned char *base = nullptr;
+    gbmp_status st = noalloc_scratch(&base);   // also the set-up when E == 0
+    if (st) return st;
+    if (E == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
+    if (!(res > 0.f)) res = r->resolution;
+    GBMP_CHECK_ARG(std::isfinite(res), "resolution is not finite");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int L = r->L;
+    int *nsteps = (int *)base, *fh = (int *)(base + kNoAllocEdgeInts), *liveA = (int *)(base + 2 * kNoAllocEdgeInts),
+        *liveB = (int *)(base + 3 * kNoAllocEdgeInts);
+    float *dir = (float *)(base + kNoAllocDirOffset);
+    int *ctr = (int *)(base + kNoAllocCtrOffset);
+    GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
+    const int tb = 256;
+    const unsigned blocks = (unsigned)((E + tb - 1) / tb);
+    k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, fh, liveA, ctr, d_length,
+                                      d_num_steps);
+    GBMP_CUDA(cudaGetLastError());
+    count_launch(1);
+    int n_max = 0;
+    GBMP_CUDA(cudaMemcpyAsync(&n_max, ctr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GBMP_CUDA(cudaStreamSynchronize(s));
+    {
+        int b = 0, waves = 0;
+        while (b < n_max && waves <= kMaxWaves) { b = wave_end(b); ++waves; }
+        if (waves > kMaxWaves) {
+            set_error("an edge has %d interpolated states; at most %d are supported per call", n_max,
+                      max_edge_states());
+            return GBMP_ERR_CAPACITY;
+        }
+    }
+
+    const DevEnv Ev = env->dev();
+    DevRobot D = r->dev;
+    D.work = work_counter();
+    const size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
+    int grid = 0;
+    const bool cull = r->dev.cull != 0;
+    GBMP_SPL_SWITCH(r->dev.spl, {
+        st = cull ? persistent_grid(k_edge_wave<SPL, true>, smem, r->num_sms, &grid)
+                  : persistent_grid(k_edge_wave<SPL, false>, smem, r->num_sms, &grid);
+    });
+    if (st) return st;
+    int b0 = 0, wave = 0;
+    int *live_in = liveA, *live_out = liveB;
+    while (b0 < n_max) {
+        const int b1 = wave_end(b0);
+        int *cnt_in = ctr + 1 + wave, *cnt_out = ctr + 2 + wave;
+        GBMP_SPL_SWITCH(r->dev.spl, {
+            if (cull)
+                k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                    D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+            else
+                k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                    D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+        });
+        GBMP_CUDA(cudaGetLastError());
+        count_launch(1);
+        if (b1 < n_max) {
+            k_edge_compact<<<(unsigned)std::min<long long>(blocks, 4LL * r->num_sms), tb, 0, s>>>(
+                live_in, cnt_in, fh, nsteps, b1, live_out, cnt_out);
+            GBMP_CUDA(cudaGetLastError());
+            count_launch(1);
+        }
+        std::swap(live_in, live_out);
+        b0 = b1;
+        ++wave;
+    }
+    k_edge_finish<<<blocks, tb, 0, s>>>(E, fh, d_ok, d_first_hit);
+    GBMP_CUDA(cudaGetLastError());
+    count_launch(1);
+    return GBMP_OK;
+}
+
+}  // extern "C"
