@@ -68,6 +68,20 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_over_ranks(dist, ws, device, timed_s, checks, e2e_s):
+    """Job totals of a weak-scaling run: every rank validates its own shard of edges,
+    so the job's time is the slowest rank's (max) and its checks are the sum.  One
+    collective for the times and one for the counts, in the same order on every rank."""
+    if ws == 1:
+        return timed_s, float(checks), e2e_s
+    import torch
+    t = torch.tensor([timed_s, e2e_s], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(checks)], dtype=torch.float64, device=device)
+    dist.all_reduce(c)
+    return float(t[0].item()), float(c[0].item()), float(t[1].item())
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -548,16 +562,6 @@ def main():
     exec_flops, exec_states = _lib.work_read()
     _lib.work_counting(False)
     total_s = sum(step_ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([total_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-        c = torch.tensor([checks], device=dev, dtype=torch.float64)
-        dist.all_reduce(c)
-        all_checks = float(c.item())
-    else:
-        all_checks = float(checks)
-    value = all_checks * args.steps / total_s
 
     # end-to-end through the same C-ABI call with host buffers
     h_from = torch.from_numpy(qf).pin_memory()
@@ -580,10 +584,8 @@ def main():
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = sum(e2e_ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    total_s, all_checks, e2e_s = reduce_over_ranks(dist, ws, dev, total_s, checks, e2e_s)
+    value = all_checks * args.steps / total_s
     e2e_value = all_checks * args.steps / e2e_s
 
     if rank == 0:
