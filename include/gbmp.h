@@ -107,6 +107,14 @@ GBMP_API gbmp_status gbmp_robot_info(gbmp_robot robot, int32_t *num_links, int32
 GBMP_API gbmp_status gbmp_robot_self_pairs(gbmp_robot robot, int32_t *h_pairs, float *h_thr_sq, int32_t cap);
 /* Select the kernel family used by later calls: 0 table-driven, 1 generated. */
 GBMP_API gbmp_status gbmp_robot_use_codegen(gbmp_robot robot, int32_t enable);
+/* The generated kernels of a robot created with GBMP_ROBOT_CODEGEN (the reference writes
+ * its generated source to a file, SingleArmSpace.cu:98-123): the CUDA C++ source
+ * (copied when `source` is non-NULL and `capacity` suffices; *source_len = bytes incl.
+ * the terminating 0), the cache key *hash, *cache = 0 compiled by this call, 1 found in
+ * the in-process cache, 2 read from the GBMP_CODEGEN_CACHE directory, and the NVRTC time
+ * *compile_ms (0 when cached).  Any output may be NULL. */
+GBMP_API gbmp_status gbmp_robot_codegen_info(gbmp_robot robot, char *source, int64_t capacity, int64_t *source_len,
+                                    uint64_t *hash, int32_t *cache, double *compile_ms);
 
 /* Replaces the constructors of EnvConstraintSphere (EnvConstraintSphere.h:21-25),
  * EnvConstraintCuboid (EnvConstraintCuboid.h:23-29; pos[3], row-major rotation[9],

@@ -90,6 +90,8 @@ SIGNATURES = {
     "gbmp_robot_info": [_vp, _i32p, _i32p, _i32p, _i32p, _i32p],
     "gbmp_robot_self_pairs": [_vp, _vp, _vp, _i32],
     "gbmp_robot_use_codegen": [_vp, _i32],
+    "gbmp_robot_codegen_info": [_vp, C.c_char_p, _i64, C.POINTER(_i64), C.POINTER(_u64), C.POINTER(_i32),
+                                C.POINTER(C.c_double)],
     "gbmp_env_create": [_i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, C.POINTER(_vp)],
     "gbmp_env_destroy": [_vp],
     "gbmp_env_counts": [_vp, _i32p, _i32p, _i32p],

@@ -61,6 +61,16 @@ class Robot:
     def use_codegen(self, enable: bool):
         check(_lib.load().gbmp_robot_use_codegen(self.handle, int(enable)))
 
+    def codegen_info(self):
+        """Generated source, cache key, cache origin (0 compiled, 1 in process, 2 disk)
+        and NVRTC milliseconds of a robot created with codegen=True."""
+        lib = _lib.load()
+        n, h, c, ms = C.c_int64(), C.c_uint64(), C.c_int32(), C.c_double()
+        check(lib.gbmp_robot_codegen_info(self.handle, None, 0, C.byref(n), C.byref(h), C.byref(c), C.byref(ms)))
+        buf = C.create_string_buffer(n.value)
+        check(lib.gbmp_robot_codegen_info(self.handle, buf, n.value, None, None, None, None))
+        return {"source": buf.value.decode(), "hash": h.value, "cache": c.value, "compile_ms": ms.value}
+
 
 class Env:
     """An obstacle set resident on the device (replaces the EnvConstraint* tables)."""

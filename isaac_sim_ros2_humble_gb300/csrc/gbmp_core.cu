@@ -410,6 +410,9 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
         sph[4 * k] = r->sph_pos[3 * k]; sph[4 * k + 1] = r->sph_pos[3 * k + 1];
         sph[4 * k + 2] = r->sph_pos[3 * k + 2]; sph[4 * k + 3] = r->sph_r[k];
     }
+    r->h_jl = jl;
+    r->h_axn = axn;
+    r->h_axr = axr;
     // Sphere groups (links that carry spheres, in link order) and their bounding spheres.
     std::vector<int> link2grp(L, -1), glink, sgrp(S ? S : 1, 0);
     for (int l = 0; l < L; ++l)
@@ -499,7 +502,16 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     }
     D.grp = (const float *)(b + o_grp); D.glink = (const int *)(b + o_glink);
     D.sgrp = (const int *)(b + o_sgrp); D.lpair = (const int4 *)(b + o_lpair);
-    (void)flags;
+    if (flags & GBMP_ROBOT_CODEGEN) {
+        gbmp_status st = codegen_build(r);
+        if (st) {
+            const std::string why = g_err;
+            gbmp_robot_destroy(r);
+            g_err = why;
+            return st;
+        }
+        r->use_cg = true;
+    }
     *out = r;
     return GBMP_OK;
 }
@@ -507,6 +519,7 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
 gbmp_status gbmp_robot_destroy(gbmp_robot r) {
     if (!r) return GBMP_OK;
     if (r->d_block) cudaFree(r->d_block);
+    codegen_free(r->cg);
     delete r;
     return GBMP_OK;
 }
@@ -608,6 +621,7 @@ gbmp_status gbmp_fk(gbmp_robot r, const float *d_q, int64_t n, float *d_poses, f
     GBMP_CHECK_ARG(n >= 0, "n < 0");
     if (n == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_q, "q is NULL");
+    if (r->use_cg) return codegen_fk(r, d_q, n, d_poses, d_centers, (cudaStream_t)stream);
     const size_t smem = smem_tables_bytes(r->dev, 0) + smem_warp_bytes(r->dev) * kWarpsPerBlock;
     int grid = 0;
     gbmp_status st = persistent_grid(k_fk, smem, r->num_sms, &grid);
@@ -683,9 +697,14 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
     const int tb = 256;
     const unsigned blocks = (unsigned)((E + tb - 1) / tb);
-    { ProfScope ps(GBMP_PROF_OTHER, s);
-    k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, fh, liveA, ctr, d_length,
-                                      d_num_steps); }
+    if (r->use_cg) {
+        st = codegen_edge_setup(r, d_from, d_to, E, res, rule, nsteps, dir, fh, liveA, ctr, d_length, d_num_steps, s);
+        if (st) return st;
+    } else {
+        ProfScope ps(GBMP_PROF_OTHER, s);
+        k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, fh, liveA, ctr, d_length,
+                                          d_num_steps);
+    }
     GBMP_CUDA(cudaGetLastError());
     int n_max = 0;
     GBMP_CUDA(cudaMemcpyAsync(&n_max, ctr, sizeof(int), cudaMemcpyDeviceToHost, s));

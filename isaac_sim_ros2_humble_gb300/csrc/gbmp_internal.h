@@ -58,7 +58,15 @@ struct DevBuf {
     }
 };
 
-struct Codegen;   // runtime-generated robot kernels (gbmp_codegen.cpp)
+// Runtime-generated robot kernels (gbmp_codegen.cu).
+struct Codegen {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t fk = nullptr, edge_setup = nullptr;
+    std::string source, arch;
+    unsigned long long hash = 0;
+    int cache = 0;              // 0 compiled now, 1 in-process cache, 2 disk cache
+    double compile_ms = 0.0;
+};
 
 // Instrumentation (gbmp_prof.cu).  A ProfScope around a launch counts it and, when
 // profiling is on, records CUDA events on the launching stream around it.
@@ -100,6 +108,7 @@ struct gbmp_robot_s {
     std::vector<int> type, parent, slink;
     std::vector<float> pose16, axis, sph_pos, sph_r, lower, upper, defv;
     std::vector<unsigned char> active, enables;
+    std::vector<float> h_jl, h_axn, h_axr;   // host copies of the uploaded joint tables
     std::vector<int> pairs;          // 2*P
     std::vector<float> thr;          // P
     // device tables (one allocation)
@@ -111,6 +120,16 @@ struct gbmp_robot_s {
     gbmp::Codegen *cg = nullptr;
     bool use_cg = false;
 };
+
+namespace gbmp {
+gbmp_status codegen_build(gbmp_robot_s *r);
+void codegen_free(Codegen *cg);
+gbmp_status codegen_fk(const gbmp_robot_s *r, const float *q, long long n, float *poses, float *centers,
+                       cudaStream_t s);
+gbmp_status codegen_edge_setup(const gbmp_robot_s *r, const float *from, const float *to, long long E, float res,
+                               int rule, int *nsteps, float *dir, int *first_hit, int *live, int *ctr,
+                               float *length_out, int *nsteps_out, cudaStream_t s);
+}  // namespace gbmp
 
 struct gbmp_env_s {
     int ns = 0, nb = 0, nc = 0;
