@@ -1,0 +1,437 @@
+// gbmp_chunk.cu -- edge validation by chunks of consecutive states.
+//
+// The interpolated states of one edge lie millimetres apart, so the obstacles near one
+// state are the obstacles near its neighbours.  A warp takes K consecutive states of
+// one edge (a chunk) and
+//   A. runs the FK of each state, keeping the link poses in shared memory, and bounds
+//      the centre of every sphere group (a link's bounding sphere) over the chunk by an
+//      axis-aligned box;
+//   B. turns each box into a swept group sphere: centre = box centre, radius = half the
+//      box diagonal + the group radius (which already carries kBroadMargin);
+//   C. runs the broad phase ONCE for the chunk: every obstacle against the swept group
+//      spheres, keeping the obstacles that touch any of them (with the group mask) in a
+//      per-warp candidate list;
+//   D. walks the states in order and tests each state's robot spheres exactly against
+//      the candidates only (the same narrow tests as warp_collide_culled), then its
+//      self-collision pairs, stopping at the first colliding state.
+// Because the swept spheres enclose every per-state group sphere, the candidate list
+// holds every obstacle any state of the chunk can touch, and the narrow tests are the
+// exact ones: verdicts and first-hit indices equal the per-state kernel's.  A chunk
+// whose candidates overflow the list falls back to the per-state routine.
+#include "gbmp_internal.h"
+
+namespace gbmp {
+
+constexpr int kChunkCands = 64;
+
+struct ChunkScratch {
+    float *lpK;       // link poses of the chunk's states [K][L*12]
+    float4 *sgb;      // swept group spheres (x, y, z, R) [kMaxGroups]
+    float *sgA;       // |c|^2 - R^2 of each swept sphere
+    unsigned *cl;     // candidate obstacle indices
+    unsigned *cm;     // their group masks
+};
+
+__host__ __device__ inline size_t smem_chunk_bytes(const DevRobot &R, int K) {
+    return align16(sizeof(float) * 12 * R.L * K) + align16(sizeof(float4) * kMaxGroups) +
+           align16(sizeof(float) * kMaxGroups) + 2 * align16(sizeof(unsigned) * kChunkCands);
+}
+
+__device__ inline ChunkScratch carve_chunk(unsigned char *base, const DevRobot &R, int K, int warp) {
+    unsigned char *p = base + smem_chunk_bytes(R, K) * warp;
+    ChunkScratch c;
+    size_t off = 0;
+    c.lpK = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L * K);
+    c.sgb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * kMaxGroups);
+    c.sgA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * kMaxGroups);
+    c.cl = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
+    c.cm = reinterpret_cast<unsigned *>(p + off);
+    return c;
+}
+
+// Append this lane's obstacle (when mask != 0) to the candidate list; returns the new
+// warp-uniform count (which may exceed the list, meaning overflow).
+__device__ __forceinline__ int push_cand(const ChunkScratch &cs, int n, unsigned idx, unsigned mask, int lane) {
+    const unsigned bal = __ballot_sync(kFull, mask != 0u);
+    if (mask) {
+        const int pos = n + __popc(bal & ((1u << lane) - 1u));
+        if (pos < kChunkCands) { cs.cl[pos] = idx; cs.cm[pos] = mask; }
+    }
+    return n + __popc(bal);
+}
+
+// Exact tests of one state (link poses lp) against the chunk's candidates, then its
+// self-collision pairs.  ns_end / nb_end / nc_end delimit the sphere / cuboid /
+// cylinder candidates.
+template <int SPL>
+__device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
+                                   const ChunkScratch &cs, const float *lp, int ns_end, int nb_end, int nc_end,
+                                   int lane, unsigned long long &fl) {
+    const bool count = R.work != nullptr;
+    float cx[SPL], cy[SPL], cz[SPL], cr[SPL], A[SPL];
+    unsigned gbit[SPL];
+#pragma unroll
+    for (int m = 0; m < SPL; ++m) {
+        const int k = lane + kWarp * m;
+        if (k < R.S) {
+            const float4 s = t.sph[k];
+            const float3 p = xform_point(lp + 12 * t.slink[k], s.x, s.y, s.z);
+            cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
+            gbit[m] = 1u << t.sgrp[k];
+            w.cen[k] = make_float4(p.x, p.y, p.z, s.w);
+        } else {
+            cx[m] = kFar; cy[m] = kFar; cz[m] = kFar; cr[m] = 0.f;
+            gbit[m] = 0u;
+        }
+        A[m] = __fmaf_rn(cz[m], cz[m], __fmaf_rn(cy[m], cy[m], __fmaf_rn(cx[m], cx[m], -cr[m] * cr[m])));
+    }
+    if (lane < R.G) {
+        const float4 g = t.grp[lane];
+        const float3 c = xform_point(lp + 12 * t.glink[lane], g.x, g.y, g.z);
+        w.gb[lane] = make_float4(c.x, c.y, c.z, g.w);
+    }
+    __syncwarp();
+    bool hit = false;
+
+    // --- obstacle spheres (expanded form, see warp_collide) ---
+    const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
+    const float *snb = reinterpret_cast<const float *>(sx + E.ns);
+    for (int i = 0; i < ns_end; ++i) {
+        const unsigned o = cs.cl[i], cm = cs.cm[i];
+        const float4 b = sx[o];
+        const float nb = snb[o];
+#pragma unroll
+        for (int m = 0; m < SPL; ++m) {
+            const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
+            hit |= (cm & gbit[m]) && v > A[m];
+            if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlSphereX;
+        }
+    }
+    if (__any_sync(kFull, hit)) return true;
+
+    // --- cuboids ---
+    const float4 *bx = t.env + E.ns;
+    for (int i = ns_end; i < nb_end; ++i) {
+        const unsigned o = cs.cl[i], cm = cs.cm[i];
+        const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
+#pragma unroll
+        for (int m = 0; m < SPL; ++m) {
+            if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlCuboid;
+            if (cm & gbit[m]) {
+                const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
+                const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                hit |= sq3(dx, dy, dz) < cr[m] * cr[m];
+            }
+        }
+    }
+    if (__any_sync(kFull, hit)) return true;
+
+    // --- cylinders ---
+    const float4 *cyl = t.env + E.ns + 5 * E.nb;
+    for (int i = nb_end; i < nc_end; ++i) {
+        const unsigned o = cs.cl[i], cm = cs.cm[i];
+        const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
+#pragma unroll
+        for (int m = 0; m < SPL; ++m) {
+            if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlCylinder;
+            if (cm & gbit[m]) {
+                const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
+                const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
+                const float dz = fabsf(l.z) - pr.y;
+                const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                const float outside = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox)));
+                const float inside = fminf(fmaxf(dx, dz), 0.f);
+                hit |= cr[m] - (outside + inside) > 0.f;
+            }
+        }
+    }
+    if (__any_sync(kFull, hit)) return true;
+
+    // --- self collision: group pairs whose per-state bounding spheres overlap ---
+    for (int k0 = 0; k0 < R.NPL; k0 += kWarp) {
+        const int k = k0 + lane;
+        bool on = false;
+        int p0 = 0, p1 = 0;
+        if (k < R.NPL) {
+            const int4 lpr = t.lpair[k];
+            const float4 a = w.gb[lpr.x], b = w.gb[lpr.y];
+            const float rr = a.w + b.w;
+            on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
+            p0 = lpr.z;
+            p1 = lpr.w;
+        }
+        unsigned bal = __ballot_sync(kFull, on);
+        if (count) fl += (unsigned long long)min(kWarp, R.NPL - k0) * kFlGroupPair;
+        while (bal) {
+            const int j = __ffs(bal) - 1;
+            bal &= bal - 1u;
+            const int q0 = __shfl_sync(kFull, p0, j), q1 = __shfl_sync(kFull, p1, j);
+            if (count) fl += (unsigned long long)(q1 - q0) * kFlSelf;
+            for (int p = q0 + lane; p < q1; p += kWarp) {
+                const unsigned ij = __ldg(R.pairs + p);
+                const float thr = __ldg(R.thr + p);
+                const float4 a = w.cen[ij & 0xffffu], b = w.cen[ij >> 16];
+                hit |= sq3(a.x - b.x, a.y - b.y, a.z - b.z) < thr;
+            }
+            if (__any_sync(kFull, hit)) return true;
+        }
+    }
+    return false;
+}
+
+// States [s0, s1) of one edge (from f to t with per-state step d, n states in all).
+// Returns the first colliding state, or -1 (also when another warp already recorded
+// a hit below the state reached).
+template <int SPL, int K>
+__device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
+                                      const ChunkScratch &cs, int lane, const float *__restrict__ f,
+                                      const float *__restrict__ to, const float *__restrict__ d, int s0, int s1,
+                                      int n, const int *first_hit) {
+    const int ks = s1 - s0;
+    const bool count = R.work != nullptr;
+    unsigned long long fl = (unsigned long long)R.base_flops * ks;
+
+    // --- A: FK of every state, box of each group centre ---
+    const bool gl = lane < R.G;
+    const float4 g = gl ? t.grp[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int glk = gl ? t.glink[lane] : 0;
+    float lox = 3.0e38f, loy = 3.0e38f, loz = 3.0e38f, hix = -3.0e38f, hiy = -3.0e38f, hiz = -3.0e38f;
+    for (int k = 0; k < ks; ++k) {
+        const int s = s0 + k;
+        for (int j = lane; j < R.L; j += kWarp) w.q[j] = (s == n - 1) ? to[j] : __fmaf_rn(d[j], (float)s, f[j]);
+        __syncwarp();
+        WarpScratch wk = w;
+        wk.lp = cs.lpK + k * 12 * R.L;
+        warp_fk(t, R.L, wk, lane);
+        if (gl) {
+            const float3 c = xform_point(wk.lp + 12 * glk, g.x, g.y, g.z);
+            lox = fminf(lox, c.x); loy = fminf(loy, c.y); loz = fminf(loz, c.z);
+            hix = fmaxf(hix, c.x); hiy = fmaxf(hiy, c.y); hiz = fmaxf(hiz, c.z);
+        }
+    }
+
+    // --- B: swept group spheres ---
+    if (gl) {
+        const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
+        const float hx = 0.5f * (hix - lox), hy = 0.5f * (hiy - loy), hz = 0.5f * (hiz - loz);
+        const float rad = sqrtf(hx * hx + hy * hy + hz * hz) + g.w;
+        cs.sgb[lane] = make_float4(cx, cy, cz, rad);
+        cs.sgA[lane] = __fmaf_rn(cz, cz, __fmaf_rn(cy, cy, __fmaf_rn(cx, cx, -rad * rad)));
+    }
+    __syncwarp();
+
+    // --- C: broad phase of the chunk ---
+    int nc = 0;
+    const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
+    const float *snb = reinterpret_cast<const float *>(sx + E.ns);
+#pragma unroll 1
+    for (int o0 = 0; o0 < E.ns; o0 += kWarp) {
+        const int o = o0 + lane;
+        unsigned mask = 0u;
+        if (o < E.ns) {
+            const float4 b = sx[o];
+            const float nb = snb[o];
+#pragma unroll 2
+            for (int q = 0; q < R.G; ++q) {
+                const float4 gs = cs.sgb[q];
+                const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
+                if (v > cs.sgA[q]) mask |= 1u << q;
+            }
+        }
+        nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+        if (count) fl += (unsigned long long)min(kWarp, E.ns - o0) * R.G * kFlSphereX;
+    }
+    const int ns_end = nc;
+    const float4 *bx = t.env + E.ns;
+#pragma unroll 1
+    for (int o0 = 0; o0 < E.nb; o0 += kWarp) {
+        const int o = o0 + lane;
+        unsigned mask = 0u;
+        if (o < E.nb) {
+            const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
+            for (int q = 0; q < R.G; ++q) {
+                const float4 gs = cs.sgb[q];
+                const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                if (sq3(dx, dy, dz) < gs.w * gs.w) mask |= 1u << q;
+            }
+        }
+        nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+        if (count) fl += (unsigned long long)min(kWarp, E.nb - o0) * R.G * kFlCuboid;
+    }
+    const int nb_end = nc;
+    const float4 *cyl = t.env + E.ns + 5 * E.nb;
+#pragma unroll 1
+    for (int o0 = 0; o0 < E.nc; o0 += kWarp) {
+        const int o = o0 + lane;
+        unsigned mask = 0u;
+        if (o < E.nc) {
+            const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
+            for (int q = 0; q < R.G; ++q) {
+                const float4 gs = cs.sgb[q];
+                const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
+                const float dz = fabsf(l.z) - pr.y;
+                const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                const float sdf = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox))) + fminf(fmaxf(dx, dz), 0.f);
+                if (gs.w - sdf > 0.f) mask |= 1u << q;
+            }
+        }
+        nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+        if (count) fl += (unsigned long long)min(kWarp, E.nc - o0) * R.G * kFlCylinder;
+    }
+    __syncwarp();
+    const bool overflow = nc > kChunkCands;
+
+    // --- D: states in order ---
+    int found = -1;
+    for (int k = 0; k < ks; ++k) {
+        const int s = s0 + k;
+        if (k > 0) {
+            int known = 0;
+            if (lane == 0) known = *(volatile const int *)first_hit;
+            known = __shfl_sync(kFull, known, 0);
+            if (known < s) break;
+        }
+        const float *lp = cs.lpK + k * 12 * R.L;
+        bool hit;
+        if (overflow) {
+            WarpScratch wk = w;
+            wk.lp = const_cast<float *>(lp);
+            hit = warp_collide_culled<SPL>(t, R, E, wk, lane);
+        } else {
+            hit = chunk_state<SPL>(t, R, E, w, cs, lp, ns_end, nb_end, nc, lane, fl);
+        }
+        __syncwarp();
+        if (hit) {
+            found = s;
+            break;
+        }
+    }
+    if (count && lane == 0) {
+        atomicAdd(R.work, fl);
+        atomicAdd(R.work + 1, (unsigned long long)ks);
+    }
+    return found;
+}
+
+// One wave of edge validation by chunks: states [b0, b1) of every live edge, K per task,
+// chunk-major order so that lower chunks of an edge are examined first.
+template <int SPL, int K>
+__global__ void __launch_bounds__(kWarpsPerBlock *kWarp, 2)
+    k_edge_chunk(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
+                 const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
+                 const int *__restrict__ live, const int *__restrict__ live_count, int b0, int b1) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nwords = env_words(E.ns, E.nb, E.nc);
+    SmemTables t = carve_tables(smem, R, nwords);
+    stage_tables(R, E, t, nwords);
+    const int warp = threadIdx.x / kWarp;
+    unsigned char *wbase = smem + smem_tables_bytes(R, nwords);
+    WarpScratch w = carve_warp(wbase, R, warp);
+    ChunkScratch cs = carve_chunk(wbase + smem_warp_bytes(R) * kWarpsPerBlock, R, K, warp);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const long long count = *live_count;
+    const int nch = (b1 - b0 + K - 1) / K;
+    const long long tasks = count * (long long)nch;
+    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
+    for (long long task = blockIdx.x * (long long)kWarpsPerBlock + warp; task < tasks; task += nw) {
+        const int c = (int)(task / count);
+        const int e = live[task % count];
+        const int n = nsteps[e];
+        const int s0 = b0 + c * K;
+        if (s0 >= n) continue;
+        const int s1 = min(min(s0 + K, b1), n);
+        int known = 0;
+        if (lane == 0) known = *(volatile int *)(first_hit + e);
+        known = __shfl_sync(kFull, known, 0);
+        if (known < s0) continue;
+        const long long off = (long long)e * R.L;
+        const int h = warp_edge_chunk<SPL, K>(t, R, E, w, cs, lane, from + off, to + off, dir + off, s0, s1, n,
+                                              first_hit + e);
+        if (h >= 0 && lane == 0) atomicMin(first_hit + e, h);
+        __syncwarp();
+    }
+}
+
+#define GBMP_CHUNK_SWITCH(spl, K, ...)                                                       \
+    do {                                                                                     \
+        if ((K) == 8) {                                                                      \
+            constexpr int KK = 8;                                                            \
+            switch (spl) {                                                                   \
+            case 1: { constexpr int SPL = 1; __VA_ARGS__; } break;                           \
+            case 2: { constexpr int SPL = 2; __VA_ARGS__; } break;                           \
+            case 3: { constexpr int SPL = 3; __VA_ARGS__; } break;                           \
+            case 4: { constexpr int SPL = 4; __VA_ARGS__; } break;                           \
+            case 5: { constexpr int SPL = 5; __VA_ARGS__; } break;                           \
+            case 6: { constexpr int SPL = 6; __VA_ARGS__; } break;                           \
+            case 7: { constexpr int SPL = 7; __VA_ARGS__; } break;                           \
+            default: { constexpr int SPL = 8; __VA_ARGS__; } break;                          \
+            }                                                                                \
+        } else {                                                                             \
+            constexpr int KK = 4;                                                            \
+            switch (spl) {                                                                   \
+            case 1: { constexpr int SPL = 1; __VA_ARGS__; } break;                           \
+            case 2: { constexpr int SPL = 2; __VA_ARGS__; } break;                           \
+            case 3: { constexpr int SPL = 3; __VA_ARGS__; } break;                           \
+            case 4: { constexpr int SPL = 4; __VA_ARGS__; } break;                           \
+            case 5: { constexpr int SPL = 5; __VA_ARGS__; } break;                           \
+            case 6: { constexpr int SPL = 6; __VA_ARGS__; } break;                           \
+            case 7: { constexpr int SPL = 7; __VA_ARGS__; } break;                           \
+            default: { constexpr int SPL = 8; __VA_ARGS__; } break;                          \
+            }                                                                                \
+        }                                                                                    \
+    } while (0)
+
+int edge_chunk_states(const DevRobot &R) {
+    if (!R.cull) return 0;
+    const char *env = getenv("GBMP_EDGE_CHUNK");
+    if (env && *env) {
+        const int k = atoi(env);
+        if (k <= 1) return 0;
+        return k >= 8 ? 8 : 4;
+    }
+    return R.L <= 16 ? 8 : 4;
+}
+
+gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid) {
+    *smem = smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) +
+            (smem_warp_bytes(R) + smem_chunk_bytes(R, K)) * kWarpsPerBlock;
+    gbmp_status st = GBMP_OK;
+    GBMP_CHUNK_SWITCH(R.spl, K, {
+        const void *fn = (const void *)k_edge_chunk<SPL, KK>;
+        static thread_local bool configured = false;
+        if (!configured) {
+            GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                           cudaSharedmemCarveoutMaxShared));
+            configured = true;
+        }
+        int per_sm = 0;
+        GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kWarpsPerBlock * kWarp, *smem));
+        if (per_sm < 1) {
+            set_error("chunked edge kernel does not fit on an SM (%zu bytes of shared memory)", *smem);
+            st = GBMP_ERR_CAPACITY;
+        }
+        *grid = per_sm * num_sms;
+    });
+    return st;
+}
+
+gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int grid, size_t smem, cudaStream_t s,
+                              const float *from, const float *to, const int *nsteps, const float *dir,
+                              int *first_hit, const int *live, const int *live_count, int b0, int b1) {
+    GBMP_CHUNK_SWITCH(R.spl, K, {
+        k_edge_chunk<SPL, KK><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(R, E, from, to, nsteps, dir, first_hit,
+                                                                          live, live_count, b0, b1);
+    });
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
+}  // namespace gbmp

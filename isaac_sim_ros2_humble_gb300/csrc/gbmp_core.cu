@@ -722,13 +722,24 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     const DevEnv Ev = env->dev();
     DevRobot D = r->dev;
     D.work = work_counter();
-    const size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
+    size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
     int grid = 0;
     const bool cull = r->dev.cull != 0;
-    GBMP_SPL_SWITCH(r->dev.spl, {
-        st = cull ? persistent_grid(k_edge_wave<SPL, true>, smem, r->num_sms, &grid)
-                  : persistent_grid(k_edge_wave<SPL, false>, smem, r->num_sms, &grid);
-    });
+    int K = edge_chunk_states(D);
+    if (K) {
+        st = edge_chunk_prepare(D, Ev, r->num_sms, K, &smem, &grid);
+        if (st == GBMP_ERR_CAPACITY) {   // chunk scratch does not fit next to a large scene
+            K = 0;
+            st = GBMP_OK;
+            smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
+        }
+    }
+    if (!K) {
+        GBMP_SPL_SWITCH(r->dev.spl, {
+            st = cull ? persistent_grid(k_edge_wave<SPL, true>, smem, r->num_sms, &grid)
+                      : persistent_grid(k_edge_wave<SPL, false>, smem, r->num_sms, &grid);
+        });
+    }
     if (st) return st;
     int b0 = 0, wave = 0;
     int *live_in = liveA, *live_out = liveB;
@@ -737,14 +748,20 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
         int *cnt_in = ctr + 1 + wave, *cnt_out = ctr + 2 + wave;
         {
             ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
-            GBMP_SPL_SWITCH(r->dev.spl, {
-                if (cull)
-                    k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                        D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
-                else
-                    k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                        D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
-            });
+            if (K) {
+                st = edge_chunk_launch(D, Ev, K, grid, smem, s, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0,
+                                       b1);
+                if (st) return st;
+            } else {
+                GBMP_SPL_SWITCH(r->dev.spl, {
+                    if (cull)
+                        k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                            D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+                    else
+                        k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                            D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
+                });
+            }
         }
         GBMP_CUDA(cudaGetLastError());
         if (b1 < n_max) {
