@@ -3,9 +3,10 @@
 // The interpolated states of one edge lie millimetres apart, so the obstacles near one
 // state are the obstacles near its neighbours.  A warp takes K consecutive states of
 // one edge (a chunk) and
-//   A. runs the FK of each state, keeping the link poses in shared memory, and bounds
-//      the centre of every sphere group (a link's bounding sphere) over the chunk by an
-//      axis-aligned box;
+//   A. runs the FK of all K states together (the K link chains advance in lock step,
+//      each lane owning (state, pose element) slots), keeping the link poses in shared
+//      memory, and bounds the centre of every sphere group (a link's bounding sphere)
+//      over the chunk by an axis-aligned box;
 //   B. turns each box into a swept group sphere: centre = box centre, radius = half the
 //      box diagonal + the group radius (which already carries kBroadMargin);
 //   C. runs the broad phase ONCE for the chunk: every obstacle against the swept group
@@ -23,30 +24,89 @@
 namespace gbmp {
 
 constexpr int kChunkCands = 64;
+constexpr int kChunkPairs = 64;
 
 struct ChunkScratch {
     float *lpK;       // link poses of the chunk's states [K][L*12]
+    float *locK;      // joint-local transforms of the chunk's states [K][L*12]
     float4 *sgb;      // swept group spheres (x, y, z, R) [kMaxGroups]
     float *sgA;       // |c|^2 - R^2 of each swept sphere
     unsigned *cl;     // candidate obstacle indices
     unsigned *cm;     // their group masks
+    int *pl;          // enabled group pairs whose swept spheres overlap (lpair indices)
 };
 
+// Per-warp shared memory of the chunk kernel: the chunk tables above plus the parts of
+// WarpScratch the per-state tests use (sphere centres, group spheres, candidates).
 __host__ __device__ inline size_t smem_chunk_bytes(const DevRobot &R, int K) {
-    return align16(sizeof(float) * 12 * R.L * K) + align16(sizeof(float4) * kMaxGroups) +
-           align16(sizeof(float) * kMaxGroups) + 2 * align16(sizeof(unsigned) * kChunkCands);
+    return 2 * align16(sizeof(float) * 12 * R.L * K) + align16(sizeof(float4) * kMaxGroups) +
+           align16(sizeof(float) * kMaxGroups) + 2 * align16(sizeof(unsigned) * kChunkCands) +
+           align16(sizeof(int) * kChunkPairs) + align16(sizeof(float4) * R.S) + align16(sizeof(float4) * kMaxGroups) + align16(sizeof(float) * kMaxGroups) +
+           2 * align16(sizeof(int) * kWarp);
 }
 
-__device__ inline ChunkScratch carve_chunk(unsigned char *base, const DevRobot &R, int K, int warp) {
+__device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K, int warp, ChunkScratch &c,
+                                   WarpScratch &w) {
     unsigned char *p = base + smem_chunk_bytes(R, K) * warp;
-    ChunkScratch c;
     size_t off = 0;
     c.lpK = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L * K);
+    c.locK = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L * K);
     c.sgb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * kMaxGroups);
     c.sgA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * kMaxGroups);
     c.cl = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
-    c.cm = reinterpret_cast<unsigned *>(p + off);
-    return c;
+    c.cm = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
+    c.pl = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * kChunkPairs);
+    w.lp = nullptr;
+    w.loc = nullptr;
+    w.q = nullptr;
+    w.cen = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.S);
+    w.gb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * kMaxGroups);
+    w.gA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * kMaxGroups);
+    w.cand = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * kWarp);
+    w.cmask = reinterpret_cast<unsigned *>(p + off);
+}
+
+// FK of the chunk's ks states (state s = s0 + k from f towards t by d, the last state of
+// the edge exactly t), all chains advancing together: first the ks x L joint-local
+// transforms spread over the lanes, then link by link the ks x 12 pose elements, slot
+// j of a lane being element (lane + 32 j) of the flattened (state, element) list.  The
+// arithmetic is warp_fk's (joint_local, mul_elem), so poses are bit-identical.
+template <int K>
+__device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const float *__restrict__ f,
+                                     const float *__restrict__ to, const float *__restrict__ d, int s0, int n,
+                                     float *locK, float *lpK, int lane) {
+    for (int idx = lane; idx < ks * L; idx += kWarp) {
+        const int k = idx / L, i = idx - k * L;
+        const int s = s0 + k;
+        const float qv = (s == n - 1) ? to[i] : __fmaf_rn(d[i], (float)s, f[i]);
+        joint_local(t, i, qv, locK + 12 * idx);
+    }
+    constexpr int J = (K * 12 + kWarp - 1) / kWarp;
+    int kk[J], ee[J];
+    bool on[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+        const int idx = lane + kWarp * j;
+        on[j] = idx < ks * 12;
+        kk[j] = idx / 12;
+        ee[j] = idx - 12 * kk[j];
+        if (on[j]) lpK[kk[j] * 12 * L + ee[j]] = (ee[j] % 5 == 0) ? 1.f : 0.f;
+    }
+    __syncwarp();
+    for (int i = 1; i < L; ++i) {
+        const int ty = t.type[i], par = t.parent[i];
+        const bool known = ty == 1 || ty == 2 || ty == 5;
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            if (on[j]) {
+                float *base = lpK + kk[j] * 12 * L;
+                const int r = ee[j] >> 2, c = ee[j] & 3;
+                base[12 * i + ee[j]] = known ? mul_elem(base + 12 * par, locK + 12 * (kk[j] * L + i), r, c)
+                                             : ((r == c) ? 1.f : 0.f);
+            }
+        }
+        __syncwarp();
+    }
 }
 
 // Append this lane's obstacle (when mask != 0) to the candidate list; returns the new
@@ -62,18 +122,22 @@ __device__ __forceinline__ int push_cand(const ChunkScratch &cs, int n, unsigned
 
 // Exact tests of one state (link poses lp) against the chunk's candidates, then its
 // self-collision pairs.  ns_end / nb_end / nc_end delimit the sphere / cuboid /
-// cylinder candidates.
+// cylinder candidates; `need` holds the groups any candidate or listed group pair
+// involves (spheres of other groups cannot collide in this chunk and are not placed);
+// npr group pairs are listed in cs.pl unless pairs_overflow.
 template <int SPL>
 __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                    const ChunkScratch &cs, const float *lp, int ns_end, int nb_end, int nc_end,
-                                   int lane, unsigned long long &fl) {
+                                   unsigned need, int npr, bool pairs_overflow, int lane, unsigned long long &fl) {
     const bool count = R.work != nullptr;
     float cx[SPL], cy[SPL], cz[SPL], cr[SPL], A[SPL];
     unsigned gbit[SPL];
 #pragma unroll
     for (int m = 0; m < SPL; ++m) {
         const int k = lane + kWarp * m;
-        if (k < R.S) {
+        const bool place = k < R.S && ((need >> t.sgrp[k]) & 1u);
+        if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, place)) * 24;
+        if (place) {
             const float4 s = t.sph[k];
             const float3 p = xform_point(lp + 12 * t.slink[k], s.x, s.y, s.z);
             cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
@@ -85,7 +149,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
         }
         A[m] = __fmaf_rn(cz[m], cz[m], __fmaf_rn(cy[m], cy[m], __fmaf_rn(cx[m], cx[m], -cr[m] * cr[m])));
     }
-    if (lane < R.G) {
+    if (lane < R.G && ((need >> lane) & 1u)) {
         const float4 g = t.grp[lane];
         const float3 c = xform_point(lp + 12 * t.glink[lane], g.x, g.y, g.z);
         w.gb[lane] = make_float4(c.x, c.y, c.z, g.w);
@@ -149,13 +213,14 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
     }
     if (__any_sync(kFull, hit)) return true;
 
-    // --- self collision: group pairs whose per-state bounding spheres overlap ---
-    for (int k0 = 0; k0 < R.NPL; k0 += kWarp) {
+    // --- self collision: listed group pairs whose per-state bounding spheres overlap ---
+    const int nlist = pairs_overflow ? R.NPL : npr;
+    for (int k0 = 0; k0 < nlist; k0 += kWarp) {
         const int k = k0 + lane;
         bool on = false;
         int p0 = 0, p1 = 0;
-        if (k < R.NPL) {
-            const int4 lpr = t.lpair[k];
+        if (k < nlist) {
+            const int4 lpr = t.lpair[pairs_overflow ? k : cs.pl[k]];
             const float4 a = w.gb[lpr.x], b = w.gb[lpr.y];
             const float rr = a.w + b.w;
             on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
@@ -163,7 +228,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             p1 = lpr.w;
         }
         unsigned bal = __ballot_sync(kFull, on);
-        if (count) fl += (unsigned long long)min(kWarp, R.NPL - k0) * kFlGroupPair;
+        if (count) fl += (unsigned long long)min(kWarp, nlist - k0) * kFlGroupPair;
         while (bal) {
             const int j = __ffs(bal) - 1;
             bal &= bal - 1u;
@@ -191,22 +256,19 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
                                       int n, const int *first_hit) {
     const int ks = s1 - s0;
     const bool count = R.work != nullptr;
-    unsigned long long fl = (unsigned long long)R.base_flops * ks;
+    // FK and the group-centre transforms of every state; sphere placements are counted
+    // where they happen
+    unsigned long long fl = (unsigned long long)(R.base_flops - 24LL * R.S) * ks;
 
     // --- A: FK of every state, box of each group centre ---
     const bool gl = lane < R.G;
     const float4 g = gl ? t.grp[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int glk = gl ? t.glink[lane] : 0;
     float lox = 3.0e38f, loy = 3.0e38f, loz = 3.0e38f, hix = -3.0e38f, hiy = -3.0e38f, hiz = -3.0e38f;
+    warp_fk_chunk<K>(t, R.L, ks, f, to, d, s0, n, cs.locK, cs.lpK, lane);
     for (int k = 0; k < ks; ++k) {
-        const int s = s0 + k;
-        for (int j = lane; j < R.L; j += kWarp) w.q[j] = (s == n - 1) ? to[j] : __fmaf_rn(d[j], (float)s, f[j]);
-        __syncwarp();
-        WarpScratch wk = w;
-        wk.lp = cs.lpK + k * 12 * R.L;
-        warp_fk(t, R.L, wk, lane);
         if (gl) {
-            const float3 c = xform_point(wk.lp + 12 * glk, g.x, g.y, g.z);
+            const float3 c = xform_point(cs.lpK + k * 12 * R.L + 12 * glk, g.x, g.y, g.z);
             lox = fminf(lox, c.x); loy = fminf(loy, c.y); loz = fminf(loz, c.z);
             hix = fmaxf(hix, c.x); hiy = fmaxf(hiy, c.y); hiz = fmaxf(hiz, c.z);
         }
@@ -224,6 +286,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
 
     // --- C: broad phase of the chunk ---
     int nc = 0;
+    unsigned need = 0u;
     const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
     const float *snb = reinterpret_cast<const float *>(sx + E.ns);
 #pragma unroll 1
@@ -241,6 +304,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
             }
         }
         nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+        need |= mask;
         if (count) fl += (unsigned long long)min(kWarp, E.ns - o0) * R.G * kFlSphereX;
     }
     const int ns_end = nc;
@@ -261,6 +325,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
             }
         }
         nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+        need |= mask;
         if (count) fl += (unsigned long long)min(kWarp, E.nb - o0) * R.G * kFlCuboid;
     }
     const int nb_end = nc;
@@ -282,14 +347,38 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
             }
         }
         nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+        need |= mask;
         if (count) fl += (unsigned long long)min(kWarp, E.nc - o0) * R.G * kFlCylinder;
     }
+    // enabled group pairs whose swept spheres overlap
+    int npr = 0;
+    for (int k0 = 0; k0 < R.NPL; k0 += kWarp) {
+        const int k = k0 + lane;
+        bool on = false;
+        if (k < R.NPL) {
+            const int4 lpr = t.lpair[k];
+            const float4 a = cs.sgb[lpr.x], b = cs.sgb[lpr.y];
+            const float rr = a.w + b.w;
+            on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
+            if (on) need |= (1u << lpr.x) | (1u << lpr.y);
+        }
+        const unsigned bal = __ballot_sync(kFull, on);
+        if (on) {
+            const int pos = npr + __popc(bal & ((1u << lane) - 1u));
+            if (pos < kChunkPairs) cs.pl[pos] = k;
+        }
+        npr += __popc(bal);
+        if (count) fl += (unsigned long long)min(kWarp, R.NPL - k0) * kFlGroupPair;
+    }
+    need = __reduce_or_sync(kFull, need);
     __syncwarp();
     const bool overflow = nc > kChunkCands;
+    const bool pairs_overflow = npr > kChunkPairs;
 
     // --- D: states in order ---
     int found = -1;
-    for (int k = 0; k < ks; ++k) {
+    const int kend = (need == 0u && !overflow) ? 0 : ks;   // nothing near any state: all free
+    for (int k = 0; k < kend; ++k) {
         const int s = s0 + k;
         if (k > 0) {
             int known = 0;
@@ -304,7 +393,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
             wk.lp = const_cast<float *>(lp);
             hit = warp_collide_culled<SPL>(t, R, E, wk, lane);
         } else {
-            hit = chunk_state<SPL>(t, R, E, w, cs, lp, ns_end, nb_end, nc, lane, fl);
+            hit = chunk_state<SPL>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, lane, fl);
         }
         __syncwarp();
         if (hit) {
@@ -331,9 +420,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, 2)
     SmemTables t = carve_tables(smem, R, nwords);
     stage_tables(R, E, t, nwords);
     const int warp = threadIdx.x / kWarp;
-    unsigned char *wbase = smem + smem_tables_bytes(R, nwords);
-    WarpScratch w = carve_warp(wbase, R, warp);
-    ChunkScratch cs = carve_chunk(wbase + smem_warp_bytes(R) * kWarpsPerBlock, R, K, warp);
+    WarpScratch w;
+    ChunkScratch cs;
+    carve_chunk(smem + smem_tables_bytes(R, nwords), R, K, warp, cs, w);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long count = *live_count;
@@ -400,8 +489,7 @@ int edge_chunk_states(const DevRobot &R) {
 }
 
 gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid) {
-    *smem = smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) +
-            (smem_warp_bytes(R) + smem_chunk_bytes(R, K)) * kWarpsPerBlock;
+    *smem = smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) + smem_chunk_bytes(R, K) * kWarpsPerBlock;
     gbmp_status st = GBMP_OK;
     GBMP_CHUNK_SWITCH(R.spl, K, {
         const void *fn = (const void *)k_edge_chunk<SPL, KK>;
