@@ -594,7 +594,8 @@ def main():
         achieved = exec_flops / wave_s_per_step / 1e12 if wave_s_per_step > 0 else None
         effective = units * flops_state / wave_s_per_step / 1e12 if wave_s_per_step > 0 else None
         traffic = None
-        tp = os.path.join(ROOT, "profiles", "edge_wave_traffic.json")
+        kernel = "k_edge_wave" if os.environ.get("GBMP_EDGE_CHUNK", "") == "1" else "k_edge_chunk"
+        tp = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
         if os.path.exists(tp):
             try:
                 traffic = json.load(open(tp)).get("bytes_per_launch")
@@ -615,18 +616,18 @@ def main():
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * n * L * 4),
                     "d2h_bytes_per_step": int(n * (1 + 4 + 4)), "ms_per_step": 1e3 * e2e_s / args.steps},
-            "roofline": {"bound": "fp32", "kernel": "k_edge_wave", "achieved": achieved, "peak": fp32_peak,
+            "roofline": {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": fp32_peak,
                          "unit": "TFLOP/s", "frac": (achieved / fp32_peak) if achieved and fp32_peak else None,
                          "traffic": traffic,
                          "peak_source": "measured FP32 FMA throughput (gbmp_measure_fp32_peak) on this GPU; "
                                         "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
                          "nominal_peak": roofline.nominal_fp32_tflops(),
-                         "achieved_is": "flops executed by the broad-phase kernel (counted in-kernel in an "
-                                        "untimed step) / k_edge_wave time",
+                         "achieved_is": f"flops executed by {kernel} (counted in-kernel in an untimed step) / "
+                                        f"{kernel} time",
                          "executed_flops_per_step": exec_flops, "states_evaluated_per_step": exec_states,
                          "effective": effective, "effective_frac": (effective / fp32_peak) if effective else None,
                          "effective_is": "reference-equivalent work (full pair tests of every needed state, "
-                                         "flops_per_state x units_per_step) / k_edge_wave time",
+                                         f"flops_per_state x units_per_step) / {kernel} time",
                          "flops_per_state": flops_state, "units_per_step": units,
                          "kernel_ms_per_step": wave_ms / args.steps,
                          "kernel_launches_per_step": wave_launches / args.steps},

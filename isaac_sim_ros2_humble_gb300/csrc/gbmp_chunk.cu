@@ -67,19 +67,21 @@ __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K
 }
 
 // FK of the chunk's ks states (state s = s0 + k from f towards t by d, the last state of
-// the edge exactly t), all chains advancing together: first the ks x L joint-local
-// transforms spread over the lanes, then link by link the ks x 12 pose elements, slot
+// the edge exactly t), all chains advancing together: first the ks x (L - 1) joint-local
+// transforms of links 1.. spread over the lanes link-major (the lanes of one pass mostly
+// share a joint type, so the type branches diverge little; link 0 is the identity and
+// needs none), then link by link the ks x 12 pose elements, slot
 // j of a lane being element (lane + 32 j) of the flattened (state, element) list.  The
 // arithmetic is warp_fk's (joint_local, mul_elem), so poses are bit-identical.
 template <int K>
 __device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const float *__restrict__ f,
                                      const float *__restrict__ to, const float *__restrict__ d, int s0, int n,
                                      float *locK, float *lpK, int lane) {
-    for (int idx = lane; idx < ks * L; idx += kWarp) {
-        const int k = idx / L, i = idx - k * L;
+    for (int idx = lane; idx < ks * (L - 1); idx += kWarp) {
+        const int i = 1 + idx / ks, k = idx - (i - 1) * ks;
         const int s = s0 + k;
         const float qv = (s == n - 1) ? to[i] : __fmaf_rn(d[i], (float)s, f[i]);
-        joint_local(t, i, qv, locK + 12 * idx);
+        joint_local(t, i, qv, locK + 12 * (k * L + i));
     }
     constexpr int J = (K * 12 + kWarp - 1) / kWarp;
     int kk[J], ee[J];
@@ -246,6 +248,15 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
     return false;
 }
 
+// Per-state routine for a chunk whose candidates overflow the list; out of line, since
+// it runs rarely and inlining it would crowd the instruction cache of the common path.
+template <int SPL>
+__device__ __noinline__ bool chunk_fallback(const SmemTables &t, const DevRobot &R, const DevEnv &E, WarpScratch w,
+                                            const float *lp, int lane) {
+    w.lp = const_cast<float *>(lp);
+    return warp_collide_culled<SPL>(t, R, E, w, lane);
+}
+
 // States [s0, s1) of one edge (from f to t with per-state step d, n states in all).
 // Returns the first colliding state, or -1 (also when another warp already recorded
 // a hit below the state reached).
@@ -389,9 +400,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
         const float *lp = cs.lpK + k * 12 * R.L;
         bool hit;
         if (overflow) {
-            WarpScratch wk = w;
-            wk.lp = const_cast<float *>(lp);
-            hit = warp_collide_culled<SPL>(t, R, E, wk, lane);
+            hit = chunk_fallback<SPL>(t, R, E, w, lp, lane);
         } else {
             hit = chunk_state<SPL>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, lane, fl);
         }
