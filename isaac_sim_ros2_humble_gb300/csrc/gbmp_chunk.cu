@@ -9,9 +9,11 @@
 //      over the chunk by an axis-aligned box;
 //   B. turns each box into a swept group sphere: centre = box centre, radius = half the
 //      box diagonal + the group radius (which already carries kBroadMargin);
-//   C. runs the broad phase ONCE for the chunk: every obstacle against the swept group
-//      spheres, keeping the obstacles that touch any of them (with the group mask) in a
-//      per-warp candidate list;
+//   C. runs the broad phase ONCE for the chunk: the bounding sphere of every run of 32
+//      obstacles (scenes store obstacles in spatially compact runs) against the swept
+//      group spheres, then the obstacles of the runs some group touches against those
+//      groups, keeping the obstacles that touch any (with the group mask) in a per-warp
+//      candidate list;
 //   D. walks the states in order and tests each state's robot spheres exactly against
 //      the candidates only (the same narrow tests as warp_collide_culled), then its
 //      self-collision pairs, stopping at the first colliding state.
@@ -120,6 +122,23 @@ __device__ __forceinline__ int push_cand(const ChunkScratch &cs, int n, unsigned
         if (pos < kChunkCands) { cs.cl[pos] = idx; cs.cm[pos] = mask; }
     }
     return n + __popc(bal);
+}
+
+// Groups (bit q) whose swept sphere touches the bounding sphere of run c0 + lane of an
+// obstacle type with nruns runs; 0 for lanes past the last run.
+__device__ __forceinline__ unsigned run_groups(const float4 *runs, int nruns, int c0, const ChunkScratch &cs, int G,
+                                               int lane) {
+    const int c = c0 + lane;
+    unsigned gm = 0u;
+    if (c < nruns) {
+        const float4 b = runs[c];
+        for (int q = 0; q < G; ++q) {
+            const float4 gs = cs.sgb[q];
+            const float rr = gs.w + b.w;
+            if (sq3(gs.x - b.x, gs.y - b.y, gs.z - b.z) < rr * rr) gm |= 1u << q;
+        }
+    }
+    return gm;
 }
 
 // Exact tests of one state (link poses lp) against the chunk's candidates, then its
@@ -295,71 +314,106 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     }
     __syncwarp();
 
-    // --- C: broad phase of the chunk ---
+    // --- C: broad phase of the chunk, run spheres first ---
+    // Lane j tests run c0 + j's bounding sphere against every swept group sphere; only
+    // runs some group touches are visited, and their obstacles are tested only against
+    // the groups that touched the run.
     int nc = 0;
     unsigned need = 0u;
+    const float4 *runs_s = t.env + env_cluster_base(E.ns, E.nb, E.nc);
     const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
     const float *snb = reinterpret_cast<const float *>(sx + E.ns);
+    const int nrs = env_clusters(E.ns);
 #pragma unroll 1
-    for (int o0 = 0; o0 < E.ns; o0 += kWarp) {
-        const int o = o0 + lane;
-        unsigned mask = 0u;
-        if (o < E.ns) {
-            const float4 b = sx[o];
-            const float nb = snb[o];
-#pragma unroll 2
-            for (int q = 0; q < R.G; ++q) {
-                const float4 gs = cs.sgb[q];
-                const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
-                if (v > cs.sgA[q]) mask |= 1u << q;
+    for (int c0 = 0; c0 < nrs; c0 += kWarp) {
+        const unsigned gmc = run_groups(runs_s, nrs, c0, cs, R.G, lane);
+        unsigned runs = __ballot_sync(kFull, gmc != 0u);
+        if (count) fl += (unsigned long long)min(kWarp, nrs - c0) * R.G * kFlGroupPair;
+        while (runs) {
+            const int j = __ffs(runs) - 1;
+            runs &= runs - 1u;
+            const unsigned gm = __shfl_sync(kFull, gmc, j);
+            const int o = (c0 + j) * kWarp + lane;
+            unsigned mask = 0u;
+            if (o < E.ns) {
+                const float4 b = sx[o];
+                const float nb = snb[o];
+                for (unsigned m = gm; m; m &= m - 1u) {
+                    const int q = __ffs(m) - 1;
+                    const float4 gs = cs.sgb[q];
+                    const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
+                    if (v > cs.sgA[q]) mask |= 1u << q;
+                }
             }
+            nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+            need |= mask;
+            if (count) fl += (unsigned long long)min(kWarp, E.ns - (c0 + j) * kWarp) * __popc(gm) * kFlSphereX;
         }
-        nc = push_cand(cs, nc, (unsigned)o, mask, lane);
-        need |= mask;
-        if (count) fl += (unsigned long long)min(kWarp, E.ns - o0) * R.G * kFlSphereX;
     }
     const int ns_end = nc;
     const float4 *bx = t.env + E.ns;
+    const int nrb = env_clusters(E.nb);
+    const float4 *runs_b = runs_s + nrs;
 #pragma unroll 1
-    for (int o0 = 0; o0 < E.nb; o0 += kWarp) {
-        const int o = o0 + lane;
-        unsigned mask = 0u;
-        if (o < E.nb) {
-            const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
-            for (int q = 0; q < R.G; ++q) {
-                const float4 gs = cs.sgb[q];
-                const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
-                const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
-                const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
-                const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
-                if (sq3(dx, dy, dz) < gs.w * gs.w) mask |= 1u << q;
+    for (int c0 = 0; c0 < nrb; c0 += kWarp) {
+        const unsigned gmc = run_groups(runs_b, nrb, c0, cs, R.G, lane);
+        unsigned runs = __ballot_sync(kFull, gmc != 0u);
+        if (count) fl += (unsigned long long)min(kWarp, nrb - c0) * R.G * kFlGroupPair;
+        while (runs) {
+            const int j = __ffs(runs) - 1;
+            runs &= runs - 1u;
+            const unsigned gm = __shfl_sync(kFull, gmc, j);
+            const int o = (c0 + j) * kWarp + lane;
+            unsigned mask = 0u;
+            if (o < E.nb) {
+                const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
+                for (unsigned m = gm; m; m &= m - 1u) {
+                    const int q = __ffs(m) - 1;
+                    const float4 gs = cs.sgb[q];
+                    const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                    const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                    const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                    const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                    if (sq3(dx, dy, dz) < gs.w * gs.w) mask |= 1u << q;
+                }
             }
+            nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+            need |= mask;
+            if (count) fl += (unsigned long long)min(kWarp, E.nb - (c0 + j) * kWarp) * __popc(gm) * kFlCuboid;
         }
-        nc = push_cand(cs, nc, (unsigned)o, mask, lane);
-        need |= mask;
-        if (count) fl += (unsigned long long)min(kWarp, E.nb - o0) * R.G * kFlCuboid;
     }
     const int nb_end = nc;
     const float4 *cyl = t.env + E.ns + 5 * E.nb;
+    const int nrc = env_clusters(E.nc);
+    const float4 *runs_c = runs_b + nrb;
 #pragma unroll 1
-    for (int o0 = 0; o0 < E.nc; o0 += kWarp) {
-        const int o = o0 + lane;
-        unsigned mask = 0u;
-        if (o < E.nc) {
-            const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
-            for (int q = 0; q < R.G; ++q) {
-                const float4 gs = cs.sgb[q];
-                const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
-                const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
-                const float dz = fabsf(l.z) - pr.y;
-                const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
-                const float sdf = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox))) + fminf(fmaxf(dx, dz), 0.f);
-                if (gs.w - sdf > 0.f) mask |= 1u << q;
+    for (int c0 = 0; c0 < nrc; c0 += kWarp) {
+        const unsigned gmc = run_groups(runs_c, nrc, c0, cs, R.G, lane);
+        unsigned runs = __ballot_sync(kFull, gmc != 0u);
+        if (count) fl += (unsigned long long)min(kWarp, nrc - c0) * R.G * kFlGroupPair;
+        while (runs) {
+            const int j = __ffs(runs) - 1;
+            runs &= runs - 1u;
+            const unsigned gm = __shfl_sync(kFull, gmc, j);
+            const int o = (c0 + j) * kWarp + lane;
+            unsigned mask = 0u;
+            if (o < E.nc) {
+                const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
+                for (unsigned m = gm; m; m &= m - 1u) {
+                    const int q = __ffs(m) - 1;
+                    const float4 gs = cs.sgb[q];
+                    const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                    const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
+                    const float dz = fabsf(l.z) - pr.y;
+                    const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                    const float sdf = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox))) + fminf(fmaxf(dx, dz), 0.f);
+                    if (gs.w - sdf > 0.f) mask |= 1u << q;
+                }
             }
+            nc = push_cand(cs, nc, (unsigned)o, mask, lane);
+            need |= mask;
+            if (count) fl += (unsigned long long)min(kWarp, E.nc - (c0 + j) * kWarp) * __popc(gm) * kFlCylinder;
         }
-        nc = push_cand(cs, nc, (unsigned)o, mask, lane);
-        need |= mask;
-        if (count) fl += (unsigned long long)min(kWarp, E.nc - o0) * R.G * kFlCylinder;
     }
     // enabled group pairs whose swept spheres overlap
     int npr = 0;

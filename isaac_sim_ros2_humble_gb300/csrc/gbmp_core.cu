@@ -552,6 +552,54 @@ gbmp_status gbmp_robot_use_codegen(gbmp_robot r, int32_t enable) {
     return GBMP_OK;
 }
 
+// Obstacle order of a scene: a k-d split of the bounding-sphere centres (longest axis,
+// left part a multiple of 32 points) so that every run of 32 consecutive obstacles of a
+// type is spatially compact.  Ties break on the input index, so the order is the same
+// on every host.
+static void cluster_order(const std::vector<double> &c, std::vector<int> &idx, int lo, int hi) {
+    if (hi - lo <= 32) return;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int k = lo; k < hi; ++k)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = std::min(mn[a], c[3 * idx[k] + a]);
+            mx[a] = std::max(mx[a], c[3 * idx[k] + a]);
+        }
+    int ax = 0;
+    for (int a = 1; a < 3; ++a)
+        if (mx[a] - mn[a] > mx[ax] - mn[ax]) ax = a;
+    const int mid = lo + ((hi - lo + 63) / 64) * 32;
+    std::nth_element(idx.begin() + lo, idx.begin() + mid, idx.begin() + hi, [&](int a, int b) {
+        const double va = c[3 * a + ax], vb = c[3 * b + ax];
+        return va < vb || (va == vb && a < b);
+    });
+    cluster_order(c, idx, lo, mid);
+    cluster_order(c, idx, mid, hi);
+}
+
+// Bounding sphere of each run of 32 obstacles (bounding-sphere centres c and radii r
+// of the obstacles, idx in run order), rounded outwards.
+static void cluster_spheres(const std::vector<double> &c, const std::vector<double> &r, const std::vector<int> &idx,
+                            float4 *out) {
+    const int n = (int)idx.size();
+    for (int b = 0; b * 32 < n; ++b) {
+        const int lo = 32 * b, hi = std::min(n, lo + 32);
+        double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+        for (int k = lo; k < hi; ++k)
+            for (int a = 0; a < 3; ++a) {
+                mn[a] = std::min(mn[a], c[3 * idx[k] + a]);
+                mx[a] = std::max(mx[a], c[3 * idx[k] + a]);
+            }
+        const double cx = 0.5 * (mn[0] + mx[0]), cy = 0.5 * (mn[1] + mx[1]), cz = 0.5 * (mn[2] + mx[2]);
+        double rad = 0.0;
+        for (int k = lo; k < hi; ++k) {
+            const int i = idx[k];
+            const double dx = c[3 * i] - cx, dy = c[3 * i + 1] - cy, dz = c[3 * i + 2] - cz;
+            rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz) + r[i]);
+        }
+        out[b] = make_float4((float)cx, (float)cy, (float)cz, (float)(rad * (1.0 + 1e-6) + 1e-5));
+    }
+}
+
 gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_t nb, const float *bp,
                             const float *brot, const float *bmin, const float *bmax, int32_t nc, const float *cp,
                             const float *crot, const float *crad, const float *chei, gbmp_env *out) {
@@ -561,34 +609,75 @@ gbmp_status gbmp_env_create(int32_t ns, const float *sp, const float *sr, int32_
     GBMP_CHECK_ARG(ns == 0 || (sp && sr), "sphere arrays are NULL");
     GBMP_CHECK_ARG(nb == 0 || (bp && brot && bmin && bmax), "cuboid arrays are NULL");
     GBMP_CHECK_ARG(nc == 0 || (cp && crot && crad && chei), "cylinder arrays are NULL");
-    const long long words = 2LL * ns + (ns + 3) / 4 + 5LL * nb + 4LL * nc;
+    const long long words = 2LL * ns + (ns + 3) / 4 + 5LL * nb + 4LL * nc + env_clusters(ns) + env_clusters(nb) +
+                            env_clusters(nc);
     if (words > kMaxEnvWords) {
         set_error("environment needs %lld float4 words, limit %d", words, kMaxEnvWords);
         return GBMP_ERR_CAPACITY;
     }
+    // bounding sphere of every obstacle, then the run order of each type
+    std::vector<double> sc(3 * (size_t)ns), srd(ns), bc(3 * (size_t)nb), brd(nb), cc(3 * (size_t)nc), crd(nc);
+    for (int i = 0; i < ns; ++i) {
+        for (int a = 0; a < 3; ++a) sc[3 * i + a] = sp[3 * i + a];
+        srd[i] = sr[i];
+    }
+    for (int i = 0; i < nb; ++i) {   // box: centre pos + R (min + max) / 2, radius half the diagonal
+        const float *R = brot + 9 * i;
+        double l[3], h2 = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            l[a] = 0.5 * ((double)bmin[3 * i + a] + bmax[3 * i + a]);
+            const double h = 0.5 * ((double)bmax[3 * i + a] - bmin[3 * i + a]);
+            h2 += h * h;
+        }
+        for (int a = 0; a < 3; ++a)
+            bc[3 * i + a] = bp[3 * i + a] + R[3 * a] * l[0] + R[3 * a + 1] * l[1] + R[3 * a + 2] * l[2];
+        brd[i] = std::sqrt(h2);
+    }
+    for (int i = 0; i < nc; ++i) {   // cylinder: centre pos, radius sqrt(r^2 + (h/2)^2)
+        for (int a = 0; a < 3; ++a) cc[3 * i + a] = cp[3 * i + a];
+        crd[i] = std::sqrt((double)crad[i] * crad[i] + 0.25 * (double)chei[i] * chei[i]);
+    }
+    std::vector<int> os(ns), ob(nb), oc(nc);
+    for (int i = 0; i < ns; ++i) os[i] = i;
+    for (int i = 0; i < nb; ++i) ob[i] = i;
+    for (int i = 0; i < nc; ++i) oc[i] = i;
+    cluster_order(sc, os, 0, ns);
+    cluster_order(bc, ob, 0, nb);
+    cluster_order(cc, oc, 0, nc);
+
     auto *e = new gbmp_env_s();
     e->ns = ns; e->nb = nb; e->nc = nc;
     e->h_words.resize(words ? words : 1);
     float4 *w = e->h_words.data();
-    for (int i = 0; i < ns; ++i) w[i] = make_float4(sp[3 * i], sp[3 * i + 1], sp[3 * i + 2], sr[i]);
+    for (int k = 0; k < ns; ++k) {
+        const int i = os[k];
+        w[k] = make_float4(sp[3 * i], sp[3 * i + 1], sp[3 * i + 2], sr[i]);
+    }
     w += ns;
-    for (int i = 0; i < nb; ++i) {
-        host_inverse_pose(bp + 3 * i, brot + 9 * i, w + 5 * i);
-        w[5 * i + 3] = make_float4(bmin[3 * i], bmin[3 * i + 1], bmin[3 * i + 2], 0.f);
-        w[5 * i + 4] = make_float4(bmax[3 * i], bmax[3 * i + 1], bmax[3 * i + 2], 0.f);
+    for (int k = 0; k < nb; ++k) {
+        const int i = ob[k];
+        host_inverse_pose(bp + 3 * i, brot + 9 * i, w + 5 * k);
+        w[5 * k + 3] = make_float4(bmin[3 * i], bmin[3 * i + 1], bmin[3 * i + 2], 0.f);
+        w[5 * k + 4] = make_float4(bmax[3 * i], bmax[3 * i + 1], bmax[3 * i + 2], 0.f);
     }
     w += 5 * nb;
-    for (int i = 0; i < nc; ++i) {
-        host_inverse_pose(cp + 3 * i, crot + 9 * i, w + 4 * i);
-        w[4 * i + 3] = make_float4(crad[i], chei[i] * 0.5f, 0.f, 0.f);
+    for (int k = 0; k < nc; ++k) {
+        const int i = oc[k];
+        host_inverse_pose(cp + 3 * i, crot + 9 * i, w + 4 * k);
+        w[4 * k + 3] = make_float4(crad[i], chei[i] * 0.5f, 0.f, 0.f);
     }
     w += 4 * nc;
     float *nbv = reinterpret_cast<float *>(w + ns);
-    for (int i = 0; i < ns; ++i) {
+    for (int k = 0; k < ns; ++k) {
+        const int i = os[k];
         const double x = sp[3 * i], y = sp[3 * i + 1], z = sp[3 * i + 2], rr = sr[i];
-        w[i] = make_float4(2.f * sp[3 * i], 2.f * sp[3 * i + 1], 2.f * sp[3 * i + 2], 2.f * sr[i]);
-        nbv[i] = (float)(-(x * x + y * y + z * z - rr * rr));
+        w[k] = make_float4(2.f * sp[3 * i], 2.f * sp[3 * i + 1], 2.f * sp[3 * i + 2], 2.f * sr[i]);
+        nbv[k] = (float)(-(x * x + y * y + z * z - rr * rr));
     }
+    float4 *runs = e->h_words.data() + env_cluster_base(ns, nb, nc);
+    cluster_spheres(sc, srd, os, runs);
+    cluster_spheres(bc, brd, ob, runs + env_clusters(ns));
+    cluster_spheres(cc, crd, oc, runs + env_clusters(ns) + env_clusters(nb));
     cudaError_t err = cudaMalloc(&e->d_words, sizeof(float4) * e->h_words.size());
     if (err == cudaSuccess)
         err = cudaMemcpy(e->d_words, e->h_words.data(), sizeof(float4) * e->h_words.size(), cudaMemcpyHostToDevice);

@@ -41,6 +41,9 @@ constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slot
 //   cylinders[nc*4]   inverse pose rows 0..2, (radius, half height, 0, 0)
 //   spheres  [ns]     expanded form (2x, 2y, 2z, 2r)
 //   spheres  [ceil(ns/4)] -(|o|^2 - r^2), four per word
+//   runs     [ceil(ns/32) + ceil(nb/32) + ceil(nc/32)]  (x, y, z, R): obstacles of each
+//            type are stored in spatially compact runs of 32; word c of a type bounds
+//            every obstacle of its run c (obstacles 32c .. 32c + 31)
 // ---------------------------------------------------------------------------------
 struct DevRobot {
     int L, S, P, spl;                 // spl = spheres per lane = ceil(S/32)
@@ -76,7 +79,11 @@ struct DevEnv {
     const float4 *words;              // env_words(ns, nb, nc) float4
 };
 
-__host__ __device__ inline int env_words(int ns, int nb, int nc) { return 2 * ns + (ns + 3) / 4 + 5 * nb + 4 * nc; }
+__host__ __device__ inline int env_clusters(int n) { return (n + 31) / 32; }
+__host__ __device__ inline int env_cluster_base(int ns, int nb, int nc) { return 2 * ns + (ns + 3) / 4 + 5 * nb + 4 * nc; }
+__host__ __device__ inline int env_words(int ns, int nb, int nc) {
+    return env_cluster_base(ns, nb, nc) + env_clusters(ns) + env_clusters(nb) + env_clusters(nc);
+}
 
 // Shared-memory staging of the robot tables and the environment.
 struct SmemTables {
