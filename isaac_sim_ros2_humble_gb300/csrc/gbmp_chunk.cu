@@ -240,11 +240,14 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
         const int k = k0 + lane;
         bool on = false;
         int p0 = 0, p1 = 0;
+        int ga = 0, gb = 0;
         if (k < nlist) {
             const int4 lpr = t.lpair[pairs_overflow ? k : cs.pl[k]];
             const float4 a = w.gb[lpr.x], b = w.gb[lpr.y];
             const float rr = a.w + b.w;
             on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
+            ga = lpr.x;
+            gb = lpr.y;
             p0 = lpr.z;
             p1 = lpr.w;
         }
@@ -254,12 +257,47 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             const int j = __ffs(bal) - 1;
             bal &= bal - 1u;
             const int q0 = __shfl_sync(kFull, p0, j), q1 = __shfl_sync(kFull, p1, j);
-            if (count) fl += (unsigned long long)(q1 - q0) * kFlSelf;
-            for (int p = q0 + lane; p < q1; p += kWarp) {
-                const unsigned ij = __ldg(R.pairs + p);
-                const float thr = __ldg(R.thr + p);
-                const float4 a = w.cen[ij & 0xffffu], b = w.cen[ij >> 16];
-                hit |= sq3(a.x - b.x, a.y - b.y, a.z - b.z) < thr;
+            const int xa = __shfl_sync(kFull, ga, j), xb = __shfl_sync(kFull, gb, j);
+            const int a0 = t.gso[xa], na = t.gso[xa + 1] - a0, b0 = t.gso[xb], nb = t.gso[xb + 1] - b0;
+            if (na <= kWarp && nb <= kWarp && q1 - q0 == na * nb) {
+                // The range holds every (sphere of a, sphere of b) pair.  A sphere of a can
+                // touch a sphere of b only if it touches b's bounding sphere (and the other
+                // way round), so only pairs of such spheres are tested, with the pair
+                // threshold (ri + rj)^2 rounded as the pair list's.
+                const float4 GA = w.gb[xa], GB = w.gb[xb];
+                bool ia = false, ib = false;
+                float4 cj = make_float4(kFar, kFar, kFar, 0.f);
+                if (lane < na) {
+                    const float4 c = w.cen[t.gsl[a0 + lane]];
+                    const float rr = c.w + GB.w;
+                    ia = sq3(c.x - GB.x, c.y - GB.y, c.z - GB.z) < rr * rr;
+                }
+                if (lane < nb) {
+                    cj = w.cen[t.gsl[b0 + lane]];
+                    const float rr = cj.w + GA.w;
+                    ib = sq3(cj.x - GA.x, cj.y - GA.y, cj.z - GA.z) < rr * rr;
+                }
+                unsigned ma = __ballot_sync(kFull, ia);
+                const unsigned mb = __ballot_sync(kFull, ib);
+                if (count) fl += (unsigned long long)(na + nb + __popc(ma) * __popc(mb)) * kFlSelf;
+                if (!mb) ma = 0u;
+                while (ma) {
+                    const int x = __ffs(ma) - 1;
+                    ma &= ma - 1u;
+                    const float4 ci = w.cen[t.gsl[a0 + x]];
+                    if (ib) {
+                        const float sr = __fadd_rn(ci.w, cj.w);
+                        hit |= sq3(ci.x - cj.x, ci.y - cj.y, ci.z - cj.z) < __fmul_rn(sr, sr);
+                    }
+                }
+            } else {
+                if (count) fl += (unsigned long long)(q1 - q0) * kFlSelf;
+                for (int p = q0 + lane; p < q1; p += kWarp) {
+                    const unsigned ij = __ldg(R.pairs + p);
+                    const float thr = __ldg(R.thr + p);
+                    const float4 a = w.cen[ij & 0xffffu], b = w.cen[ij >> 16];
+                    hit |= sq3(a.x - b.x, a.y - b.y, a.z - b.z) < thr;
+                }
             }
             if (__any_sync(kFull, hit)) return true;
         }

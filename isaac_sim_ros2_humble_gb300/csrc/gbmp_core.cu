@@ -468,7 +468,15 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     size_t o_lo = put(r->lower.data(), 4 * L), o_up = put(r->upper.data(), 4 * L);
     size_t o_def = put(r->defv.data(), 4 * L), o_act = put(r->active.data(), L);
     size_t o_grp = put(grp.data(), 4 * 4 * (size_t)G), o_glink = put(glink.data(), 4 * (size_t)G);
+    std::vector<int> gso(G + 1, 0), gsl(S ? S : 1, 0);   // spheres of each group, index order
+    for (int k = 0; k < S; ++k) gso[sgrp[k] + 1]++;
+    for (int g = 0; g < G; ++g) gso[g + 1] += gso[g];
+    {
+        std::vector<int> fill(gso.begin(), gso.end() - 1);
+        for (int k = 0; k < S; ++k) gsl[fill[sgrp[k]]++] = k;
+    }
     size_t o_sgrp = put(sgrp.data(), 4 * (size_t)S), o_lpair = put(lpair.data(), 4 * lpair.size());
+    size_t o_gso = put(gso.data(), 4 * (size_t)(G + 1)), o_gsl = put(gsl.data(), 4 * (size_t)S);
 
     int dev = 0;
     r->num_sms = current_device_sms(&dev);
@@ -502,6 +510,7 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     }
     D.grp = (const float *)(b + o_grp); D.glink = (const int *)(b + o_glink);
     D.sgrp = (const int *)(b + o_sgrp); D.lpair = (const int4 *)(b + o_lpair);
+    D.gso = (const int *)(b + o_gso); D.gsl = (const int *)(b + o_gsl);
     if (flags & GBMP_ROBOT_CODEGEN) {
         gbmp_status st = codegen_build(r);
         if (st) {

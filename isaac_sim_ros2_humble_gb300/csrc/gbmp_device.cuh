@@ -35,6 +35,7 @@ constexpr float kFar = 1.0e15f;           // parking spot for unused sphere slot
 //   grp   [G*4]  per sphere-carrying link ("group"): bounding sphere (x, y, z, R) in the
 //         link frame enclosing all its spheres, inflated by kBroadMargin
 //   glink [G], sgrp [S] (group of each sphere), lpair [NPL*4] (ga, gb, p0, p1)
+//   gso [G+1], gsl [S]: the spheres of group g are gsl[gso[g] .. gso[g+1]) in index order
 // Environment words (float4):
 //   spheres  [ns]     (x, y, z, r)
 //   cuboids  [nb*5]   inverse pose rows 0..2, (min xyz, 0), (max xyz, 0)
@@ -58,6 +59,7 @@ struct DevRobot {
     const float *grp;
     const int *glink, *sgrp;
     const int4 *lpair;
+    const int *gso, *gsl;
     // Executed-work accounting (only when `work` is non-null): work[0] += flops executed,
     // work[1] += states evaluated.  base_flops = per-state FK + sphere + group transforms.
     unsigned long long *work;
@@ -93,6 +95,7 @@ struct SmemTables {
     float4 *grp;
     int *glink, *sgrp;
     int4 *lpair;
+    int *gso, *gsl;
     float4 *env;                      // staged environment words
 };
 
@@ -109,6 +112,8 @@ __host__ __device__ inline size_t smem_tables_bytes(const DevRobot &R, int nword
     b += align16(sizeof(int) * R.G);
     b += align16(sizeof(int) * R.S);
     b += align16(sizeof(int4) * R.NPL);
+    b += align16(sizeof(int) * (R.G + 1));
+    b += align16(sizeof(int) * R.S);
     b += align16(sizeof(float4) * nwords);
     return b;
 }
@@ -146,6 +151,8 @@ __device__ inline SmemTables carve_tables(unsigned char *base, const DevRobot &R
     t.glink = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.G);
     t.sgrp = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.S);
     t.lpair = reinterpret_cast<int4 *>(base + off); off += align16(sizeof(int4) * R.NPL);
+    t.gso = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * (R.G + 1));
+    t.gsl = reinterpret_cast<int *>(base + off); off += align16(sizeof(int) * R.S);
     t.env = reinterpret_cast<float4 *>(base + off);
     return t;
 }
@@ -182,6 +189,8 @@ __device__ inline void stage_tables(const DevRobot &R, const DevEnv &E, const Sm
         t.glink[i] = R.glink[i];
     }
     for (int i = tid; i < R.NPL; i += nt) t.lpair[i] = R.lpair[i];
+    for (int i = tid; i <= R.G; i += nt) t.gso[i] = R.gso[i];
+    for (int i = tid; i < R.S; i += nt) t.gsl[i] = R.gsl[i];
     for (int i = tid; i < nwords; i += nt) t.env[i] = E.words[i];
 }
 
