@@ -7,7 +7,7 @@
 #include <fstream>
 #include <iostream>
 
-#include "gbmp_cudampl.hpp"
+#include "gbmp_cudampl_rrg.hpp"
 
 namespace {
 
@@ -180,7 +180,28 @@ int main(int argc, char **argv) {
         std::vector<float> pf;
         for (auto &row : path) pf.insert(pf.end(), row.begin(), row.end());
         out.flat("path", pf);
-        std::printf("facade ok: %d states, %d edges, path of %zu waypoints\n", n, m, path.size());
+
+        // ---- RRG (RRG.cpp) over a space whose constraints are the shelf boxes ----
+        std::vector<CUDAMPLib::BaseConstraintPtr> shelf_cons;
+        shelf_cons.push_back(std::make_shared<CUDAMPLib::SelfCollisionConstraint>("self_collision_constraint", slink,
+                                                                                  srad, enables));
+        std::vector<std::vector<float>> eye(nshelf, std::vector<float>{1, 0, 0, 0, 1, 0, 0, 0, 1});
+        shelf_cons.push_back(
+            std::make_shared<CUDAMPLib::EnvConstraintCuboid>("shelf", shelf_p, eye, shelf_mx, shelf_mn));
+        auto shelf_space = std::make_shared<CUDAMPLib::SingleArmSpace>(dim, shelf_cons, types, pose_arr, axis_arr,
+                                                                       parent, slink, spos, srad, active, lower,
+                                                                       upper, defv, names, res);
+        CUDAMPLib::RRG rrg(shelf_space);
+        auto task = std::make_shared<CUDAMPLib::SingleArmTask>(std::vector<std::vector<float>>{start},
+                                                               std::vector<std::vector<float>>{goal});
+        rrg.setMotionTask(task);
+        rrg.solve(std::make_shared<CUDAMPLib::TimeoutTermination>(30.f));
+        std::vector<float> rf;
+        for (auto &row : task->getSolution()) rf.insert(rf.end(), row.begin(), row.end());
+        out.flat("rrg_path", rf);
+        out.flat("rrg_vertices", std::vector<int>{rrg.getNumOfVertices()});
+        std::printf("facade ok: %d states, %d edges, path of %zu waypoints, RRG path of %zu states (%s)\n", n, m,
+                    path.size(), task->getSolution().size(), task->getFailureReason().c_str());
         return 0;
     } catch (const std::exception &e) {
         std::fprintf(stderr, "error: %s\n", e.what());

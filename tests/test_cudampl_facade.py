@@ -1,9 +1,9 @@
 """The C++ facade include/gbmp_cudampl.hpp (CUDAMPLib::SingleArmSpace / SingleArmStates /
-SingleArmStateManager and CPRRTC::RobotSolver over the C-ABI) compiles against gbmp.h
-and libgbmp, and a C++ program driving it the way the reference's callers do gives the
-oracle's results: collision verdicts and per-constraint costs, link poses, motion
-feasibility and costs, samples, nearest neighbours, and a planned path that the oracle
-re-validates."""
+SingleArmStateManager and CPRRTC::RobotSolver over the C-ABI) and its RRG planner
+(include/gbmp_cudampl_rrg.hpp) compile against gbmp.h and libgbmp, and a C++ program
+driving them the way the reference's callers do gives the oracle's results: collision
+verdicts and per-constraint costs, link poses, motion feasibility and costs, samples,
+nearest neighbours, and RobotSolver and RRG paths that the oracle re-validates."""
 import os
 import shutil
 import subprocess
@@ -126,6 +126,19 @@ def test_facade_matches_oracle(tmp_path):
 
     path = got["path"].astype(np.float32).reshape(-1, robot.dim)
     assert len(path) >= 2
+    _check_path(ms, robot, path, start, goal)
+
+    # RRG over the shelf space: a dense path, waypoints interpolated with the reference's
+    # rule (util.cpp:205-248: floor(d / res) steps, so spacing in [res, 2 res), and each
+    # segment ends on its waypoint again)
+    rrg = got["rrg_path"].astype(np.float32).reshape(-1, robot.dim)
+    assert len(rrg) >= 2 and got["rrg_vertices"][0] > 4
+    _check_path(ms, robot, rrg, start, goal)
+    assert np.all(np.linalg.norm(np.diff(rrg, axis=0), axis=1) < 2 * RES)
+
+
+def _check_path(ms, robot, path, start, goal):
+    act = robot.active.astype(bool)
     np.testing.assert_array_equal(path[0], start[act])
     np.testing.assert_array_equal(path[-1], goal[act])
     full = robot.full_from_active(path)
