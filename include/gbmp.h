@@ -207,6 +207,30 @@ GBMP_API gbmp_status gbmp_steer(gbmp_robot robot, const float *d_from, const int
 GBMP_API gbmp_status gbmp_sample(gbmp_robot robot, uint64_t seed, uint64_t offset, int64_t n, float *d_q,
                         void *stream);
 
+/* Projection onto a task-space region and the joint limits, replacing
+ * SingleArmSpace::projectStates (SingleArmSpace.cu:1631-1662) with the projectable
+ * TaskSpaceConstraint (TaskSpaceConstraint.cu:66-396) and BoundaryConstraint
+ * (BoundaryConstraint.cu:36-155).  `iterations` rounds (the reference uses 10) of: FK;
+ * the pose (x, y, z, roll, pitch, yaw) of `offset` in link `task_link`; the error
+ * reference - pose with each component shrunk by its tolerance; the step
+ * J_a^T (J_a J_a^T + 1e-4 I)^-1 error over the active joints (J: geometric Jacobian,
+ * angular rows first); plus, with use_boundary, the pull back inside the limits; added to
+ * the active joints.  The Euler-angle error is used as an angular error, as in the
+ * reference, so orientation targets converge only near zero roll / pitch / yaw of the
+ * constrained frame (choose `offset` accordingly, or loosen the orientation tolerances).
+ * In place on d_q [n*L]; d_task_cost / d_bound_cost [n] (NULL allowed) get the final
+ * costs of computeCost (0 below 1e-4).  task_link = -1 disables the task-space part. */
+typedef struct gbmp_projection {
+    int32_t task_link;
+    float offset[16];      /* row-major 4x4 pose of the constrained frame in the task link */
+    float reference[6];    /* x, y, z, roll, pitch, yaw in the base frame */
+    float tolerance[6];
+    int32_t use_boundary;
+    int32_t iterations;
+} gbmp_projection;
+GBMP_API gbmp_status gbmp_project_states(gbmp_robot robot, const gbmp_projection *proj, float *d_q, int64_t n,
+                                float *d_task_cost, float *d_bound_cost, void *stream);
+
 /* ---- parallel RRT-Connect ----
  * Replaces CPRRTC::RobotSolver (cudampl/CPRRTC/include/RobotSolver.h:84-101,
  * cudampl/CPRRTC/src/RobotSolver.cu:348-473) and pRRTC::solve (pRRTC/src/planning/

@@ -22,6 +22,11 @@ STEP_L2, STEP_LINF = 0, 1
 ROBOT_GENERIC, ROBOT_CODEGEN = 0, 1
 
 
+class Projection(C.Structure):
+    _fields_ = [("task_link", C.c_int32), ("offset", C.c_float * 16), ("reference", C.c_float * 6),
+                ("tolerance", C.c_float * 6), ("use_boundary", C.c_int32), ("iterations", C.c_int32)]
+
+
 class GbmpError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"gbmp status {status} ({STATUS.get(status, '?')}): {message}")
@@ -102,6 +107,7 @@ SIGNATURES = {
     "gbmp_nearest": [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp],
     "gbmp_steer": [_vp, _vp, _vp, _vp, _i64, _f32, _vp],
     "gbmp_sample": [_vp, _u64, _u64, _i64, _vp, _vp],
+    "gbmp_project_states": [_vp, C.c_void_p, _vp, _i64, _vp, _vp, _vp],
     "gbmp_planner_create": [_vp, _i32, _i32, C.POINTER(_vp)],
     "gbmp_planner_destroy": [_vp],
     "gbmp_rrtc_solve": [_vp, _vp, _vp, _vp, C.POINTER(RrtcSettings), _vp, _i32, C.POINTER(RrtcResult), _vp],

@@ -130,6 +130,25 @@ def check_edges(robot: Robot, env: Env, q_from, q_to, resolution: float = 0.0, r
                                        stream_handle(stream)))
 
 
+def project_states(robot: Robot, q, task_link: int = -1, offset=None, reference=(0, 0, 0, 0, 0, 0),
+                   tolerance=(0, 0, 0, 0, 0, 0), use_boundary: bool = True, iterations: int = 10, task_cost=None,
+                   bound_cost=None, stream=None):
+    """Project the states q [n, L] (in place) onto a task-space region of link
+    `task_link` (pose of `offset` in that link, reference x y z roll pitch yaw, per-axis
+    tolerances) and the joint limits; final costs into task_cost / bound_cost [n]."""
+    n = _n(q, robot.L)
+    p = _lib.Projection()
+    p.task_link = int(task_link)
+    off = np.eye(4, dtype=np.float32) if offset is None else np.asarray(offset, np.float32)
+    p.offset[:] = [float(v) for v in off.reshape(16)]
+    p.reference[:] = [float(v) for v in reference]
+    p.tolerance[:] = [float(v) for v in tolerance]
+    p.use_boundary = int(bool(use_boundary))
+    p.iterations = int(iterations)
+    check(_lib.load().gbmp_project_states(robot.handle, C.byref(p), ptr(q), n, ptr(task_cost), ptr(bound_cost),
+                                          stream_handle(stream)))
+
+
 def nearest(robot: Robot, tree, queries, out, cand=None, stream=None):
     M = _n(tree, robot.L)
     Q = _n(queries, robot.L)

@@ -778,3 +778,151 @@ int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *p
     free(P); free(C); free(dir); free(st); free(qs); free(qn); free(qa); free(qb); free(qc);
     return solved;
 }
+
+/* ------------------------------------------------------------------------------------
+ * Constraint projection.
+ * ---------------------------------------------------------------------------------- */
+
+/* 4x4 product with an implicit last row (0 0 0 1), TaskSpaceConstraint.cu:47-63. */
+static void pr_mul44(const float *A, const float *B, float *C)
+{
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c)
+            C[4 * r + c] = A[4 * r] * B[c] + A[4 * r + 1] * B[4 + c] + A[4 * r + 2] * B[8 + c] + A[4 * r + 3] * B[12 + c];
+    C[12] = 0.f; C[13] = 0.f; C[14] = 0.f; C[15] = 1.f;
+}
+
+/* Task-frame pose and its x, y, z, roll, pitch, yaw (TaskSpaceConstraint.cu:185-206). */
+static void pr_task_frame(const float *poses, int task_link, const float *offset, float *P, float v[6])
+{
+    pr_mul44(poses + 16 * task_link, offset, P);
+    v[0] = P[3]; v[1] = P[7]; v[2] = P[11];
+    v[4] = asinf(-P[8]);
+    v[3] = atan2f(P[9], P[10]);
+    v[5] = atan2f(P[4], P[0]);
+}
+
+static float pr_dead(float diff, float tol)
+{
+    return copysignf(fmaxf(fabsf(diff) - tol, 0.0f), diff);
+}
+
+/* Gradient of the task-space constraint for one state (TaskSpaceConstraint.cu:167-396). */
+static void pr_task_grad(const or_robot *r, const uint8_t *active, const or_projection *p, const float *poses,
+                         float *grad)
+{
+    const int L = r->L;
+    float P[16], v[6], err[6];
+    pr_task_frame(poses, p->task_link, p->offset, P, v);
+    /* reference - current, dead-banded; order roll pitch yaw x y z (angular rows first) */
+    err[0] = pr_dead(p->reference[3] - v[3], p->tolerance[3]);
+    err[1] = pr_dead(p->reference[4] - v[4], p->tolerance[4]);
+    err[2] = pr_dead(p->reference[5] - v[5], p->tolerance[5]);
+    err[3] = pr_dead(p->reference[0] - v[0], p->tolerance[0]);
+    err[4] = pr_dead(p->reference[1] - v[1], p->tolerance[1]);
+    err[5] = pr_dead(p->reference[2] - v[2], p->tolerance[2]);
+    float J[64 * 6];
+    for (int j = 0; j < L; ++j) {
+        float *c = J + 6 * j;
+        for (int k = 0; k < 6; ++k) c[k] = 0.f;
+        if (j > p->task_link) continue;
+        const float *T = poses + 16 * j;
+        const float *a = r->axis + 3 * j;
+        const float w0 = T[0] * a[0] + T[1] * a[1] + T[2] * a[2];
+        const float w1 = T[4] * a[0] + T[5] * a[1] + T[6] * a[2];
+        const float w2 = T[8] * a[0] + T[9] * a[1] + T[10] * a[2];
+        if (r->type[j] == OR_REVOLUTE) {
+            const float d0 = v[0] - T[3], d1 = v[1] - T[7], d2 = v[2] - T[11];
+            c[0] = w0; c[1] = w1; c[2] = w2;
+            c[3] = w1 * d2 - w2 * d1;
+            c[4] = w2 * d0 - w0 * d2;
+            c[5] = w0 * d1 - w1 * d0;
+        } else if (r->type[j] == OR_PRISMATIC) {
+            c[3] = w0; c[4] = w1; c[5] = w2;
+        }
+    }
+    /* A = J_a J_a^T + 1e-4 I, Gauss-Jordan without pivoting (TaskSpaceConstraint.cu:290-350) */
+    float aug[6][12];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            float sum = 0.0f;
+            for (int k = 0; k < L; ++k)
+                if (active[k]) sum += J[6 * k + i] * J[6 * k + j];
+            aug[i][j] = (i == j) ? sum + 1e-4f : sum;
+        }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 6; j < 12; ++j) aug[i][j] = (j - 6 == i) ? 1.0f : 0.0f;
+    int invertible = 1;
+    for (int i = 0; i < 6 && invertible; ++i) {
+        const float pivot = aug[i][i];
+        if (fabsf(pivot) < 1e-8f) { invertible = 0; break; }
+        for (int j = 0; j < 12; ++j) aug[i][j] /= pivot;
+        for (int k = 0; k < 6; ++k)
+            if (k != i) {
+                const float f = aug[k][i];
+                for (int j = 0; j < 12; ++j) aug[k][j] -= f * aug[i][j];
+            }
+    }
+    for (int j = 0; j < L; ++j) {
+        grad[j] = 0.f;
+        if (!active[j] || !invertible) continue;
+        float g = 0.0f;
+        for (int i = 0; i < 6; ++i) {
+            float s = 0.0f;
+            for (int m = 0; m < 6; ++m) s += J[6 * j + m] * aug[m][6 + i];
+            g += s * err[i];
+        }
+        grad[j] = g;
+    }
+}
+
+static float pr_task_cost(const or_projection *p, const float *poses)
+{
+    float P[16], v[6], c = 0.f;
+    pr_task_frame(poses, p->task_link, p->offset, P, v);
+    for (int k = 0; k < 6; ++k) {
+        const float d = v[k] - p->reference[k], t = p->tolerance[k];
+        c += fmaxf(d * d - t * t, 0.f);
+    }
+    c = sqrtf(c);
+    return c < 1e-4f ? 0.0f : c;
+}
+
+static float pr_bound_cost(int L, const uint8_t *active, const float *lower, const float *upper, const float *q)
+{
+    float c = 0.0f;
+    for (int j = 0; j < L; ++j) {
+        if (!active[j]) continue;
+        if (q[j] < lower[j]) c += (lower[j] - q[j]) * (lower[j] - q[j]);
+        else if (q[j] > upper[j]) c += (q[j] - upper[j]) * (q[j] - upper[j]);
+    }
+    return c < 1e-4f ? 0.0f : sqrtf(c);
+}
+
+void or_project(const or_robot *r, const uint8_t *active, const float *lower, const float *upper,
+                const or_projection *p, float *q, int64_t n, float *task_cost, float *bound_cost,
+                int32_t nthreads)
+{
+    const int L = r->L;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+    for (int64_t s = 0; s < n; ++s) {
+        float *qs = q + s * L;
+        float poses[64 * 16], gt[64], gb[64];
+        for (int it = 0; it < p->iterations; ++it) {
+            or_fk_f32(r, qs, 1, poses);
+            for (int j = 0; j < L; ++j) gt[j] = gb[j] = 0.f;
+            if (p->task_link >= 0) pr_task_grad(r, active, p, poses, gt);
+            if (p->use_boundary)
+                for (int j = 0; j < L; ++j) {
+                    if (!active[j]) continue;
+                    if (qs[j] < lower[j]) gb[j] = lower[j] - qs[j];
+                    else if (qs[j] > upper[j]) gb[j] = upper[j] - qs[j];
+                }
+            for (int j = 0; j < L; ++j)
+                if (active[j]) qs[j] = qs[j] + (gt[j] + gb[j]);
+        }
+        or_fk_f32(r, qs, 1, poses);
+        if (task_cost) task_cost[s] = p->task_link >= 0 ? pr_task_cost(p, poses) : 0.f;
+        if (bound_cost) bound_cost[s] = p->use_boundary ? pr_bound_cost(L, active, lower, upper, qs) : 0.f;
+    }
+}

@@ -100,6 +100,26 @@ int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *p
 
 int32_t or_num_threads(void);
 
+/* ---- constraint projection ----
+ * SingleArmSpace::projectStates (SingleArmSpace.cu:1631-1662): `iterations` rounds of
+ * FK, the task-space gradient (TaskSpaceConstraint.cu:167-396: damped pseudo-inverse of
+ * the task link's geometric Jacobian times the dead-banded pose error) plus the
+ * joint-limit gradient (BoundaryConstraint.cu:104-155), added to the active joints with
+ * step 1 (update_with_grad).  task_link < 0 disables the task-space constraint.
+ * After the rounds, the final costs (TaskSpaceConstraint.cu:66-139,
+ * BoundaryConstraint.cu:36-88) go to task_cost[n] / bound_cost[n] (either may be NULL). */
+typedef struct or_projection {
+    int32_t task_link;
+    float offset[16];          /* pose of the constrained frame in the task link       */
+    float reference[6];        /* x, y, z, roll, pitch, yaw                           */
+    float tolerance[6];
+    int32_t use_boundary;
+    int32_t iterations;
+} or_projection;
+void or_project(const or_robot *r, const uint8_t *active, const float *lower, const float *upper,
+                const or_projection *p, float *q, int64_t n, float *task_cost, float *bound_cost,
+                int32_t nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,12 +69,32 @@ def lib():
                               C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32), _i32p]
         L.or_rrtc.restype = C.c_int32
         L.or_num_threads.restype = C.c_int32
+        L.or_project.argtypes = [vp, _u8p, _f32p, _f32p, vp, _f32p, C.c_int64, vp, vp, C.c_int32]
         _lib = L
     return _lib
 
 
 def _c(a, dt):
     return np.ascontiguousarray(a, dtype=dt)
+
+
+class Projection(C.Structure):
+    """Task-space + joint-limit projection settings (layout of or_projection)."""
+    _fields_ = [("task_link", C.c_int32), ("offset", C.c_float * 16), ("reference", C.c_float * 6),
+                ("tolerance", C.c_float * 6), ("use_boundary", C.c_int32), ("iterations", C.c_int32)]
+
+
+def projection(task_link=-1, offset=None, reference=(0, 0, 0, 0, 0, 0), tolerance=(0, 0, 0, 0, 0, 0),
+               use_boundary=True, iterations=10) -> Projection:
+    p = Projection()
+    p.task_link = int(task_link)
+    off = np.eye(4, dtype=np.float32) if offset is None else np.asarray(offset, np.float32).reshape(16)
+    p.offset[:] = [float(v) for v in np.asarray(off, np.float32).reshape(16)]
+    p.reference[:] = [float(v) for v in reference]
+    p.tolerance[:] = [float(v) for v in tolerance]
+    p.use_boundary = int(bool(use_boundary))
+    p.iterations = int(iterations)
+    return p
 
 
 class OracleModel:
@@ -178,6 +198,17 @@ class OracleModel:
         for k in range(n):
             lib().or_edge_state(f, t, d, self.L, n, k, out[k])
         return out
+
+    def project(self, q, proj: Projection, nthreads=0):
+        """Projected copies of q [n, L] and the final task-space / joint-limit costs."""
+        rb = self.robot
+        q = _c(np.asarray(q).reshape(-1, self.L), np.float32).copy()
+        n = q.shape[0]
+        tc = np.zeros(n, np.float32)
+        bc = np.zeros(n, np.float32)
+        lib().or_project(C.byref(self.r), _c(rb.active, np.uint8), _c(rb.lower, np.float32), _c(rb.upper, np.float32),
+                         C.byref(proj), q, n, tc.ctypes.data, bc.ctypes.data, nthreads)
+        return q, tc, bc
 
     def check_motions(self, q_from, q_to, res, rule=STEP_L2, early_exit=True, nthreads=0):
         f = _c(np.asarray(q_from).reshape(-1, self.L), np.float32)

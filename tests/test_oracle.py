@@ -179,3 +179,30 @@ def test_sampler_in_limits_and_reproducible():
     # uniformity (loose): mean of the unit-range coordinate
     u = (a[:, 2] - robot.lower[2]) / (robot.upper[2] - robot.lower[2])
     assert abs(u.mean() - 0.5) < 0.05
+
+
+def test_projection_restatement_converges_where_the_method_is_consistent():
+    """The projection restatement (SingleArmSpace.cu:1631-1662) reaches position targets
+    and zero-orientation frame targets from nearby states; with a general target
+    orientation the reference's Euler-angle error does not act as an angular error and the
+    iteration does not converge (a property of the reference method, kept as is)."""
+    import math
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    m = O.OracleModel(robot)
+    rng = np.random.default_rng(0)
+    q0 = robot.sample_full(rng, 1)
+    tip = robot.num_links - 1
+    T = W.fk_numpy(robot, q0)[0][tip]
+    near = (q0 + 0.01 * rng.standard_normal((100, robot.num_links)) * robot.active).astype(np.float32)
+    pos_only = O.projection(task_link=tip, reference=[T[0, 3], T[1, 3], T[2, 3], 0, 0, 0],
+                            tolerance=(1e-3,) * 3 + (2 * math.pi,) * 3, use_boundary=False)
+    assert (m.project(near, pos_only)[1] == 0).all()
+    off = np.eye(4, dtype=np.float32)
+    off[:3, :3] = T[:3, :3].T
+    full = O.projection(task_link=tip, offset=off, reference=[T[0, 3], T[1, 3], T[2, 3], 0, 0, 0],
+                        tolerance=(1e-3,) * 3 + (1e-2,) * 3, use_boundary=False)
+    assert (m.project(near, full)[1] == 0).all()
+    rpy = [math.atan2(T[2, 1], T[2, 2]), math.asin(-T[2, 0]), math.atan2(T[1, 0], T[0, 0])]
+    general = O.projection(task_link=tip, reference=[T[0, 3], T[1, 3], T[2, 3]] + rpy,
+                           tolerance=(1e-3,) * 3 + (1e-2,) * 3, use_boundary=False)
+    assert (m.project(near, general)[1] == 0).mean() < 0.5
