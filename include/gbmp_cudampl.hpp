@@ -88,14 +88,14 @@ inline void rpy_to_rot(float roll, float pitch, float yaw, float *R) {   // R = 
 // Constraints.  Only their tables are kept; SingleArmSpace turns them into one robot
 // (self-collision link matrix) and one environment (all obstacles).
 // ---------------------------------------------------------------------------------
-enum class ConstraintKind { Self = 0, Sphere = 1, Cuboid = 2, Cylinder = 3 };
+enum class ConstraintKind { Self = 0, Sphere = 1, Cuboid = 2, Cylinder = 3, TaskSpace = 4, Boundary = 5 };
 
 class BaseConstraint {
   public:
     BaseConstraint(std::string name, ConstraintKind k) : constraint_name(std::move(name)), kind(k) {}
     virtual ~BaseConstraint() = default;
     std::string getName() const { return constraint_name; }
-    bool isProjectable() const { return false; }
+    bool isProjectable() const { return kind == ConstraintKind::TaskSpace || kind == ConstraintKind::Boundary; }
     std::string constraint_name;
     ConstraintKind kind;
 };
@@ -149,6 +149,39 @@ class EnvConstraintCylinder : public BaseConstraint {
     }
     std::vector<std::vector<float>> pos, rot;
     std::vector<float> radius, height;
+};
+
+// Task-space region of a frame fixed in one link (TaskSpaceConstraint.h): pose of
+// `offset_pose_in_task_link` (4x4, Eigen or 16 row-major floats) in link
+// `task_link_index`, reference x y z roll pitch yaw and per-axis tolerances.  Projectable:
+// samples and interpolated states of a space that holds it are projected onto it.
+class TaskSpaceConstraint : public BaseConstraint {
+  public:
+    template <typename M>
+    TaskSpaceConstraint(const std::string &name, int task_link_index, const M &offset_pose_in_task_link,
+                        const std::vector<float> &reference_frame, const std::vector<float> &tolerance)
+        : BaseConstraint(name, ConstraintKind::TaskSpace), task_link(task_link_index), reference(reference_frame),
+          tol(tolerance) {
+        if (reference_frame.size() != 6 || tolerance.size() != 6)
+            throw std::runtime_error("reference frame and tolerance need 6 values each");
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) offset[4 * r + c] = detail::pose_at(offset_pose_in_task_link, r, c);
+    }
+    int task_link;
+    float offset[16];
+    std::vector<float> reference, tol;
+};
+
+// Joint limits as a projectable constraint (BoundaryConstraint.h).  The bounds are the
+// space's joint limits (the reference builds it from the same limits).
+class BoundaryConstraint : public BaseConstraint {
+  public:
+    BoundaryConstraint(const std::string &name, const std::vector<float> &lower_bound,
+                       const std::vector<float> &upper_bound, const std::vector<bool> &active_joint_map)
+        : BaseConstraint(name, ConstraintKind::Boundary), lower(lower_bound), upper(upper_bound),
+          active(active_joint_map) {}
+    std::vector<float> lower, upper;
+    std::vector<bool> active;
 };
 
 class SingleArmSpace;
@@ -267,7 +300,17 @@ class SingleArmSpace {
         if (!st->isValid()) return nullptr;
         detail::check(gbmp_sample(robot_, seed_, offset_, num_of_config, st->getJointStatesCuda(), nullptr));
         offset_ += (uint64_t)num_of_config;
+        if (projectable_) projectStates(st);   // SingleArmSpace.cu:316-320
         return st;
+    }
+
+    bool hasProjectableConstraints() const { return projectable_; }
+    // Projection onto the projectable constraints (SingleArmSpace.cu:1631-1662).
+    void projectStates(const BaseStatesPtr &states) {
+        if (!projectable_ || states->getNumOfStates() == 0) return;
+        detail::check(gbmp_project_states(robot_, &proj_, states->getJointStatesCuda(), states->getNumOfStates(),
+                                          nullptr, nullptr, nullptr));
+        cudaDeviceSynchronize();
     }
     void setSeed(uint64_t seed) { seed_ = seed; offset_ = 0; }
 
@@ -283,11 +326,33 @@ class SingleArmSpace {
         int seen[4] = {0, 0, 0, 0};
         for (size_t c = 0; c < constraints_.size(); ++c) {
             const int k = (int)constraints_[c]->kind;
+            if (k > 3) continue;   // projectable constraints: below
             float *dst = states->getCostsCuda() + c * (size_t)n;
             if (!seen[k]++) detail::check(cudaMemcpy(dst, static_cast<float *>(slots.p) + (size_t)k * n,
                                                      sizeof(float) * n, cudaMemcpyDeviceToDevice) == cudaSuccess
                                               ? GBMP_OK : GBMP_ERR_CUDA);
             else detail::check(cudaMemset(dst, 0, sizeof(float) * n) == cudaSuccess ? GBMP_OK : GBMP_ERR_CUDA);
+        }
+        if (projectable_) {
+            // task-space and joint-limit costs (computeCost of the two constraints): a
+            // projection of zero iterations only evaluates them
+            detail::DevArray tc(sizeof(float) * n), bc(sizeof(float) * n);
+            gbmp_projection p0 = proj_;
+            p0.iterations = 0;
+            detail::check(gbmp_project_states(robot_, &p0, states->getJointStatesCuda(), n, static_cast<float *>(tc.p),
+                                              static_cast<float *>(bc.p), nullptr));
+            std::vector<float> h_tc(n), h_bc(n), tot = states->getTotalCostsHost();
+            cudaMemcpy(h_tc.data(), tc.p, sizeof(float) * n, cudaMemcpyDeviceToHost);
+            cudaMemcpy(h_bc.data(), bc.p, sizeof(float) * n, cudaMemcpyDeviceToHost);
+            for (size_t c = 0; c < constraints_.size(); ++c) {
+                const ConstraintKind k = constraints_[c]->kind;
+                if (k != ConstraintKind::TaskSpace && k != ConstraintKind::Boundary) continue;
+                const std::vector<float> &src = k == ConstraintKind::TaskSpace ? h_tc : h_bc;
+                cudaMemcpy(states->getCostsCuda() + c * (size_t)n, src.data(), sizeof(float) * n,
+                           cudaMemcpyHostToDevice);
+                for (int i = 0; i < n; ++i) tot[i] += src[i];
+            }
+            cudaMemcpy(states->getTotalCostsCuda(), tot.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
         }
         detail::check(cudaDeviceSynchronize() == cudaSuccess ? GBMP_OK : GBMP_ERR_CUDA);
     }
@@ -327,6 +392,7 @@ class SingleArmSpace {
         detail::check(gbmp_steer(robot_, from_states->getJointStatesCuda(), nullptr, to_states->getJointStatesCuda(),
                                  to_states->getNumOfStates(), max_distance, nullptr));
         cudaDeviceSynchronize();
+        if (projectable_) projectStates(to_states);   // SingleArmSpace.cu:1400-1405
     }
 
     BaseStatesPtr createStatesFromVectorFull(const std::vector<std::vector<float>> &joint_values) {
@@ -405,6 +471,33 @@ class SingleArmSpace {
         d.self_enables = enables_.data();
         d.resolution = resolution_;
         detail::check(gbmp_robot_create(&d, GBMP_ROBOT_GENERIC, &robot_));
+        // projectable constraints (SingleArmSpace.cu:33-60): one task-space region and / or
+        // the joint limits
+        proj_.task_link = -1;
+        proj_.iterations = 10;   // CUDAMPLib_PROJECT_MAX_ITERATION
+        for (int k = 0; k < 16; ++k) proj_.offset[k] = (k % 5 == 0) ? 1.f : 0.f;
+        for (auto &c : constraints_) {
+            if (c->kind == ConstraintKind::TaskSpace) {
+                if (proj_.task_link >= 0) throw std::runtime_error("one task-space constraint per space is supported");
+                auto *tc = static_cast<TaskSpaceConstraint *>(c.get());
+                if (tc->task_link < 0 || tc->task_link >= L_) throw std::runtime_error("task link index out of range");
+                proj_.task_link = tc->task_link;
+                for (int k = 0; k < 16; ++k) proj_.offset[k] = tc->offset[k];
+                for (int k = 0; k < 6; ++k) {
+                    proj_.reference[k] = tc->reference[k];
+                    proj_.tolerance[k] = tc->tol[k];
+                }
+                projectable_ = true;
+            } else if (c->kind == ConstraintKind::Boundary) {
+                auto *bc = static_cast<BoundaryConstraint *>(c.get());
+                for (int j = 0; j < L_; ++j)
+                    if (active_[j] && (j >= (int)bc->lower.size() || j >= (int)bc->upper.size() ||
+                                       bc->lower[j] != lower_[j] || bc->upper[j] != upper_[j]))
+                        throw std::runtime_error("BoundaryConstraint bounds must be the space's joint limits");
+                proj_.use_boundary = 1;
+                projectable_ = true;
+            }
+        }
         std::vector<float> sp, sr, bp, br, bmn, bmx, cp, cr, crad, chei;
         for (auto &c : constraints_) {
             if (c->kind == ConstraintKind::Sphere) {
@@ -436,6 +529,8 @@ class SingleArmSpace {
                                       chei.data(), &env_));
     }
 
+    bool projectable_ = false;
+    gbmp_projection proj_{};
     size_t dim_;
     std::vector<BaseConstraintPtr> constraints_;
     float resolution_;

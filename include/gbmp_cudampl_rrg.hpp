@@ -89,11 +89,40 @@ class BaseTask {
 };
 typedef std::shared_ptr<BaseTask> BaseTaskPtr;
 
+// Vectors of `vec` without the ones within `tol` (per element) of an earlier kept one
+// (util.cpp:250-266).
+inline std::vector<std::vector<float>> removeRedundantVectors(const std::vector<std::vector<float>> &vec, float tol) {
+    std::vector<std::vector<float>> unique;
+    for (const auto &v : vec) {
+        bool dup = false;
+        for (const auto &u : unique) {
+            bool same = u.size() == v.size();
+            for (size_t k = 0; same && k < v.size(); ++k) same = std::fabs(v[k] - u[k]) <= tol;
+            if (same) { dup = true; break; }
+        }
+        if (!dup) unique.push_back(v);
+    }
+    return unique;
+}
+
 class SingleArmTask : public BaseTask {
   public:
     SingleArmTask(const std::vector<std::vector<float>> &start_joint_values,
                   const std::vector<std::vector<float>> &goal_joint_values)
         : start_(start_joint_values), goal_(goal_joint_values) {}
+    // Goal region (SingleArmTask.cpp:12-39): `goal_config_sampling_attempts` samples of a
+    // space whose projectable constraints describe the region (sampling projects them),
+    // kept when feasible, duplicates within 1e-5 removed.
+    SingleArmTask(const std::vector<std::vector<float>> &start_joint_values, const BaseSpacePtr &goal_region,
+                  int goal_config_sampling_attempts = 50)
+        : start_(start_joint_values) {
+        auto goals = goal_region->sample(goal_config_sampling_attempts);
+        if (!goals) throw std::runtime_error("goal region sampling failed");
+        std::vector<bool> feasible;
+        goal_region->checkStates(goals, feasible);
+        goals->filterStates(feasible);
+        goal_ = removeRedundantVectors(goals->getJointStatesHost(), 1e-5f);
+    }
     std::vector<std::vector<float>> getStartStatesVector() override { return start_; }
     std::vector<std::vector<float>> getGoalStatesVector() override { return goal_; }
     BaseStatesPtr getStartStates(BaseSpacePtr space) override { return space->createStatesFromVector(start_); }

@@ -97,6 +97,8 @@ int main(int argc, char **argv) {
         auto start = in.fv(dim), goal = in.fv(dim);
         const int nshelf = in.i();
         auto shelf_p = in.rows(nshelf, 3), shelf_mn = in.rows(nshelf, 3), shelf_mx = in.rows(nshelf, 3);
+        const int region_link = in.i();
+        auto region_ref = in.fv(6), region_tol = in.fv(6);
 
         std::vector<bool> active(L);
         for (int j = 0; j < L; ++j) active[j] = act[j] != 0;
@@ -200,8 +202,27 @@ int main(int argc, char **argv) {
         for (auto &row : task->getSolution()) rf.insert(rf.end(), row.begin(), row.end());
         out.flat("rrg_path", rf);
         out.flat("rrg_vertices", std::vector<int>{rrg.getNumOfVertices()});
-        std::printf("facade ok: %d states, %d edges, path of %zu waypoints, RRG path of %zu states (%s)\n", n, m,
-                    path.size(), task->getSolution().size(), task->getFailureReason().c_str());
+
+        // ---- goal region (SingleArmTask.cpp:12-39): task-space + joint-limit constraints ----
+        std::vector<CUDAMPLib::BaseConstraintPtr> gcons;
+        gcons.push_back(std::make_shared<CUDAMPLib::SelfCollisionConstraint>("self_collision_constraint", slink, srad,
+                                                                             enables));
+        gcons.push_back(std::make_shared<CUDAMPLib::EnvConstraintSphere>("obstacle_sphere", sp, sr));
+        gcons.push_back(std::make_shared<CUDAMPLib::EnvConstraintCuboid>("obstacle_cuboid", bp, brot, bmx, bmn));
+        gcons.push_back(std::make_shared<CUDAMPLib::EnvConstraintCylinder>("obstacle_cylinder", cp, crot, crad, chei));
+        const std::array<float, 16> ident{1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        gcons.push_back(std::make_shared<CUDAMPLib::TaskSpaceConstraint>("goal_region", region_link, ident, region_ref,
+                                                                         region_tol));
+        gcons.push_back(std::make_shared<CUDAMPLib::BoundaryConstraint>("boundary", lower, upper, active));
+        auto region = std::make_shared<CUDAMPLib::SingleArmSpace>(dim, gcons, types, pose_arr, axis_arr, parent, slink,
+                                                                  spos, srad, active, lower, upper, defv, names, res);
+        CUDAMPLib::SingleArmTask gtask(std::vector<std::vector<float>>{start}, region, 256);
+        std::vector<float> gf;
+        for (auto &row : gtask.getGoalStatesVector()) gf.insert(gf.end(), row.begin(), row.end());
+        out.flat("region_goals", gf);
+        std::printf("facade ok: %d states, %d edges, path of %zu waypoints, RRG path of %zu states (%s), %zu region "
+                    "goals\n", n, m, path.size(), task->getSolution().size(), task->getFailureReason().c_str(),
+                    gtask.getGoalStatesVector().size());
         return 0;
     } catch (const std::exception &e) {
         std::fprintf(stderr, "error: %s\n", e.what());

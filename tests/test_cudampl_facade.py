@@ -47,7 +47,7 @@ def test_facade_compiles_and_links(tmp_path):
     assert os.access(exe, os.X_OK)
 
 
-def _write_problem(path, robot, env, states, e_from, e_to, queries, start, goal, shelf):
+def _write_problem(path, robot, env, states, e_from, e_to, queries, start, goal, shelf, region):
     L = robot.num_links
     f = lambda a: " ".join("%.9g" % v for v in np.asarray(a, np.float32).ravel())
     i = lambda a: " ".join(str(int(v)) for v in np.asarray(a).ravel())
@@ -60,7 +60,8 @@ def _write_problem(path, robot, env, states, e_from, e_to, queries, start, goal,
              str(len(env.cyl_radius)), f(env.cyl_pos), f(env.cyl_rot), f(env.cyl_radius), f(env.cyl_height),
              str(len(states)), f(states[:, act]), str(len(e_from)), f(e_from[:, act]), f(e_to[:, act]),
              str(len(queries)), f(queries[:, act]), f(start[act]), f(goal[act]),
-             str(len(shelf.box_pos)), f(shelf.box_pos), f(shelf.box_min), f(shelf.box_max)]
+             str(len(shelf.box_pos)), f(shelf.box_pos), f(shelf.box_min), f(shelf.box_max),
+             str(region[0]), f(region[1]), f(region[2])]
     with open(path, "w") as fp:
         fp.write("\n".join(lines) + "\n")
 
@@ -95,8 +96,13 @@ def test_facade_matches_oracle(tmp_path):
     edge_free = lambda a, b: bool(ms.check_motions(a[None], b[None], RES, 0)[0][0])
     _, _, free = W.planning_workload(0, checker, robot=robot, env=shelf)
     start, goal = W.pick_problem(free, edge_free, 0)
+    # goal region: the last link's origin within 5 cm of where a free state puts it
+    tip = robot.num_links - 1
+    free_q = states[O.OracleModel(robot, env).check_states(states)[1] == 0][0]
+    tip_pos = W.fk_numpy(robot, free_q[None])[0][tip][:3, 3]
+    region = (tip, [*tip_pos, 0.0, 0.0, 0.0], [0.05, 0.05, 0.05, 7.0, 7.0, 7.0])
     prob, resf = tmp_path / "problem.txt", tmp_path / "results.txt"
-    _write_problem(prob, robot, env, states, e_from, e_to, queries, start, goal, shelf)
+    _write_problem(prob, robot, env, states, e_from, e_to, queries, start, goal, shelf, region)
     r = subprocess.run([exe, str(prob), str(resf)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     got = _read_results(resf)
@@ -135,6 +141,15 @@ def test_facade_matches_oracle(tmp_path):
     assert len(rrg) >= 2 and got["rrg_vertices"][0] > 4
     _check_path(ms, robot, rrg, start, goal)
     assert np.all(np.linalg.norm(np.diff(rrg, axis=0), axis=1) < 2 * RES)
+
+    # goal-region states: in the region, inside the limits, collision-free (oracle)
+    goals = got["region_goals"].astype(np.float32).reshape(-1, robot.dim)
+    assert len(goals) >= 1
+    full_g = robot.full_from_active(goals)
+    pos = m.fk(full_g.astype(np.float64), f64=True)[:, tip].reshape(-1, 4, 4)[:, :3, 3]
+    assert np.abs(pos - np.asarray(region[1][:3])).max() < 0.05 + 2e-4
+    assert np.all(full_g[:, act] >= robot.lower[act] - 1e-6) and np.all(full_g[:, act] <= robot.upper[act] + 1e-6)
+    assert np.all(m.clearance(full_g) > -BAND)
 
 
 def _check_path(ms, robot, path, start, goal):
