@@ -27,24 +27,36 @@ namespace gbmp {
 
 constexpr int kChunkCands = 64;
 constexpr int kChunkPairs = 64;
+// Warps per block of the chunk kernel.  Two blocks of 8 warps per SM at 128 registers
+// per thread: measured faster than 2 x 10 warps at 96 registers or 3 x 8 warps at 80,
+// where the chunk routine spills.
+constexpr int kChunkWarps = 8;
 
 struct ChunkScratch {
     float *lpK;       // link poses of the chunk's states [K][L*12]
     float *locK;      // joint-local transforms of the chunk's states [K][L*12]
-    float4 *sgb;      // swept group spheres (x, y, z, R) [kMaxGroups]
+    float4 *sgb;      // swept group spheres (x, y, z, R) [G]
     float *sgA;       // |c|^2 - R^2 of each swept sphere
     unsigned *cl;     // candidate obstacle indices
     unsigned *cm;     // their group masks
     int *pl;          // enabled group pairs whose swept spheres overlap (lpair indices)
 };
 
-// Per-warp shared memory of the chunk kernel: the chunk tables above plus the parts of
-// WarpScratch the per-state tests use (sphere centres, group spheres, candidates).
+// Per-warp shared memory of the chunk kernel: the link poses of the chunk, then one
+// region used twice: by the joint-local transforms while the FK runs (phase A), and
+// afterwards by the swept spheres, candidate lists and the parts of WarpScratch the
+// per-state tests use (sphere centres, group spheres, candidates).  Group arrays are
+// sized by the robot's group count.  For the 8-DOF benchmark arm this is 6.9 KB per warp
+// (11 KB without the sharing), which leaves room for larger scenes.
+__host__ __device__ inline size_t smem_chunk_rest(const DevRobot &R) {
+    return align16(sizeof(float4) * R.G) + align16(sizeof(float) * R.G) + 2 * align16(sizeof(unsigned) * kChunkCands) +
+           align16(sizeof(int) * kChunkPairs) + align16(sizeof(float4) * R.S) + align16(sizeof(float4) * R.G) +
+           align16(sizeof(float) * R.G) + 2 * align16(sizeof(int) * kWarp);
+}
+
 __host__ __device__ inline size_t smem_chunk_bytes(const DevRobot &R, int K) {
-    return 2 * align16(sizeof(float) * 12 * R.L * K) + align16(sizeof(float4) * kMaxGroups) +
-           align16(sizeof(float) * kMaxGroups) + 2 * align16(sizeof(unsigned) * kChunkCands) +
-           align16(sizeof(int) * kChunkPairs) + align16(sizeof(float4) * R.S) + align16(sizeof(float4) * kMaxGroups) + align16(sizeof(float) * kMaxGroups) +
-           2 * align16(sizeof(int) * kWarp);
+    const size_t poses = align16(sizeof(float) * 12 * R.L * K), rest = smem_chunk_rest(R);
+    return poses + (poses > rest ? poses : rest);
 }
 
 __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K, int warp, ChunkScratch &c,
@@ -52,9 +64,9 @@ __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K
     unsigned char *p = base + smem_chunk_bytes(R, K) * warp;
     size_t off = 0;
     c.lpK = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L * K);
-    c.locK = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * 12 * R.L * K);
-    c.sgb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * kMaxGroups);
-    c.sgA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * kMaxGroups);
+    c.locK = reinterpret_cast<float *>(p + off);   // shares the region carved below
+    c.sgb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.G);
+    c.sgA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * R.G);
     c.cl = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
     c.cm = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
     c.pl = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * kChunkPairs);
@@ -62,8 +74,8 @@ __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K
     w.loc = nullptr;
     w.q = nullptr;
     w.cen = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.S);
-    w.gb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * kMaxGroups);
-    w.gA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * kMaxGroups);
+    w.gb = reinterpret_cast<float4 *>(p + off); off += align16(sizeof(float4) * R.G);
+    w.gA = reinterpret_cast<float *>(p + off); off += align16(sizeof(float) * R.G);
     w.cand = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * kWarp);
     w.cmask = reinterpret_cast<unsigned *>(p + off);
 }
@@ -146,11 +158,11 @@ __device__ __forceinline__ unsigned run_groups(const float4 *runs, int nruns, in
 // cylinder candidates; `need` holds the groups any candidate or listed group pair
 // involves (spheres of other groups cannot collide in this chunk and are not placed);
 // npr group pairs are listed in cs.pl unless pairs_overflow.
-template <int SPL>
+template <int SPL, bool CNT>
 __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                    const ChunkScratch &cs, const float *lp, int ns_end, int nb_end, int nc_end,
                                    unsigned need, int npr, bool pairs_overflow, int lane, unsigned long long &fl) {
-    const bool count = R.work != nullptr;
+    constexpr bool count = CNT;   // executed-work accounting compiled in only when asked for
     float cx[SPL], cy[SPL], cz[SPL], cr[SPL], A[SPL];
     unsigned gbit[SPL];
 #pragma unroll
@@ -317,13 +329,13 @@ __device__ __noinline__ bool chunk_fallback(const SmemTables &t, const DevRobot 
 // States [s0, s1) of one edge (from f to t with per-state step d, n states in all).
 // Returns the first colliding state, or -1 (also when another warp already recorded
 // a hit below the state reached).
-template <int SPL, int K>
+template <int SPL, int K, bool CNT>
 __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                       const ChunkScratch &cs, int lane, const float *__restrict__ f,
                                       const float *__restrict__ to, const float *__restrict__ d, int s0, int s1,
                                       int n, const int *first_hit) {
     const int ks = s1 - s0;
-    const bool count = R.work != nullptr;
+    constexpr bool count = CNT;   // executed-work accounting compiled in only when asked for
     // FK and the group-centre transforms of every state; sphere placements are counted
     // where they happen
     unsigned long long fl = (unsigned long long)(R.base_flops - 24LL * R.S) * ks;
@@ -494,7 +506,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
         if (overflow) {
             hit = chunk_fallback<SPL>(t, R, E, w, lp, lane);
         } else {
-            hit = chunk_state<SPL>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, lane, fl);
+            hit = chunk_state<SPL, CNT>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, lane, fl);
         }
         __syncwarp();
         if (hit) {
@@ -511,8 +523,8 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
 
 // One wave of edge validation by chunks: states [b0, b1) of every live edge, K per task,
 // chunk-major order so that lower chunks of an edge are examined first.
-template <int SPL, int K>
-__global__ void __launch_bounds__(kWarpsPerBlock *kWarp, 2)
+template <int SPL, int K, bool CNT>
+__global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
     k_edge_chunk(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
                  const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
                  const int *__restrict__ live, const int *__restrict__ live_count, int b0, int b1) {
@@ -529,8 +541,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, 2)
     const long long count = *live_count;
     const int nch = (b1 - b0 + K - 1) / K;
     const long long tasks = count * (long long)nch;
-    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
-    for (long long task = blockIdx.x * (long long)kWarpsPerBlock + warp; task < tasks; task += nw) {
+    const long long nw = (long long)gridDim.x * kChunkWarps;
+    for (long long task = blockIdx.x * (long long)kChunkWarps + warp; task < tasks; task += nw) {
         const int c = (int)(task / count);
         const int e = live[task % count];
         const int n = nsteps[e];
@@ -542,7 +554,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, 2)
         known = __shfl_sync(kFull, known, 0);
         if (known < s0) continue;
         const long long off = (long long)e * R.L;
-        const int h = warp_edge_chunk<SPL, K>(t, R, E, w, cs, lane, from + off, to + off, dir + off, s0, s1, n,
+        const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, s0, s1, n,
                                               first_hit + e);
         if (h >= 0 && lane == 0) atomicMin(first_hit + e, h);
         __syncwarp();
@@ -590,19 +602,19 @@ int edge_chunk_states(const DevRobot &R) {
 }
 
 gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid) {
-    *smem = smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) + smem_chunk_bytes(R, K) * kWarpsPerBlock;
+    *smem = smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) + smem_chunk_bytes(R, K) * kChunkWarps;
     gbmp_status st = GBMP_OK;
     GBMP_CHUNK_SWITCH(R.spl, K, {
-        const void *fn = (const void *)k_edge_chunk<SPL, KK>;
-        static thread_local bool configured = false;
-        if (!configured) {
+        const void *fn = R.work ? (const void *)k_edge_chunk<SPL, KK, true> : (const void *)k_edge_chunk<SPL, KK, false>;
+        static thread_local bool configured[2] = {false, false};
+        if (!configured[R.work != nullptr]) {
             GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
                                            cudaSharedmemCarveoutMaxShared));
-            configured = true;
+            configured[R.work != nullptr] = true;
         }
         int per_sm = 0;
-        GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kWarpsPerBlock * kWarp, *smem));
+        GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kChunkWarps * kWarp, *smem));
         if (per_sm < 1) {
             set_error("chunked edge kernel does not fit on an SM (%zu bytes of shared memory)", *smem);
             st = GBMP_ERR_CAPACITY;
@@ -616,8 +628,12 @@ gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int gri
                               const float *from, const float *to, const int *nsteps, const float *dir,
                               int *first_hit, const int *live, const int *live_count, int b0, int b1) {
     GBMP_CHUNK_SWITCH(R.spl, K, {
-        k_edge_chunk<SPL, KK><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(R, E, from, to, nsteps, dir, first_hit,
-                                                                          live, live_count, b0, b1);
+        if (R.work)
+            k_edge_chunk<SPL, KK, true><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir,
+                                                                                first_hit, live, live_count, b0, b1);
+        else
+            k_edge_chunk<SPL, KK, false><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir,
+                                                                                 first_hit, live, live_count, b0, b1);
     });
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
