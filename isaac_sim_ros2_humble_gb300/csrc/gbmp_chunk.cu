@@ -495,7 +495,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     const int kend = (need == 0u && !overflow) ? 0 : ks;   // nothing near any state: all free
     for (int k = 0; k < kend; ++k) {
         const int s = s0 + k;
-        if (k > 0) {
+        if (k == 4) {   // once per chunk: stop if another warp found an earlier hit on this edge
             int known = 0;
             if (lane == 0) known = *(volatile const int *)first_hit;
             known = __shfl_sync(kFull, known, 0);
