@@ -343,16 +343,26 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     // --- A: FK of every state, box of each group centre ---
     const bool gl = lane < R.G;
     const float4 g = gl ? t.grp[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int glk = gl ? t.glink[lane] : 0;
     float lox = 3.0e38f, loy = 3.0e38f, loz = 3.0e38f, hix = -3.0e38f, hiy = -3.0e38f, hiz = -3.0e38f;
     warp_fk_chunk<K>(t, R.L, ks, f, to, d, s0, n, cs.locK, cs.lpK, lane);
-    for (int k = 0; k < ks; ++k) {
-        if (gl) {
-            const float3 c = xform_point(cs.lpK + k * 12 * R.L + 12 * glk, g.x, g.y, g.z);
+    // group centres of every (state, group) pair, spread over the lanes, into the region
+    // the joint-local transforms used (dead now; ks x G float4 fit in it since G <= L)
+    float4 *gc = reinterpret_cast<float4 *>(cs.locK);
+    for (int p = lane; p < ks * R.G; p += kWarp) {
+        const int k = p / R.G, q = p - k * R.G;
+        const float4 gq = t.grp[q];
+        const float3 c = xform_point(cs.lpK + k * 12 * R.L + 12 * t.glink[q], gq.x, gq.y, gq.z);
+        gc[p] = make_float4(c.x, c.y, c.z, 0.f);
+    }
+    __syncwarp();
+    if (gl) {
+        for (int k = 0; k < ks; ++k) {
+            const float4 c = gc[k * R.G + lane];
             lox = fminf(lox, c.x); loy = fminf(loy, c.y); loz = fminf(loz, c.z);
             hix = fmaxf(hix, c.x); hiy = fmaxf(hiy, c.y); hiz = fmaxf(hiz, c.z);
         }
     }
+    __syncwarp();   // the swept spheres below overwrite the start of that region
 
     // --- B: swept group spheres ---
     if (gl) {
