@@ -375,106 +375,84 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     __syncwarp();
 
     // --- C: broad phase of the chunk, run spheres first ---
-    // Lane j tests run c0 + j's bounding sphere against every swept group sphere; only
-    // runs some group touches are visited, and their obstacles are tested only against
-    // the groups that touched the run.
-    int nc = 0;
+    // The bounding spheres of all runs (sphere runs, then box runs, then cylinder runs)
+    // are tested in one pass, lane j taking run c0 + j against every swept group sphere;
+    // only runs some group touches are visited, in run order (so the candidates come out
+    // grouped by obstacle type), and their obstacles are tested only against the groups
+    // that touched the run.
+    int nc = 0, nsph = 0, nbox = 0;
     unsigned need = 0u;
-    const float4 *runs_s = t.env + env_cluster_base(E.ns, E.nb, E.nc);
     const float4 *sx = t.env + E.ns + 5 * E.nb + 4 * E.nc;
     const float *snb = reinterpret_cast<const float *>(sx + E.ns);
-    const int nrs = env_clusters(E.ns);
-#pragma unroll 1
-    for (int c0 = 0; c0 < nrs; c0 += kWarp) {
-        const unsigned gmc = run_groups(runs_s, nrs, c0, cs, R.G, lane);
-        unsigned runs = __ballot_sync(kFull, gmc != 0u);
-        if (count) fl += (unsigned long long)min(kWarp, nrs - c0) * R.G * kFlGroupPair;
-        while (runs) {
-            const int j = __ffs(runs) - 1;
-            runs &= runs - 1u;
-            const unsigned gm = __shfl_sync(kFull, gmc, j);
-            const int o = (c0 + j) * kWarp + lane;
-            unsigned mask = 0u;
-            if (o < E.ns) {
-                const float4 b = sx[o];
-                const float nb = snb[o];
-                for (unsigned m = gm; m; m &= m - 1u) {
-                    const int q = __ffs(m) - 1;
-                    const float4 gs = cs.sgb[q];
-                    const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
-                    if (v > cs.sgA[q]) mask |= 1u << q;
-                }
-            }
-            nc = push_cand(cs, nc, (unsigned)o, mask, lane);
-            need |= mask;
-            if (count) fl += (unsigned long long)min(kWarp, E.ns - (c0 + j) * kWarp) * __popc(gm) * kFlSphereX;
-        }
-    }
-    const int ns_end = nc;
     const float4 *bx = t.env + E.ns;
-    const int nrb = env_clusters(E.nb);
-    const float4 *runs_b = runs_s + nrs;
-#pragma unroll 1
-    for (int c0 = 0; c0 < nrb; c0 += kWarp) {
-        const unsigned gmc = run_groups(runs_b, nrb, c0, cs, R.G, lane);
-        unsigned runs = __ballot_sync(kFull, gmc != 0u);
-        if (count) fl += (unsigned long long)min(kWarp, nrb - c0) * R.G * kFlGroupPair;
-        while (runs) {
-            const int j = __ffs(runs) - 1;
-            runs &= runs - 1u;
-            const unsigned gm = __shfl_sync(kFull, gmc, j);
-            const int o = (c0 + j) * kWarp + lane;
-            unsigned mask = 0u;
-            if (o < E.nb) {
-                const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
-                for (unsigned m = gm; m; m &= m - 1u) {
-                    const int q = __ffs(m) - 1;
-                    const float4 gs = cs.sgb[q];
-                    const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
-                    const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
-                    const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
-                    const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
-                    if (sq3(dx, dy, dz) < gs.w * gs.w) mask |= 1u << q;
-                }
-            }
-            nc = push_cand(cs, nc, (unsigned)o, mask, lane);
-            need |= mask;
-            if (count) fl += (unsigned long long)min(kWarp, E.nb - (c0 + j) * kWarp) * __popc(gm) * kFlCuboid;
-        }
-    }
-    const int nb_end = nc;
     const float4 *cyl = t.env + E.ns + 5 * E.nb;
-    const int nrc = env_clusters(E.nc);
-    const float4 *runs_c = runs_b + nrb;
+    const int nrs = env_clusters(E.ns), nrb = env_clusters(E.nb), nrun = nrs + nrb + env_clusters(E.nc);
+    const float4 *runs_w = t.env + env_cluster_base(E.ns, E.nb, E.nc);
 #pragma unroll 1
-    for (int c0 = 0; c0 < nrc; c0 += kWarp) {
-        const unsigned gmc = run_groups(runs_c, nrc, c0, cs, R.G, lane);
+    for (int c0 = 0; c0 < nrun; c0 += kWarp) {
+        const unsigned gmc = run_groups(runs_w, nrun, c0, cs, R.G, lane);
         unsigned runs = __ballot_sync(kFull, gmc != 0u);
-        if (count) fl += (unsigned long long)min(kWarp, nrc - c0) * R.G * kFlGroupPair;
+        if (count) fl += (unsigned long long)min(kWarp, nrun - c0) * R.G * kFlGroupPair;
         while (runs) {
             const int j = __ffs(runs) - 1;
             runs &= runs - 1u;
             const unsigned gm = __shfl_sync(kFull, gmc, j);
-            const int o = (c0 + j) * kWarp + lane;
+            const int c = c0 + j;
             unsigned mask = 0u;
-            if (o < E.nc) {
-                const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
-                for (unsigned m = gm; m; m &= m - 1u) {
-                    const int q = __ffs(m) - 1;
-                    const float4 gs = cs.sgb[q];
-                    const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
-                    const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
-                    const float dz = fabsf(l.z) - pr.y;
-                    const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
-                    const float sdf = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox))) + fminf(fmaxf(dx, dz), 0.f);
-                    if (gs.w - sdf > 0.f) mask |= 1u << q;
+            int o;
+            if (c < nrs) {   // obstacle spheres (expanded form, see warp_collide)
+                o = c * kWarp + lane;
+                if (o < E.ns) {
+                    const float4 b = sx[o];
+                    const float nb = snb[o];
+                    for (unsigned m = gm; m; m &= m - 1u) {
+                        const int q = __ffs(m) - 1;
+                        const float4 gs = cs.sgb[q];
+                        const float v = __fmaf_rn(gs.x, b.x, __fmaf_rn(gs.y, b.y, __fmaf_rn(gs.z, b.z, __fmaf_rn(gs.w, b.w, nb))));
+                        if (v > cs.sgA[q]) mask |= 1u << q;
+                    }
                 }
+                if (count) fl += (unsigned long long)min(kWarp, E.ns - c * kWarp) * __popc(gm) * kFlSphereX;
+            } else if (c < nrs + nrb) {   // cuboids
+                o = (c - nrs) * kWarp + lane;
+                if (o < E.nb) {
+                    const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
+                    for (unsigned m = gm; m; m &= m - 1u) {
+                        const int q = __ffs(m) - 1;
+                        const float4 gs = cs.sgb[q];
+                        const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                        const float dx = l.x - fminf(fmaxf(l.x, mn.x), mx.x);
+                        const float dy = l.y - fminf(fmaxf(l.y, mn.y), mx.y);
+                        const float dz = l.z - fminf(fmaxf(l.z, mn.z), mx.z);
+                        if (sq3(dx, dy, dz) < gs.w * gs.w) mask |= 1u << q;
+                    }
+                }
+                if (count) fl += (unsigned long long)min(kWarp, E.nb - (c - nrs) * kWarp) * __popc(gm) * kFlCuboid;
+            } else {   // cylinders
+                o = (c - nrs - nrb) * kWarp + lane;
+                if (o < E.nc) {
+                    const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
+                    for (unsigned m = gm; m; m &= m - 1u) {
+                        const int q = __ffs(m) - 1;
+                        const float4 gs = cs.sgb[q];
+                        const float3 l = xform_rows(r0, r1, r2, gs.x, gs.y, gs.z);
+                        const float dx = sqrtf(__fmaf_rn(l.y, l.y, __fmul_rn(l.x, l.x))) - pr.x;
+                        const float dz = fabsf(l.z) - pr.y;
+                        const float ox = dx > 0.f ? dx : 0.f, oz = dz > 0.f ? dz : 0.f;
+                        const float sdf = sqrtf(__fmaf_rn(oz, oz, __fmul_rn(ox, ox))) + fminf(fmaxf(dx, dz), 0.f);
+                        if (gs.w - sdf > 0.f) mask |= 1u << q;
+                    }
+                }
+                if (count) fl += (unsigned long long)min(kWarp, E.nc - (c - nrs - nrb) * kWarp) * __popc(gm) * kFlCylinder;
             }
+            const int before = nc;
             nc = push_cand(cs, nc, (unsigned)o, mask, lane);
             need |= mask;
-            if (count) fl += (unsigned long long)min(kWarp, E.nc - (c0 + j) * kWarp) * __popc(gm) * kFlCylinder;
+            if (c < nrs) nsph += nc - before;
+            else if (c < nrs + nrb) nbox += nc - before;
         }
     }
+    const int ns_end = nsph, nb_end = nsph + nbox;
     // enabled group pairs whose swept spheres overlap
     int npr = 0;
     for (int k0 = 0; k0 < R.NPL; k0 += kWarp) {
