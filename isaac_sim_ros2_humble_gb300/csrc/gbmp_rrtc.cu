@@ -62,25 +62,89 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
+// Squared active-joint distance of one node (NW float4 words) from the query held in
+// registers, accumulated joint by joint in index order; inactive joints add exactly 0.
+// `written` clears if any coordinate still holds the NaN sentinel.
+template <int NW>
+__device__ __forceinline__ float node_dist(const float4 *__restrict__ y, const float (&qr)[4 * NW], unsigned am, int L,
+                                           bool &written) {
+    float4 v4[NW];
+#pragma unroll
+    for (int k = 0; k < NW; ++k) v4[k] = __ldcg(y + k);
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+        const float v[4] = {v4[k].x, v4[k].y, v4[k].z, v4[k].w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int j = 4 * k + c;
+            if (j < L) {
+                written &= v[c] == v[c];
+                const float d = ((am >> j) & 1u) ? __fadd_rn(qr[j], -v[c]) : 0.f;
+                s = __fmaf_rn(d, d, s);
+            }
+        }
+    }
+    return s;
+}
+
+// Per-thread part of the nearest-node scan for trees of at most 4 * NW joints: nodes as
+// float4 words, two nodes per step (the second clamped to the last node, so both loads
+// are always issued).
+template <int NW>
+__device__ __forceinline__ void scan_nearest(const float *__restrict__ nodes, int size, int stride, int L,
+                                             const unsigned char *act, const float *q, float &best, int &bi) {
+    float qr[4 * NW];
+    unsigned am = 0u;
+#pragma unroll
+    for (int j = 0; j < 4 * NW; ++j) {
+        qr[j] = j < L ? q[j] : 0.f;
+        if (j < L && act[j]) am |= 1u << j;
+    }
+    const int bd = blockDim.x;
+    for (int i = threadIdx.x; i < size; i += 2 * bd) {
+        const int i2 = i + bd;
+        bool w1 = true, w2 = i2 < size;
+        const float s1 = node_dist<NW>(reinterpret_cast<const float4 *>(nodes + (long long)i * stride), qr, am, L, w1);
+        const float s2 =
+            node_dist<NW>(reinterpret_cast<const float4 *>(nodes + (long long)min(i2, size - 1) * stride), qr, am, L, w2);
+        if (w1 && (s1 < best || (s1 == best && i < bi))) { best = s1; bi = i; }
+        if (w2 && (s2 < best || (s2 == best && i2 < bi))) { best = s2; bi = i2; }
+    }
+}
+
 // Block-wide argmin of the squared active-joint distance from q to the written nodes
-// of one tree.  Returns the node index (or -1) to every thread.
+// of one tree (ties to the lower index).  Returns the node index (or -1) to every
+// thread.  Trees of up to 16 joints (stride a multiple of 4, 16-byte aligned) are read
+// as float4 words with the query in registers; longer chains coordinate by coordinate.
 __device__ int block_nearest(const float *__restrict__ nodes, int size, int stride, int L,
                              const unsigned char *act, const float *q, float *s_d, int *s_i) {
     float best = __int_as_float(0x7f800000);
     int bi = INT_MAX;
-    for (int i = threadIdx.x; i < size; i += blockDim.x) {
-        const float *y = nodes + (long long)i * stride;
-        float s = 0.f;
-        bool written = true;
-        for (int j = 0; j < L; ++j) {
-            const float v = __ldcg(y + j);
-            written &= v == v;
-            if (act[j]) {
-                const float d = __fadd_rn(q[j], -v);
-                s = __fmaf_rn(d, d, s);
+    const bool vec = (stride & 3) == 0 && (reinterpret_cast<unsigned long long>(nodes) & 15ull) == 0 && L <= 16;
+    if (vec && L <= 4) {
+        scan_nearest<1>(nodes, size, stride, L, act, q, best, bi);
+    } else if (vec && L <= 8) {
+        scan_nearest<2>(nodes, size, stride, L, act, q, best, bi);
+    } else if (vec && L <= 12) {
+        scan_nearest<3>(nodes, size, stride, L, act, q, best, bi);
+    } else if (vec) {
+        scan_nearest<4>(nodes, size, stride, L, act, q, best, bi);
+    } else {
+        for (int i = threadIdx.x; i < size; i += blockDim.x) {
+            const float *y = nodes + (long long)i * stride;
+            float s = 0.f;
+            bool written = true;
+            for (int j = 0; j < L; ++j) {
+                const float v = __ldcg(y + j);
+                written &= v == v;
+                if (act[j]) {
+                    const float d = __fadd_rn(q[j], -v);
+                    s = __fmaf_rn(d, d, s);
+                }
             }
+            if (written && (s < best || (s == best && i < bi))) { best = s; bi = i; }
         }
-        if (written && (s < best || (s == best && i < bi))) { best = s; bi = i; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -355,7 +419,7 @@ struct BatchProblem {
     RrtcDev P;
     unsigned long long seed;
     const float *start, *goal;      // device copies of the roots
-    int prev[2];                    // slots used by the previous solve (to reset)
+    int prev[2];                    // node words the previous solve wrote (to reset)
 };
 
 // Batched planning: block b serves problem b % n as lane b / n, so every problem gets
@@ -422,7 +486,8 @@ __global__ void k_rrtc_batch_reset(BatchProblem *__restrict__ probs, int n, unsi
     BatchProblem &b = probs[p];
     const int L = b.R.L;
     for (int t = 0; t < 2; ++t) {
-        const long long words = (long long)max(b.prev[t], 1) * b.P.stride;
+        // the words the previous solve of this slot wrote (its stride may differ)
+        const long long words = max((long long)b.prev[t], (long long)b.P.stride);
         for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < words;
              i += (long long)gridDim.x * blockDim.x)
             b.P.nodes[t][i] = __int_as_float(0xffffffff);
@@ -443,12 +508,12 @@ __global__ void k_rrtc_batch_reset(BatchProblem *__restrict__ probs, int n, unsi
     }
 }
 
-// Record the used slots for the next reset.
+// Record the node words used, for the next reset.
 __global__ void k_rrtc_batch_finish(BatchProblem *__restrict__ probs, int n) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    probs[p].prev[0] = min(probs[p].P.size[0], probs[p].P.cap);
-    probs[p].prev[1] = min(probs[p].P.size[1], probs[p].P.cap);
+    probs[p].prev[0] = min(probs[p].P.size[0], probs[p].P.cap) * probs[p].P.stride;
+    probs[p].prev[1] = min(probs[p].P.size[1], probs[p].P.cap) * probs[p].P.stride;
 }
 
 __global__ void k_read_clock(unsigned long long *t) {
@@ -888,7 +953,7 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
         bp.P.path_len = ints + 16;
         bp.P.path = (float *)(base + 2 * nodes_b + 2 * par_b + 256);
         bp.P.cap = b->cap;
-        bp.P.stride = b->stride;
+        bp.P.stride = (pr.robot->L + 3) & ~3;   // its own joints, padded to float4 words
         bp.P.path_cap = b->path_cap;
         bp.P.flag = b->d_flags + i;
         bp.seed = pr.seed;
@@ -984,8 +1049,8 @@ gbmp_status batch_end(gbmp_batch_planner b, const gbmp_rrtc_problem *problems, g
         r.goal_tree_size = o[3];
         r.iterations = o[4];
         r.kernel_ms = ms;
-        b->prev[2 * i] = std::max(o[2], 1);
-        b->prev[2 * i + 1] = std::max(o[3], 1);
+        b->prev[2 * i] = std::max(o[2], 1) * b->h_table[i].P.stride;
+        b->prev[2 * i + 1] = std::max(o[3], 1) * b->h_table[i].P.stride;
         max_len = std::max(max_len, r.path_len);
     }
     if (h_paths && max_len > 0) {
