@@ -20,6 +20,7 @@ no collective on the data path); the step time is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -46,7 +47,7 @@ CPU_SAMPLE_EDGES = 1536
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
     ap.add_argument("--edges", type=int, default=65536)
@@ -83,8 +84,11 @@ def reduce_over_ranks(dist, ws, device, timed_s, checks, e2e_s):
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region:
+    sampling starts (and its first sample is awaited) before the region, every sample
+    carries its time stamp, and only the samples inside the region are summarised (all
+    of them if none fell inside)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -99,10 +103,27 @@ class ClockSampler:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
+        self.t_begin = self.t_end = None
+
+    def mark_begin(self):
+        self.t_begin = time.time()
+
+    def mark_end(self):
+        self.t_end = time.time()
+
+    @staticmethod
+    def _stamp(text):
+        try:
+            return datetime.datetime.strptime(text.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
 
     def stop(self):
         if self.proc is None:
@@ -116,17 +137,25 @@ class ClockSampler:
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
+            if len(parts) >= 10:
                 rows.append(parts)
         os.unlink(self.path)
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside, in_region = rows, False
+        if self.t_begin is not None and self.t_end is not None:
+            # a sample stamped up to one period after the region still describes it
+            sel = [r for r in rows if (lambda t: t is not None and self.t_begin <= t <= self.t_end + 0.05)(
+                self._stamp(r[0]))]
+            if sel:
+                inside, in_region = sel, True
+        sm = [float(r[2]) for r in inside if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in inside if r[3].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        reasons = sorted({names[i] for r in inside for i in range(4) if r[6 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(rows), "reasons": reasons}
+                "samples": len(inside), "samples_in_region": in_region,
+                "reasons": reasons}
 
 
 def run_reference(args):
@@ -541,6 +570,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     clk.start()
+    clk.mark_begin()
     _lib.profile_enable(True)
     for i in range(args.steps):
         flush.fill_(float(i))
@@ -548,6 +578,7 @@ def main():
         step()
         ev[i][1].record(stream)
     torch.cuda.synchronize()
+    clk.mark_end()
     _lib.profile_enable(False)
     if ws > 1:
         dist.barrier()
