@@ -200,6 +200,13 @@ GBMP_API gbmp_status gbmp_nearest(gbmp_robot robot, const float *d_tree, int64_t
 GBMP_API gbmp_status gbmp_steer(gbmp_robot robot, const float *d_from, const int32_t *d_idx, float *d_to,
                        int64_t n, float max_distance, void *stream);
 
+/* Gather of stored states by index, replacing SingleArmStateManager::get_states
+ * (SingleArmStates.cu:1433-1453, one cudaMemcpy per index there): d_dst[k] = d_src[d_idx[k]]
+ * for k < n, rows of L floats, one launch.  An index outside [0, M) gives a row of NaN
+ * and sets *d_bad to 1 when d_bad is not NULL (d_bad is only ever set, never cleared). */
+GBMP_API gbmp_status gbmp_gather_states(int32_t L, const float *d_src, int64_t M, const int32_t *d_idx, int64_t n,
+                               float *d_dst, int32_t *d_bad, void *stream);
+
 /* Uniform samples within the joint limits, inactive joints at their defaults, replacing
  * SingleArmSpace::sample / sampleConfigurations (SingleArmSpace.cu:184-217, :251-403).
  * Counter-based Philox4x32-10: sample k, joint j uses counter (offset + k, j) and key seed,

@@ -694,13 +694,18 @@ class SingleArmStateManager {
         }
     }
 
+    // Gather by index (SingleArmStates.cu:1433-1453): one index upload and one gather
+    // launch instead of a copy per index.
     BaseStatesPtr get_states(const std::vector<int> &states_index) {
         auto st = std::make_shared<SingleArmStates>((int)states_index.size(), space_);
-        for (size_t i = 0; i < states_index.size(); ++i) {
-            if (states_index[i] < 0 || states_index[i] >= n_) throw std::runtime_error("state index out of range");
-            cudaMemcpy(st->getJointStatesCuda() + i * L_, static_cast<float *>(buf_->p) + (size_t)states_index[i] * L_,
-                       sizeof(float) * L_, cudaMemcpyDeviceToDevice);
-        }
+        if (states_index.empty()) return st;
+        for (int i : states_index)
+            if (i < 0 || i >= n_) throw std::runtime_error("state index out of range");
+        detail::DevArray idx(sizeof(int) * states_index.size());
+        cudaMemcpy(idx.p, states_index.data(), idx.bytes, cudaMemcpyHostToDevice);
+        detail::check(gbmp_gather_states(L_, static_cast<float *>(buf_->p), n_, static_cast<int *>(idx.p),
+                                         (int64_t)states_index.size(), st->getJointStatesCuda(), nullptr, nullptr));
+        cudaDeviceSynchronize();
         return st;
     }
 

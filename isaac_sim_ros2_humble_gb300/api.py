@@ -163,6 +163,14 @@ def steer(robot: Robot, q_from, q_to, max_distance: float, idx=None, stream=None
                                  stream_handle(stream)))
 
 
+def gather_states(src, idx, out, bad=None, stream=None):
+    """out[k] = src[idx[k]] (rows of src.shape[1] floats) in one launch; an index outside
+    the rows gives a NaN row and sets bad[0] to 1 (bad: int32 device tensor or None)."""
+    L = int(src.shape[1])
+    check(_lib.load().gbmp_gather_states(L, ptr(src), int(src.shape[0]), ptr(idx), int(idx.shape[0]), ptr(out),
+                                         ptr(bad), stream_handle(stream)))
+
+
 def sample(robot: Robot, seed: int, offset: int, out, stream=None):
     n = _n(out, robot.L)
     check(_lib.load().gbmp_sample(robot.handle, seed, offset, n, ptr(out), stream_handle(stream)))

@@ -66,6 +66,22 @@ __global__ void k_steer(const float *__restrict__ from, const int *__restrict__ 
     }
 }
 
+// Gather rows of L floats by index, one thread per output element (coalesced stores).
+__global__ void k_gather_states(const float *__restrict__ src, long long M, const int *__restrict__ idx, long long n,
+                                int L, float *__restrict__ dst, int *__restrict__ bad) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= n * L) return;
+    const long long k = e / L;
+    const int j = (int)(e - k * L);
+    const int i = idx[k];
+    if (i >= 0 && i < M) {
+        dst[e] = src[(long long)i * L + j];
+    } else {
+        dst[e] = __int_as_float(0x7fffffff);
+        if (bad && j == 0) *bad = 1;
+    }
+}
+
 // Uniform sample in [lower, upper) per active joint, default value otherwise.
 __global__ void k_sample(DevRobot R, unsigned long long seed, unsigned long long offset, long long n,
                          float *__restrict__ q) {
@@ -116,6 +132,23 @@ gbmp_status gbmp_steer(gbmp_robot r, const float *d_from, const int32_t *d_idx, 
     const unsigned blocks = (unsigned)((n + 255) / 256);
     ProfScope ps(GBMP_PROF_OTHER, (cudaStream_t)stream);
     k_steer<<<blocks, 256, 0, (cudaStream_t)stream>>>(d_from, d_idx, d_to, n, r->L, max_distance);
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_gather_states(int32_t L, const float *d_src, int64_t M, const int32_t *d_idx, int64_t n,
+                               float *d_dst, int32_t *d_bad, void *stream) {
+    GBMP_CHECK_ARG(L >= 1, "L < 1");
+    GBMP_CHECK_ARG(M >= 0 && n >= 0, "negative count");
+    GBMP_CHECK_ARG(n <= (1LL << 40) / L, "n too large");
+    if (n == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_idx && d_dst, "idx/dst is NULL");
+    GBMP_CHECK_ARG(d_src || M == 0, "src is NULL");
+    const long long total = n * (long long)L;
+    const unsigned long long blocks = (unsigned long long)((total + 255) / 256);
+    GBMP_CHECK_ARG(blocks <= 0x7fffffffull, "n too large");
+    ProfScope ps(GBMP_PROF_OTHER, (cudaStream_t)stream);
+    k_gather_states<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(d_src, M, d_idx, n, L, d_dst, d_bad);
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
 }

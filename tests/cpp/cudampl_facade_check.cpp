@@ -164,6 +164,18 @@ int main(int argc, char **argv) {
         for (auto &r : nbr) nn.push_back(r[0]);
         out.flat("nearest", nn);
 
+        // ---- state manager: gather by index (get_states), unordered and repeated ----
+        std::vector<int> pos, pick;
+        for (int k = (int)idx.size() - 1; k >= 0; k -= 3) pos.push_back(k);
+        pos.push_back(0);
+        pos.push_back(0);
+        for (int k : pos) pick.push_back(idx[k]);
+        auto gathered = mgr->get_states(pick)->getJointStatesFullHost();
+        auto stored = st->getJointStatesFullHost();
+        std::vector<int> gather_ok{(int)(gathered.size() == pos.size())};
+        for (size_t k = 0; gather_ok[0] && k < pos.size(); ++k) gather_ok[0] = gathered[k] == stored[pos[k]];
+        out.flat("gather_ok", gather_ok);
+
         // ---- CPRRTC::RobotSolver in the shelf scene ----
         std::vector<MiniVec3> spos_v(S);
         for (int k = 0; k < S; ++k)

@@ -129,6 +129,7 @@ def test_facade_matches_oracle(tmp_path):
 
     np.testing.assert_array_equal(got["sample"].astype(np.float32).reshape(64, L), O.sample(robot, 0x5EED, 0, 64))
     np.testing.assert_array_equal(got["nearest"].astype(np.int32), O.nearest(states, queries, active=robot.active))
+    assert int(got["gather_ok"][0]) == 1   # get_states rows equal the stored rows bit for bit
 
     path = got["path"].astype(np.float32).reshape(-1, robot.dim)
     assert len(path) >= 2

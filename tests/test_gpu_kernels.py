@@ -190,6 +190,33 @@ def test_steer_bit_exact(edge):
     np.testing.assert_array_equal(to.cpu().numpy(), O.steer(qf, qt, 0.5))
 
 
+def test_gather_states_exact(edge):
+    """SingleArmStateManager::get_states as one gather launch: rows copied bit for bit,
+    repeated and unordered indices included; an index outside the rows gives a NaN row
+    and raises the flag without touching memory outside the source."""
+    robot, env, qf, qt, m, R, E = edge
+    M = len(qf)
+    src = dev(qf)
+    rng = np.random.default_rng(3)
+    idx = rng.integers(0, M, size=777).astype(np.int32)
+    idx[:5] = [M - 1, 0, 0, 17, M - 1]
+    out = torch.zeros((777, robot.num_links), device="cuda")
+    bad = torch.zeros(1, dtype=torch.int32, device="cuda")
+    api.gather_states(src, torch.from_numpy(idx).cuda(), out, bad)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), qf[idx])
+    assert int(bad.item()) == 0
+    idx2 = np.array([3, -1, M, 2], np.int32)
+    out2 = torch.zeros((4, robot.num_links), device="cuda")
+    api.gather_states(src, torch.from_numpy(idx2).cuda(), out2, bad)
+    torch.cuda.synchronize()
+    o = out2.cpu().numpy()
+    np.testing.assert_array_equal(o[[0, 3]], qf[[3, 2]])
+    assert np.isnan(o[1]).all() and np.isnan(o[2]).all()
+    assert int(bad.item()) == 1
+    api.gather_states(src, torch.from_numpy(idx2[:0]).cuda(), out2[:0])   # nothing to do
+
+
 def test_sample_bit_exact(edge):
     robot, env, qf, qt, m, R, E = edge
     out = torch.zeros((1000, robot.num_links), device="cuda")
