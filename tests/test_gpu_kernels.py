@@ -246,3 +246,42 @@ def test_many_links_uses_full_path():
     torch.cuda.synchronize()
     _edge_parity(m, qf, qt, 0.05, 1, ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(),
                  ns.cpu().numpy())
+
+
+def _run_edges(R, E, qf, qt, res, rule):
+    n = qf.shape[0]
+    ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    fh = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(n, device="cuda")
+    ns = torch.zeros(n, dtype=torch.int32, device="cuda")
+    api.check_edges(R, E, dev(qf), dev(qt), res, rule, ok, fh, ln, ns)
+    torch.cuda.synchronize()
+    return ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(), ns.cpu().numpy()
+
+
+@pytest.mark.parametrize("kinds", [(0, 0, 0), (48, 0, 0), (0, 24, 0), (0, 0, 12), (40, 0, 9), (0, 20, 6)])
+def test_check_edges_obstacle_type_mixes(edge, kinds):
+    """The chunked edge kernel's broad phase walks the obstacle runs of every type in one
+    pass; scenes with some types absent (or none at all) take the same pass."""
+    robot, _, qf, qt, _, R, _ = edge
+    ns_, nb_, nc_ = kinds
+    env = W.Environment.empty() if not any(kinds) else W.random_env(40 + sum(kinds), ns_, nb_, nc_, oriented=True)
+    m = O.OracleModel(robot, env)
+    E = api.Env(env)
+    ok, fh, ln, ns = _run_edges(R, E, qf[:256], qt[:256], 0.02, 1)
+    _edge_parity(m, qf[:256], qt[:256], 0.02, 1, ok, fh, ln, ns)
+
+
+def test_check_edges_full_size_sampled_parity():
+    """The benchmark call itself (65,536 edges, at most 0.01 rad per joint between states):
+    state counts and lengths match the oracle on every edge of a seeded sample of 384,
+    first hits match outside the clearance band, and the verdict is the first-hit flag."""
+    robot, env, qf, qt = W.edge_workload()
+    R, E = api.Robot(robot), api.Env(env)
+    ok, fh, ln, ns = _run_edges(R, E, qf, qt, 0.01, 1)
+    assert len(ok) == 65536
+    np.testing.assert_array_equal(ok, fh < 0)
+    assert 0 < ok.sum() < len(ok)
+    pick = np.sort(np.random.default_rng(11).choice(len(qf), size=384, replace=False))
+    m = O.OracleModel(robot, env)
+    _edge_parity(m, qf[pick], qt[pick], 0.01, 1, ok[pick], fh[pick], ln[pick], ns[pick])
