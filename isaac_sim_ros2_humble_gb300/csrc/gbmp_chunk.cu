@@ -153,6 +153,19 @@ __device__ __forceinline__ unsigned run_groups(const float4 *runs, int nruns, in
     return gm;
 }
 
+// xform_point for a link pose in the chunk's pose block, which is 16-byte aligned (the
+// block starts on 16 bytes and every pose is 48 bytes): three float4 loads, the same
+// arithmetic.
+__device__ __forceinline__ float3 xform_point_a16(const float *T, float x, float y, float z) {
+    const float4 *T4 = reinterpret_cast<const float4 *>(T);
+    const float4 r0 = T4[0], r1 = T4[1], r2 = T4[2];
+    float3 o;
+    o.x = __fadd_rn(__fmaf_rn(r0.z, z, __fmaf_rn(r0.y, y, __fmul_rn(r0.x, x))), r0.w);
+    o.y = __fadd_rn(__fmaf_rn(r1.z, z, __fmaf_rn(r1.y, y, __fmul_rn(r1.x, x))), r1.w);
+    o.z = __fadd_rn(__fmaf_rn(r2.z, z, __fmaf_rn(r2.y, y, __fmul_rn(r2.x, x))), r2.w);
+    return o;
+}
+
 // Exact tests of one state (link poses lp) against the chunk's candidates, then its
 // self-collision pairs.  ns_end / nb_end / nc_end delimit the sphere / cuboid /
 // cylinder candidates; `need` holds the groups any candidate or listed group pair
@@ -172,7 +185,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
         if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, place)) * 24;
         if (place) {
             const float4 s = t.sph[k];
-            const float3 p = xform_point(lp + 12 * t.slink[k], s.x, s.y, s.z);
+            const float3 p = xform_point_a16(lp + 12 * t.slink[k], s.x, s.y, s.z);
             cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
             gbit[m] = 1u << t.sgrp[k];
             w.cen[k] = make_float4(p.x, p.y, p.z, s.w);
@@ -184,7 +197,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
     }
     if (lane < R.G && ((need >> lane) & 1u)) {
         const float4 g = t.grp[lane];
-        const float3 c = xform_point(lp + 12 * t.glink[lane], g.x, g.y, g.z);
+        const float3 c = xform_point_a16(lp + 12 * t.glink[lane], g.x, g.y, g.z);
         w.gb[lane] = make_float4(c.x, c.y, c.z, g.w);
     }
     __syncwarp();
@@ -275,12 +288,13 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
                 // The range holds every (sphere of a, sphere of b) pair.  A sphere of a can
                 // touch a sphere of b only if it touches b's bounding sphere (and the other
                 // way round), so only pairs of such spheres are tested, with the pair
-                // threshold (ri + rj)^2 rounded as the pair list's.
+                // threshold (ri + rj)^2 rounded as the pair list's.  The spheres of a stay
+                // in the registers of their lanes and are broadcast by shuffles.
                 const float4 GA = w.gb[xa], GB = w.gb[xb];
                 bool ia = false, ib = false;
-                float4 cj = make_float4(kFar, kFar, kFar, 0.f);
+                float4 cj = make_float4(kFar, kFar, kFar, 0.f), c = cj;
                 if (lane < na) {
-                    const float4 c = w.cen[t.gsl[a0 + lane]];
+                    c = w.cen[t.gsl[a0 + lane]];
                     const float rr = c.w + GB.w;
                     ia = sq3(c.x - GB.x, c.y - GB.y, c.z - GB.z) < rr * rr;
                 }
@@ -296,7 +310,8 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
                 while (ma) {
                     const int x = __ffs(ma) - 1;
                     ma &= ma - 1u;
-                    const float4 ci = w.cen[t.gsl[a0 + x]];
+                    const float4 ci = make_float4(__shfl_sync(kFull, c.x, x), __shfl_sync(kFull, c.y, x),
+                                                  __shfl_sync(kFull, c.z, x), __shfl_sync(kFull, c.w, x));
                     if (ib) {
                         const float sr = __fadd_rn(ci.w, cj.w);
                         hit |= sq3(ci.x - cj.x, ci.y - cj.y, ci.z - cj.z) < __fmul_rn(sr, sr);
@@ -351,7 +366,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     for (int p = lane; p < ks * R.G; p += kWarp) {
         const int k = p / R.G, q = p - k * R.G;
         const float4 gq = t.grp[q];
-        const float3 c = xform_point(cs.lpK + k * 12 * R.L + 12 * t.glink[q], gq.x, gq.y, gq.z);
+        const float3 c = xform_point_a16(cs.lpK + k * 12 * R.L + 12 * t.glink[q], gq.x, gq.y, gq.z);
         gc[p] = make_float4(c.x, c.y, c.z, 0.f);
     }
     __syncwarp();
