@@ -108,5 +108,194 @@ def robot_kernels(robot):
     return lib
 
 
+# ---------------------------------------------------------------------------------
+# Collision-cost kernels (cudampl/CUDAMPLib/src/constraints/*.cu).  Those files also
+# hold the constraint classes, which need the reference's headers (Eigen, CUDA
+# runtime); the recipe takes from them, unmodified, only the four cost kernels, the two
+# inverse-pose helpers and the body of the self-collision constructor (the pair list),
+# and compiles those for the host with oracle/ref_block_shim.h.
+# ---------------------------------------------------------------------------------
+REF_SRC = "/root/reference/cudampl/CUDAMPLib/src/constraints"
+
+_COST_HARNESS = r'''
+#include "ref_block_shim.h"
+#include <algorithm>
+
+namespace CUDAMPLib {
+float sdata[1024];   // the kernels' extern __shared__ array (256 floats a block)
+
+// util.h's flattening of the link-pair mask (only fills the unused device copy here)
+inline std::vector<int> boolMatrixFlatten(const std::vector<std::vector<bool>> &m) {
+    std::vector<int> out;
+    for (const auto &row : m)
+        for (bool b : row) out.push_back(b ? 1 : 0);
+    return out;
+}
+
+%(cuboid_inv)s
+
+%(k_sphere)s
+
+%(k_cuboid)s
+
+%(k_cylinder)s
+
+%(k_self)s
+
+struct RefSelfPairs {
+    int *d_self_collision_enables_map = nullptr;
+    int num_of_self_collision_check_ = 0;
+    int *d_collision_sphere_indices_1 = nullptr;
+    int *d_collision_sphere_indices_2 = nullptr;
+    float *d_collision_distance_threshold = nullptr;
+    std::vector<int> collision_sphere_indices_1;
+    std::vector<int> collision_sphere_indices_2;
+    std::vector<float> collision_distance_threshold;
+    void build(const std::string &constraint_name, const std::vector<int> &self_collision_spheres_map,
+               const std::vector<float> &self_collision_spheres_radius,
+               const std::vector<std::vector<bool>> &self_collision_enables_map)
+%(self_ctor)s
+    ~RefSelfPairs() {
+        cudaFree(d_self_collision_enables_map);
+        cudaFree(d_collision_sphere_indices_1);
+        cudaFree(d_collision_sphere_indices_2);
+        cudaFree(d_collision_distance_threshold);
+    }
+};
+}  // namespace CUDAMPLib
+
+%(cylinder_inv)s
+
+static std::vector<float> ref_inverse_poses(bool cylinder, const float *pos, const float *rot, int O) {
+    std::vector<float> inv(12 * (size_t)O);
+    for (int o = 0; o < O; ++o) {
+        std::vector<float> p(pos + 3 * o, pos + 3 * o + 3), r(rot + 9 * o, rot + 9 * o + 9);
+        std::vector<float> m = cylinder ? ::computeInversePoseMatrix(p, r) : CUDAMPLib::computeInversePoseMatrix(p, r);
+        std::copy(m.begin(), m.begin() + 12, inv.begin() + 12 * (size_t)o);
+    }
+    return inv;
+}
+
+extern "C" {
+// centres [n*S*3], radius [S]; one block of 256 threads per configuration, as computeCost
+void ref_cost_sphere(const float *c, const float *r, int S, int n, const float *op, const float *orad, int O,
+                     float *out) {
+    ref_block_launch(n, 256, [&] { CUDAMPLib::computeAndSumCollisionCostKernel(c, r, S, n, op, orad, O, out); });
+}
+void ref_cost_cuboid(const float *c, const float *r, int S, int n, const float *pos, const float *rot,
+                     const float *mn, const float *mx, int O, float *out) {
+    std::vector<float> inv = ref_inverse_poses(false, pos, rot, O);
+    ref_block_launch(n, 256, [&] {
+        CUDAMPLib::computeAndSumCuboidCollisionCostKernel(c, r, S, n, inv.data(), mn, mx, O, out);
+    });
+}
+void ref_cost_cylinder(const float *c, const float *r, int S, int n, const float *pos, const float *rot,
+                       const float *crad, const float *chei, int O, float *out) {
+    std::vector<float> inv = ref_inverse_poses(true, pos, rot, O);
+    ref_block_launch(n, 256, [&] {
+        CUDAMPLib::computeAndSumCylinderCollisionCostKernel(c, r, S, n, inv.data(), crad, chei, O, out);
+    });
+}
+// sphere_link [S], enables [L*L] (row-major 0/1); returns the pair count
+int ref_cost_self(const float *c, const int *sphere_link, const float *r, const unsigned char *enables, int S, int L,
+                  int n, float *out) {
+    std::vector<int> map(sphere_link, sphere_link + S);
+    std::vector<float> rad(r, r + S);
+    std::vector<std::vector<bool>> en(L, std::vector<bool>(L));
+    for (int i = 0; i < L; ++i)
+        for (int j = 0; j < L; ++j) en[i][j] = enables[i * L + j] != 0;
+    CUDAMPLib::RefSelfPairs sp;
+    sp.build("self_collision_constraint", map, rad, en);
+    const int P = sp.num_of_self_collision_check_;
+    ref_block_launch(n, 256, [&] {
+        CUDAMPLib::computeAndSumSelfCollisionCostKernel(c, n, S, P, sp.d_collision_sphere_indices_1,
+                                                        sp.d_collision_sphere_indices_2,
+                                                        sp.d_collision_distance_threshold, out);
+    });
+    return P;
+}
+}
+'''
+
+
+def _extract(text: str, start: str, body_only: bool = False) -> str:
+    """The definition beginning at `start` (through its matching closing brace), or only
+    its braced body; comments and literals are skipped while matching."""
+    i = text.index(start)
+    j = text.index("{", i)
+    depth, k, n = 0, j, len(text)
+    while k < n:
+        if text.startswith("//", k):
+            k = text.index("\n", k)
+            continue
+        if text.startswith("/*", k):
+            k = text.index("*/", k) + 2
+            continue
+        c = text[k]
+        if c in "\"'":
+            k += 1
+            while text[k] != c:
+                k += 2 if text[k] == "\\" else 1
+        elif c == "{":
+            depth += 1
+        elif c == "}":
+            depth -= 1
+            if depth == 0:
+                break
+        k += 1
+    return text[j:k + 1] if body_only else text[i:k + 1]
+
+
+def cost_available() -> bool:
+    return all(os.path.exists(os.path.join(REF_SRC, f)) for f in
+               ("EnvConstraintSphere.cu", "EnvConstraintCuboid.cu", "EnvConstraintCylinder.cu",
+                "SelfCollisionConstraint.cu"))
+
+
+def cost_kernels():
+    """ctypes library with ref_cost_{self,sphere,cuboid,cylinder} built from the
+    reference's own cost kernels, or None without the reference tree."""
+    if not cost_available():
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    rd = lambda f: open(os.path.join(REF_SRC, f)).read()
+    sph, cub, cyl, slf = (rd("EnvConstraintSphere.cu"), rd("EnvConstraintCuboid.cu"), rd("EnvConstraintCylinder.cu"),
+                          rd("SelfCollisionConstraint.cu"))
+    parts = dict(
+        cuboid_inv=_extract(cub, "std::vector<float> computeInversePoseMatrix("),
+        cylinder_inv=_extract(cyl, "std::vector<float> computeInversePoseMatrix("),
+        k_sphere=_extract(sph, "__global__ void computeAndSumCollisionCostKernel("),
+        k_cuboid=_extract(cub, "__global__ void computeAndSumCuboidCollisionCostKernel("),
+        k_cylinder=_extract(cyl, "__global__ void computeAndSumCylinderCollisionCostKernel("),
+        k_self=_extract(slf, "__global__ void computeAndSumSelfCollisionCostKernel("),
+        self_ctor=_extract(slf, "SelfCollisionConstraint::SelfCollisionConstraint(", body_only=True),
+    )
+    src = _COST_HARNESS % parts
+    key = hashlib.sha1((src + open(os.path.join(HERE, "ref_block_shim.h")).read()).encode()).hexdigest()[:16]
+    so = os.path.join(OUT, f"ref_costs_{key}.so")
+    if not os.path.exists(so):
+        cpp = os.path.join(OUT, f"ref_costs_{key}.cpp")
+        with open(cpp, "w") as fh:
+            fh.write(src)
+        # the kernels are compiled by nvcc with multiply-add contraction on by default;
+        # -ffp-contract=fast with FMA instructions mirrors that on the host
+        cmd = ["g++", "-O1", "-std=c++20", "-shared", "-fPIC", "-pthread", "-ffp-contract=fast", "-I" + HERE, cpp,
+               "-o", so]
+        try:
+            subprocess.run(cmd[:7] + ["-mfma"] + cmd[7:], check=True, capture_output=True)
+        except subprocess.CalledProcessError:
+            subprocess.run(cmd, check=True)
+    lib = C.CDLL(so)
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+    lib.ref_cost_sphere.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p, f32p, C.c_int, f32p]
+    lib.ref_cost_cuboid.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p, f32p, f32p, f32p, C.c_int, f32p]
+    lib.ref_cost_cylinder.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p, f32p, f32p, f32p, C.c_int, f32p]
+    lib.ref_cost_self.argtypes = [f32p, i32p, f32p, u8p, C.c_int, C.c_int, C.c_int, f32p]
+    lib.ref_cost_self.restype = C.c_int
+    return lib
+
+
 if __name__ == "__main__":
     print(build(force=True))

@@ -1,7 +1,9 @@
 """Pins the oracle to the reference's own code: the FK, edge-step and interpolation
-kernels that cudampl/CUDAMPLib/include/spaces/KernelGenerator.h generates for a robot
-are compiled for the CPU (oracle/ref_build.py) and compared with the oracle's
-restatement.  Skipped where the reference tree is absent."""
+kernels that cudampl/CUDAMPLib/include/spaces/KernelGenerator.h generates for a robot,
+and the four collision-cost kernels of cudampl/CUDAMPLib/src/constraints/ with the
+self-collision pair list of SelfCollisionConstraint's constructor, are compiled for the
+CPU (oracle/ref_build.py) and compared with the oracle's restatement.  Skipped where
+the reference tree is absent."""
 import numpy as np
 import pytest
 
@@ -64,3 +66,44 @@ def test_step_and_interpolation_match_reference(idx):
         st = m.edge_states(qf[k], qt[k], res, O.STEP_L2)
         np.testing.assert_allclose(st, out[start[k]:start[k] + ns[k]], rtol=0, atol=2.5e-7)
         np.testing.assert_array_equal(st[-1], qt[k])
+
+
+def _cost_case(which):
+    if which == "plain":
+        robot, env, q = W.plain_check_workload(n=48)
+    else:
+        robot, env, q, _ = W.edge_workload(n_edges=48)
+    return robot, env, q
+
+
+@pytest.mark.skipif(not ref_build.cost_available(), reason="reference constraint sources not present")
+@pytest.mark.parametrize("which", ["plain", "edge"])
+def test_collision_costs_match_reference_kernels(which):
+    """Per-configuration self, sphere, cuboid and cylinder costs of the reference's kernels
+    (one 256-thread block per configuration and its shared-memory reduction, run on the
+    host) against the oracle's, on the sphere centres of the oracle's FP32 FK (FK itself
+    is pinned above).  Same bar as the GPU tests: 1e-4 relative, 2e-5 absolute."""
+    robot, env, q = _cost_case(which)
+    ref = ref_build.cost_kernels()
+    m = O.OracleModel(robot, env)
+    oc, ot = m.check_states(q)
+    cen = np.ascontiguousarray(m.sphere_centers(m.fk(q)), np.float32)
+    n, S, L = q.shape[0], robot.num_spheres, robot.num_links
+    r = np.ascontiguousarray(robot.sphere_r, np.float32)
+    ns, nb, nc = env.counts
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    got = np.zeros((4, n), np.float32)
+    npairs = ref.ref_cost_self(cen, np.ascontiguousarray(robot.sphere_link, np.int32), r,
+                               np.ascontiguousarray(robot.enables, np.uint8), S, L, n, got[0])
+    assert npairs == m.npairs                      # the constructor's pair list, counted
+    ref.ref_cost_sphere(cen, r, S, n, f(env.sphere_pos), f(env.sphere_r), ns, got[1])
+    ref.ref_cost_cuboid(cen, r, S, n, f(env.box_pos), f(env.box_rot), f(env.box_min), f(env.box_max), nb, got[2])
+    ref.ref_cost_cylinder(cen, r, S, n, f(env.cyl_pos), f(env.cyl_rot), f(env.cyl_radius), f(env.cyl_height), nc,
+                          got[3])
+    for k in range(4):
+        if k == 3 and nc == 0:
+            assert np.all(got[3] == 0)
+            continue
+        assert (oc[k] > 0).any(), f"no configuration with cost in slot {k}"
+        np.testing.assert_allclose(got[k], oc[k], rtol=1e-4, atol=2e-5, err_msg=f"cost slot {k}")
+        np.testing.assert_array_equal(got[k] > 0, oc[k] > 0)
