@@ -52,6 +52,32 @@ def available() -> bool:
     return os.path.exists(os.path.join(REF_INCLUDE, "spaces", "KernelGenerator.h"))
 
 
+# The reference's kernels are compiled by NVRTC / nvcc with multiply-add contraction on
+# (their default).  GCC forms fused multiply-adds from -O2 on under -ffp-contract=fast,
+# with FMA instructions enabled (-mfma where the target needs the flag, as x86-64 does;
+# aarch64 has them in the base ISA).
+_HOST_FLAGS = ["-O2", "-ffp-contract=fast", "-shared", "-fPIC", "-pthread"]
+
+
+def _host_library(tag: str, src: str, std: str) -> str:
+    """Compile `src` (host C++ around reference code) into oracle/_ref/, cached by a hash
+    of the source, the shims and the flags; returns the library path."""
+    shims = "".join(open(os.path.join(HERE, f)).read() for f in ("ref_shim.h", "ref_block_shim.h"))
+    key = hashlib.sha1((src + shims + " ".join(_HOST_FLAGS) + std).encode()).hexdigest()[:16]
+    so = os.path.join(OUT, f"{tag}_{key}.so")
+    if not os.path.exists(so):
+        os.makedirs(OUT, exist_ok=True)
+        cpp = os.path.join(OUT, f"{tag}_{key}.cpp")
+        with open(cpp, "w") as fh:
+            fh.write(src)
+        cmd = ["g++", std] + _HOST_FLAGS + ["-I" + HERE, cpp, "-o", so]
+        try:
+            subprocess.run(cmd[:2] + ["-mfma"] + cmd[2:], check=True, capture_output=True)
+        except subprocess.CalledProcessError:
+            subprocess.run(cmd, check=True)
+    return so
+
+
 def build(force: bool = False):
     """Build oracle/_ref/ref_gen when the reference tree is present; returns its path or None."""
     if not available():
@@ -77,29 +103,16 @@ def robot_kernels(robot):
     if gen is None:
         return None
     text = _robot_text(robot)
-    key = hashlib.sha1(text.encode()).hexdigest()[:16]
-    so = os.path.join(OUT, f"ref_kernels_{key}.so")
-    if not os.path.exists(so):
-        out = subprocess.run([gen], input=text, capture_output=True, text=True, check=True).stdout
-        parts = {}
-        cur = None
-        for line in out.splitlines(keepends=True):
-            if line.startswith("//@@ "):
-                cur = line.split()[1]
-                parts[cur] = ""
-            elif cur:
-                parts[cur] += line
-        cpp = os.path.join(OUT, f"ref_kernels_{key}.cpp")
-        with open(cpp, "w") as fh:
-            fh.write(_HARNESS % parts)
-        # NVRTC contracts multiply-adds by default (fmad=true); -ffp-contract=fast with FMA
-        # instructions mirrors that on the host.
-        cmd = ["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=fast", "-I" + HERE, cpp, "-o", so]
-        try:
-            subprocess.run(cmd[:5] + ["-mfma"] + cmd[5:], check=True, capture_output=True)
-        except subprocess.CalledProcessError:
-            subprocess.run(cmd, check=True)
-    lib = C.CDLL(so)
+    out = subprocess.run([gen], input=text, capture_output=True, text=True, check=True).stdout
+    parts = {}
+    cur = None
+    for line in out.splitlines(keepends=True):
+        if line.startswith("//@@ "):
+            cur = line.split()[1]
+            parts[cur] = ""
+        elif cur:
+            parts[cur] += line
+    lib = C.CDLL(_host_library("ref_kernels", _HARNESS % parts, "-std=c++17"))
     f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
     i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
     lib.ref_fk.argtypes = [f32p, C.c_int, f32p]
@@ -270,22 +283,7 @@ def cost_kernels():
         k_self=_extract(slf, "__global__ void computeAndSumSelfCollisionCostKernel("),
         self_ctor=_extract(slf, "SelfCollisionConstraint::SelfCollisionConstraint(", body_only=True),
     )
-    src = _COST_HARNESS % parts
-    key = hashlib.sha1((src + open(os.path.join(HERE, "ref_block_shim.h")).read()).encode()).hexdigest()[:16]
-    so = os.path.join(OUT, f"ref_costs_{key}.so")
-    if not os.path.exists(so):
-        cpp = os.path.join(OUT, f"ref_costs_{key}.cpp")
-        with open(cpp, "w") as fh:
-            fh.write(src)
-        # the kernels are compiled by nvcc with multiply-add contraction on by default;
-        # -ffp-contract=fast with FMA instructions mirrors that on the host
-        cmd = ["g++", "-O1", "-std=c++20", "-shared", "-fPIC", "-pthread", "-ffp-contract=fast", "-I" + HERE, cpp,
-               "-o", so]
-        try:
-            subprocess.run(cmd[:7] + ["-mfma"] + cmd[7:], check=True, capture_output=True)
-        except subprocess.CalledProcessError:
-            subprocess.run(cmd, check=True)
-    lib = C.CDLL(so)
+    lib = C.CDLL(_host_library("ref_costs", _COST_HARNESS % parts, "-std=c++20"))
     f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
     i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
     u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
@@ -294,6 +292,59 @@ def cost_kernels():
     lib.ref_cost_cylinder.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p, f32p, f32p, f32p, C.c_int, f32p]
     lib.ref_cost_self.argtypes = [f32p, i32p, f32p, u8p, C.c_int, C.c_int, C.c_int, f32p]
     lib.ref_cost_self.restype = C.c_int
+    return lib
+
+
+# The state manager's nearest-neighbour and steer kernels (cudampl/CUDAMPLib/src/states/
+# SingleArmStates.cu), taken the same way.
+REF_STATES = "/root/reference/cudampl/CUDAMPLib/src/states/SingleArmStates.cu"
+
+_MANAGER_HARNESS = r'''
+#include "ref_block_shim.h"
+
+namespace CUDAMPLib {
+alignas(16) char shared_mem[256 * 8];   // the NN kernel's extern __shared__ array
+
+%(k_nn)s
+
+%(k_steer)s
+}  // namespace CUDAMPLib
+
+extern "C" {
+// one block of 256 threads per query, one group holding candidate indices cand[G]
+void ref_nearest(float *query, int Q, float *tree, int *cand, int G, int L, int *active, int *out) {
+    ref_block_launch(Q, 256, [&] {
+        CUDAMPLib::find_the_nearest_neighbors_kernel(query, Q, tree, cand, G, L, active, 1, 0, out);
+    });
+}
+// in place on to[n*L]; 256 threads a block, as interpolateToStates
+void ref_steer(float *to, int n, float *tree, int L, int *nn, float max_distance) {
+    ref_block_launch((n + 255) / 256, 256, [&] {
+        CUDAMPLib::interpolate_to_states(to, n, tree, L, nn, max_distance);
+    });
+}
+}
+'''
+
+
+def manager_available() -> bool:
+    return os.path.exists(REF_STATES)
+
+
+def manager_kernels():
+    """ctypes library with ref_nearest / ref_steer built from the reference's own state
+    manager kernels, or None without the reference tree."""
+    if not manager_available():
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    text = open(REF_STATES).read()
+    src = _MANAGER_HARNESS % dict(k_nn=_extract(text, "__global__ void find_the_nearest_neighbors_kernel("),
+                                  k_steer=_extract(text, "__global__ void interpolate_to_states("))
+    lib = C.CDLL(_host_library("ref_manager", src, "-std=c++20"))
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    lib.ref_nearest.argtypes = [f32p, C.c_int, f32p, i32p, C.c_int, C.c_int, i32p, i32p]
+    lib.ref_steer.argtypes = [f32p, C.c_int, f32p, C.c_int, i32p, C.c_float]
     return lib
 
 

@@ -107,3 +107,32 @@ def test_collision_costs_match_reference_kernels(which):
         assert (oc[k] > 0).any(), f"no configuration with cost in slot {k}"
         np.testing.assert_allclose(got[k], oc[k], rtol=1e-4, atol=2e-5, err_msg=f"cost slot {k}")
         np.testing.assert_array_equal(got[k] > 0, oc[k] > 0)
+
+
+@pytest.mark.skipif(not ref_build.manager_available(), reason="reference state sources not present")
+def test_nearest_and_steer_match_reference_kernels():
+    """SingleArmStateManager's nearest-neighbour kernel (block per query, shared-memory
+    argmin over sqrtf distances of the active joints) and its steer kernel, run on the
+    host, against the oracle's restatement: the same nearest index for every query, and
+    steered states within 1e-6 and nearly all of them equal to the bit (the host
+    compiler fuses the interpolation's multiply-add but not the squared-distance sum,
+    where nvcc, the oracle and the GPU kernel fuse both; a one-ulp change of the
+    distance moves a state by at most about |to - from| x 1e-7)."""
+    robot = W.edge_workload(n_edges=1)[0]
+    L = robot.num_links
+    rng = np.random.default_rng(5)
+    tree = robot.sample_full(rng, 3000)
+    queries = robot.sample_full(rng, 128)
+    cand = np.sort(rng.choice(3000, 1700, replace=False)).astype(np.int32)
+    ref = ref_build.manager_kernels()
+    out = np.zeros(128, np.int32)
+    ref.ref_nearest(queries, 128, tree, cand, len(cand), L, np.ascontiguousarray(robot.active, np.int32), out)
+    np.testing.assert_array_equal(out, O.nearest(tree, queries, active=robot.active, cand=cand))
+
+    to = robot.sample_full(rng, 500)
+    steered = to.copy()
+    ref.ref_steer(steered, 500, tree, L, np.arange(500, dtype=np.int32), 0.5)
+    o = O.steer(tree[:500], to, 0.5)
+    assert not np.array_equal(o, to)                # the limit binds on these pairs
+    assert np.abs(steered - o).max() <= 1e-6
+    assert np.mean(steered == o) > 0.95
