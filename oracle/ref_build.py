@@ -295,8 +295,9 @@ def cost_kernels():
     return lib
 
 
-# The state manager's nearest-neighbour and steer kernels (cudampl/CUDAMPLib/src/states/
-# SingleArmStates.cu), taken the same way.
+# The state manager's nearest-neighbour and steer kernels and the sphere transform of
+# SingleArmStates::update (cudampl/CUDAMPLib/src/states/SingleArmStates.cu), taken the
+# same way.
 REF_STATES = "/root/reference/cudampl/CUDAMPLib/src/states/SingleArmStates.cu"
 
 _MANAGER_HARNESS = r'''
@@ -308,6 +309,8 @@ alignas(16) char shared_mem[256 * 8];   // the NN kernel's extern __shared__ arr
 %(k_nn)s
 
 %(k_steer)s
+
+%(k_spheres)s
 }  // namespace CUDAMPLib
 
 extern "C" {
@@ -315,6 +318,12 @@ extern "C" {
 void ref_nearest(float *query, int Q, float *tree, int *cand, int G, int L, int *active, int *out) {
     ref_block_launch(Q, 256, [&] {
         CUDAMPLib::find_the_nearest_neighbors_kernel(query, Q, tree, cand, G, L, active, 1, 0, out);
+    });
+}
+// sphere centres [n*S*3] from link poses [n*L*16]; 256 threads a block, as update()
+void ref_sphere_centers(int n, int L, int S, int *map, float *pos, float *poses, float *out) {
+    ref_block_launch((n * S + 255) / 256, 256, [&] {
+        CUDAMPLib::update_self_collision_spheres_kernel(n, L, S, map, pos, poses, out);
     });
 }
 // in place on to[n*L]; 256 threads a block, as interpolateToStates
@@ -332,19 +341,21 @@ def manager_available() -> bool:
 
 
 def manager_kernels():
-    """ctypes library with ref_nearest / ref_steer built from the reference's own state
-    manager kernels, or None without the reference tree."""
+    """ctypes library with ref_nearest / ref_steer / ref_sphere_centers built from the
+    reference's own state kernels, or None without the reference tree."""
     if not manager_available():
         return None
     os.makedirs(OUT, exist_ok=True)
     text = open(REF_STATES).read()
     src = _MANAGER_HARNESS % dict(k_nn=_extract(text, "__global__ void find_the_nearest_neighbors_kernel("),
-                                  k_steer=_extract(text, "__global__ void interpolate_to_states("))
+                                  k_steer=_extract(text, "__global__ void interpolate_to_states("),
+                                  k_spheres=_extract(text, "__global__ void update_self_collision_spheres_kernel("))
     lib = C.CDLL(_host_library("ref_manager", src, "-std=c++20"))
     f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
     i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
     lib.ref_nearest.argtypes = [f32p, C.c_int, f32p, i32p, C.c_int, C.c_int, i32p, i32p]
     lib.ref_steer.argtypes = [f32p, C.c_int, f32p, C.c_int, i32p, C.c_float]
+    lib.ref_sphere_centers.argtypes = [C.c_int, C.c_int, C.c_int, i32p, f32p, f32p, f32p]
     return lib
 
 

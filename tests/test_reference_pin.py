@@ -136,3 +136,25 @@ def test_nearest_and_steer_match_reference_kernels():
     assert not np.array_equal(o, to)                # the limit binds on these pairs
     assert np.abs(steered - o).max() <= 1e-6
     assert np.mean(steered == o) > 0.95
+
+
+@pytest.mark.skipif(not ref_build.manager_available(), reason="reference state sources not present")
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_sphere_transform_matches_reference_kernel(idx):
+    """update_self_collision_spheres_kernel (SingleArmStates.cu:340-393) on the oracle's
+    FP32 link poses: sphere centres within one rounding of the oracle's and mostly equal
+    to the bit (which two products of m0 x + m1 y + m2 z + m3 a compiler fuses first is
+    its own choice), both within 1e-6 of the FP64 centres."""
+    robot = robots()[idx]
+    m = O.OracleModel(robot)
+    q = robot.sample_full(np.random.default_rng(20 + idx), 500)
+    poses = np.ascontiguousarray(m.fk(q), np.float32)
+    n, L, S = q.shape[0], robot.num_links, robot.num_spheres
+    out = np.zeros((n, S, 3), np.float32)
+    ref_build.manager_kernels().ref_sphere_centers(n, L, S, np.ascontiguousarray(robot.sphere_link, np.int32),
+                                                   np.ascontiguousarray(robot.sphere_pos, np.float32), poses, out)
+    o = m.sphere_centers(poses)
+    assert np.abs(out - o).max() <= 2.5e-7
+    assert np.mean(out == o) > 0.9
+    p64 = m.sphere_centers(m.fk(q.astype(np.float64), f64=True))
+    assert np.abs(out - p64).max() < 1e-6
