@@ -84,9 +84,8 @@ __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K
 // the edge exactly t), all chains advancing together: first the ks x (L - 1) joint-local
 // transforms of links 1.. spread over the lanes link-major (the lanes of one pass mostly
 // share a joint type, so the type branches diverge little; link 0 is the identity and
-// needs none), then link by link the ks x 12 pose elements, slot
-// j of a lane being element (lane + 32 j) of the flattened (state, element) list.  The
-// arithmetic is warp_fk's (joint_local, mul_elem), so poses are bit-identical.
+// needs none), then the chains, one pose row a lane (below).  The arithmetic is
+// warp_fk's (joint_local, mul_elem), so poses are bit-identical.
 template <int K>
 __device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const float *__restrict__ f,
                                      const float *__restrict__ to, const float *__restrict__ d, int s0, int n,
@@ -97,32 +96,36 @@ __device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const f
         const float qv = (s == n - 1) ? to[i] : __fmaf_rn(d[i], (float)s, f[i]);
         joint_local(t, i, qv, locK + 12 * (k * L + i));
     }
-    constexpr int J = (K * 12 + kWarp - 1) / kWarp;
-    int kk[J], ee[J];
-    bool on[J];
-#pragma unroll
-    for (int j = 0; j < J; ++j) {
-        const int idx = lane + kWarp * j;
-        on[j] = idx < ks * 12;
-        kk[j] = idx / 12;
-        ee[j] = idx - 12 * kk[j];
-        if (on[j]) lpK[kk[j] * 12 * L + ee[j]] = (ee[j] % 5 == 0) ? 1.f : 0.f;
+    __syncwarp();
+    // Composition: lane 3 k + r (k < ks) owns row r of state k's poses and walks the
+    // links in order.  The parent's row is the lane's own: in registers while the parent
+    // is the previous link, else its own earlier store, so no lane waits on another.
+    // Rows and joint-local transforms are 16-byte aligned (48-byte poses in a block
+    // carved on 16 bytes) and move as float4.
+    const int kr = lane / 3, rr = lane - 3 * kr;
+    if (lane < 3 * ks) {
+        float4 *rowp = reinterpret_cast<float4 *>(lpK + kr * 12 * L) + rr;   // row rr of link 0
+        float4 a = make_float4(rr == 0 ? 1.f : 0.f, rr == 1 ? 1.f : 0.f, rr == 2 ? 1.f : 0.f, 0.f);
+        *rowp = a;
+        const float4 *loc = reinterpret_cast<const float4 *>(locK + kr * 12 * L);
+        for (int i = 1; i < L; ++i) {
+            const int ty = t.type[i], par = t.parent[i];
+            if (par != i - 1) a = rowp[3 * par];
+            float4 o;
+            if (ty == 1 || ty == 2 || ty == 5) {
+                const float4 b0 = loc[3 * i], b1 = loc[3 * i + 1], b2 = loc[3 * i + 2];
+                o.x = __fmaf_rn(a.z, b2.x, __fmaf_rn(a.y, b1.x, __fmul_rn(a.x, b0.x)));
+                o.y = __fmaf_rn(a.z, b2.y, __fmaf_rn(a.y, b1.y, __fmul_rn(a.x, b0.y)));
+                o.z = __fmaf_rn(a.z, b2.z, __fmaf_rn(a.y, b1.z, __fmul_rn(a.x, b0.z)));
+                o.w = __fadd_rn(__fmaf_rn(a.z, b2.w, __fmaf_rn(a.y, b1.w, __fmul_rn(a.x, b0.w))), a.w);
+            } else {
+                o = make_float4(rr == 0 ? 1.f : 0.f, rr == 1 ? 1.f : 0.f, rr == 2 ? 1.f : 0.f, 0.f);
+            }
+            rowp[3 * i] = o;
+            a = o;
+        }
     }
     __syncwarp();
-    for (int i = 1; i < L; ++i) {
-        const int ty = t.type[i], par = t.parent[i];
-        const bool known = ty == 1 || ty == 2 || ty == 5;
-#pragma unroll
-        for (int j = 0; j < J; ++j) {
-            if (on[j]) {
-                float *base = lpK + kk[j] * 12 * L;
-                const int r = ee[j] >> 2, c = ee[j] & 3;
-                base[12 * i + ee[j]] = known ? mul_elem(base + 12 * par, locK + 12 * (kk[j] * L + i), r, c)
-                                             : ((r == c) ? 1.f : 0.f);
-            }
-        }
-        __syncwarp();
-    }
 }
 
 // Append this lane's obstacle (when mask != 0) to the candidate list; returns the new
