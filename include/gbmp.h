@@ -105,6 +105,12 @@ GBMP_API gbmp_status gbmp_robot_info(gbmp_robot robot, int32_t *num_links, int32
                             int32_t *num_self_pairs, int32_t *dim, int32_t *codegen_active);
 /* Host copy of the self-collision pair list: h_pairs [2*P] (i, j), h_thr_sq [P]. */
 GBMP_API gbmp_status gbmp_robot_self_pairs(gbmp_robot robot, int32_t *h_pairs, float *h_thr_sq, int32_t cap);
+/* Host copies of the joint tables given at creation, each [L] and each optional: the
+ * active map (1 = planning joint), the value inactive joints take, and the limits.
+ * Callers that hold active-joint vectors (the reference's Configuration / vector<float>
+ * of `dim` values) build full vectors from these. */
+GBMP_API gbmp_status gbmp_robot_joints(gbmp_robot robot, uint8_t *h_active, float *h_default, float *h_lower,
+                              float *h_upper);
 /* Select the kernel family used by later calls: 0 table-driven, 1 generated. */
 GBMP_API gbmp_status gbmp_robot_use_codegen(gbmp_robot robot, int32_t enable);
 /* The generated kernels of a robot created with GBMP_ROBOT_CODEGEN (the reference writes
@@ -159,6 +165,10 @@ GBMP_API gbmp_status gbmp_check_states(gbmp_robot robot, gbmp_env env, const flo
  * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read). */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
+/* Planners only: every edge is checked at a fixed count of equal steps, `resolution`
+ * rounded down to an integer G >= 1 (the states at k / G of the edge for k = 1..G, the
+ * last one the edge's end), pRRTC's `granularity` (pRRTC/src/planning/pRRTC.cu:430-440). */
+#define GBMP_STEP_COUNT 2
 GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const float *d_from, const float *d_to,
                              int64_t n_edges, float resolution, int32_t step_rule, uint8_t *d_ok,
                              int32_t *d_first_hit, float *d_length, int32_t *d_num_steps, void *stream);
@@ -251,7 +261,7 @@ typedef struct gbmp_rrtc_settings {
     int32_t max_iters;      /* iteration cap per lane                                    */
     float range;            /* maximum extension length, L2 over active joints            */
     float resolution;       /* edge collision-check step (<= 0: the robot's resolution)   */
-    int32_t step_rule;      /* GBMP_STEP_L2 or GBMP_STEP_LINF                             */
+    int32_t step_rule;      /* GBMP_STEP_L2, GBMP_STEP_LINF or GBMP_STEP_COUNT             */
     uint64_t seed;          /* Philox key; sample (lane, iteration, joint)                */
     double time_limit_s;    /* device-side deadline (<= 0: 10 s)                          */
 } gbmp_rrtc_settings;
@@ -269,6 +279,14 @@ typedef struct gbmp_rrtc_result {
 GBMP_API gbmp_status gbmp_planner_create(gbmp_robot robot, int32_t max_nodes, int32_t path_cap,
                                          gbmp_planner *out);
 GBMP_API gbmp_status gbmp_planner_destroy(gbmp_planner planner);
+/* Several goals, replacing pRRTC::solve's goal list (pRRTC/src/planning/Planners.hh:75-78,
+ * pRRTC.cu:640-700): every goal is a root of the goal tree, and the path ends at the
+ * goal its chain reaches.  h_goals: [n_goals * L] full joint vectors, n_goals >= 1 and at
+ * most the planner's max_nodes.  Otherwise as gbmp_rrtc_solve. */
+GBMP_API gbmp_status gbmp_rrtc_solve_goals(gbmp_planner planner, gbmp_env env, const float *h_start,
+                                           const float *h_goals, int32_t n_goals,
+                                           const gbmp_rrtc_settings *settings, float *h_path, int32_t path_cap,
+                                           gbmp_rrtc_result *result, void *stream);
 /* h_start / h_goal: full joint vectors [L].  h_path: [path_cap * L] host buffer.
  * Returns GBMP_OK when solved, GBMP_ERR_NOT_SOLVED / GBMP_ERR_TIMEOUT otherwise (the
  * result struct is filled in every case).  Synchronous on `stream`. */

@@ -18,7 +18,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "CUDA er
           4: "code generation failed", 5: "capacity exceeded", 6: "timed out", 7: "not solved",
           8: "unsupported"}
 CHECK_VERDICT, CHECK_COST = 0, 1
-STEP_L2, STEP_LINF = 0, 1
+STEP_L2, STEP_LINF, STEP_COUNT = 0, 1, 2
 ROBOT_GENERIC, ROBOT_CODEGEN = 0, 1
 
 
@@ -94,6 +94,7 @@ SIGNATURES = {
     "gbmp_robot_destroy": [_vp],
     "gbmp_robot_info": [_vp, _i32p, _i32p, _i32p, _i32p, _i32p],
     "gbmp_robot_self_pairs": [_vp, _vp, _vp, _i32],
+    "gbmp_robot_joints": [_vp, _vp, _vp, _vp, _vp],
     "gbmp_robot_use_codegen": [_vp, _i32],
     "gbmp_robot_codegen_info": [_vp, C.c_char_p, _i64, C.POINTER(_i64), C.POINTER(_u64), C.POINTER(_i32),
                                 C.POINTER(C.c_double)],
@@ -112,6 +113,8 @@ SIGNATURES = {
     "gbmp_planner_create": [_vp, _i32, _i32, C.POINTER(_vp)],
     "gbmp_planner_destroy": [_vp],
     "gbmp_rrtc_solve": [_vp, _vp, _vp, _vp, C.POINTER(RrtcSettings), _vp, _i32, C.POINTER(RrtcResult), _vp],
+    "gbmp_rrtc_solve_goals": [_vp, _vp, _vp, _vp, _i32, C.POINTER(RrtcSettings), _vp, _i32, C.POINTER(RrtcResult),
+                              _vp],
     "gbmp_batch_planner_create": [_i32, _i32, _i32, _i32, C.POINTER(_vp)],
     "gbmp_batch_planner_destroy": [_vp],
     "gbmp_rrtc_solve_batch": [_vp, _i32, C.POINTER(RrtcProblem), C.POINTER(RrtcSettings), _i32, _i32,

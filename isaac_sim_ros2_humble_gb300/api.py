@@ -202,16 +202,17 @@ class Planner:
               resolution: float = 0.0, rule: int = _lib.STEP_L2, seed: int = 0, time_limit_s: float = 10.0,
               stream=None, raise_on_failure: bool = False):
         """Returns (result, path): result is a dict of the C result struct, path the
-        [path_len, L] float32 waypoints (empty when not solved)."""
+        [path_len, L] float32 waypoints (empty when not solved).  `goal` is one full joint
+        vector [L] or several [n, L] (every one a root of the goal tree)."""
         st = _lib.RrtcSettings(int(lanes), int(max_iters), float(range_), float(resolution), int(rule), int(seed),
                                float(time_limit_s))
         res = _lib.RrtcResult()
         s0 = _c(start, np.float32).reshape(-1)
-        g0 = _c(goal, np.float32).reshape(-1)
-        assert s0.size == self.robot.L and g0.size == self.robot.L
-        status = _lib.load().gbmp_rrtc_solve(self.handle, env.handle, s0.ctypes.data, g0.ctypes.data, C.byref(st),
-                                             self._path.ctypes.data, self.path_cap, C.byref(res),
-                                             stream_handle(stream))
+        g0 = _c(goal, np.float32).reshape(-1, self.robot.L)
+        assert s0.size == self.robot.L
+        status = _lib.load().gbmp_rrtc_solve_goals(self.handle, env.handle, s0.ctypes.data, g0.ctypes.data,
+                                                   int(g0.shape[0]), C.byref(st), self._path.ctypes.data,
+                                                   self.path_cap, C.byref(res), stream_handle(stream))
         if status not in (_lib.OK, 6, 7) or raise_on_failure:
             check(status)
         out = {f: getattr(res, f) for f, _ in _lib.RrtcResult._fields_}

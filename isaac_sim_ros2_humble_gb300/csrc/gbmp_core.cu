@@ -551,6 +551,16 @@ gbmp_status gbmp_robot_self_pairs(gbmp_robot r, int32_t *h_pairs, float *h_thr, 
     return GBMP_OK;
 }
 
+gbmp_status gbmp_robot_joints(gbmp_robot r, uint8_t *h_active, float *h_default, float *h_lower, float *h_upper) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    const size_t L = (size_t)r->L;
+    if (h_active) memcpy(h_active, r->active.data(), L);
+    if (h_default) memcpy(h_default, r->defv.data(), sizeof(float) * L);
+    if (h_lower) memcpy(h_lower, r->lower.data(), sizeof(float) * L);
+    if (h_upper) memcpy(h_upper, r->upper.data(), sizeof(float) * L);
+    return GBMP_OK;
+}
+
 gbmp_status gbmp_robot_use_codegen(gbmp_robot r, int32_t enable) {
     GBMP_CHECK_ARG(r, "robot is NULL");
     if (enable && !r->cg) {

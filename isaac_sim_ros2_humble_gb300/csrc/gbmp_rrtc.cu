@@ -166,9 +166,10 @@ __device__ int block_nearest(const float *__restrict__ nodes, int size, int stri
 }
 
 // Validate the edge a -> b (full joint vectors in shared memory) with the step rule of
-// checkMotions: n = floor(metric / res) + 1 states, state k = a + dir * k, the last
-// state is b; state 0 (= a, already in the tree) is skipped unless n == 1.  One warp
-// per state.  Returns true if every state is collision-free.
+// checkMotions: n = floor(metric / res) + 1 states (for GBMP_STEP_COUNT n = res + 1,
+// pRRTC's granularity), state k = a + dir * k, the last state is b; state 0 (= a,
+// already in the tree) is skipped unless n == 1.  One warp per state.  Returns true if
+// every state is collision-free.
 template <int SPL, bool CULL>
 __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                 const float *a, const float *b, float res, int rule, int *s_flag, float *s_dir,
@@ -181,9 +182,13 @@ __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const De
             d2 = __fmaf_rn(d, d, d2);
             dinf = fmaxf(dinf, fabsf(d));
         }
-        const float metric = rule == GBMP_STEP_LINF ? dinf : __fsqrt_rn(d2);
-        const float ratio = __fdiv_rn(metric, res);
-        *s_n = ratio < 1e6f ? (int)ratio + 1 : 1000001;
+        if (rule == GBMP_STEP_COUNT) {
+            *s_n = (int)res + 1;   // res in [1, 1e6] (checked by the host): G equal steps
+        } else {
+            const float metric = rule == GBMP_STEP_LINF ? dinf : __fsqrt_rn(d2);
+            const float ratio = __fdiv_rn(metric, res);
+            *s_n = ratio < 1e6f ? (int)ratio + 1 : 1000001;
+        }
         *s_flag = 0;
     }
     __syncthreads();
@@ -593,6 +598,19 @@ __global__ void k_rrtc_batch_trace(const BatchProblem *__restrict__ probs, int n
 
 using namespace gbmp;
 
+// Edge-check step of a solve: the settings' resolution (or the robot's), or for
+// GBMP_STEP_COUNT the step count G in [1, 1e6].  Returns false on invalid settings.
+static bool plan_step(const gbmp_rrtc_settings *s, float robot_res, float *res) {
+    if (s->step_rule == GBMP_STEP_COUNT) {
+        if (!(s->resolution >= 1.f && s->resolution <= 1e6f)) return false;
+        *res = floorf(s->resolution);
+        return true;
+    }
+    if (s->step_rule != GBMP_STEP_L2 && s->step_rule != GBMP_STEP_LINF) return false;
+    *res = s->resolution > 0.f ? s->resolution : robot_res;
+    return *res > 0.f;
+}
+
 struct gbmp_planner_s {
     gbmp_robot robot = nullptr;
     int cap = 0, stride = 0, path_cap = 0;
@@ -643,15 +661,23 @@ gbmp_status gbmp_planner_destroy(gbmp_planner p) {
 gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, const float *h_goal,
                             const gbmp_rrtc_settings *s, float *h_path, int32_t path_cap, gbmp_rrtc_result *res,
                             void *stream) {
-    GBMP_CHECK_ARG(p && env && h_start && h_goal && s && res, "NULL argument");
+    return gbmp_rrtc_solve_goals(p, env, h_start, h_goal, 1, s, h_path, path_cap, res, stream);
+}
+
+gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_start, const float *h_goals,
+                                  int32_t n_goals, const gbmp_rrtc_settings *s, float *h_path, int32_t path_cap,
+                                  gbmp_rrtc_result *res, void *stream) {
+    GBMP_CHECK_ARG(p && env && h_start && h_goals && s && res, "NULL argument");
     gbmp_robot r = p->robot;
     const int L = r->L;
+    GBMP_CHECK_ARG(n_goals >= 1 && n_goals <= p->cap, "n_goals %d outside [1, %d]", n_goals, p->cap);
     GBMP_CHECK_ARG(s->lanes >= 1 && s->lanes <= (1 << 20), "lanes %d outside [1, 2^20]", s->lanes);
     GBMP_CHECK_ARG(s->range > 0.f && std::isfinite(s->range), "range must be > 0");
     GBMP_CHECK_ARG(s->max_iters >= 1, "max_iters < 1");
-    GBMP_CHECK_ARG(s->step_rule == GBMP_STEP_L2 || s->step_rule == GBMP_STEP_LINF, "unknown step rule");
-    for (int j = 0; j < L; ++j)
-        GBMP_CHECK_ARG(std::isfinite(h_start[j]) && std::isfinite(h_goal[j]), "start/goal not finite");
+    float step_res = 0.f;
+    GBMP_CHECK_ARG(plan_step(s, r->resolution, &step_res), "unknown step rule or resolution out of range");
+    for (int j = 0; j < L; ++j) GBMP_CHECK_ARG(std::isfinite(h_start[j]), "start not finite");
+    for (long long j = 0; j < (long long)n_goals * L; ++j) GBMP_CHECK_ARG(std::isfinite(h_goals[j]), "goal not finite");
     memset(res, 0, sizeof *res);
     cudaStream_t st = (cudaStream_t)stream;
     const RrtcDev &D = p->dev;
@@ -659,12 +685,15 @@ gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, 
     GBMP_CUDA(cudaMemsetAsync(D.nodes[0], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
     GBMP_CUDA(cudaMemsetAsync(D.nodes[1], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
     GBMP_CUDA(cudaMemsetAsync(D.size, 0, 256, st));
-    int h_init[2] = {1, 1}, h_root = 0;
-    GBMP_CUDA(cudaMemcpyAsync(D.size, h_init, sizeof h_init, cudaMemcpyHostToDevice, st));
+    // the goal tree starts with every goal as a root (a node that is its own parent)
+    std::vector<int> h_init{1, n_goals}, h_roots(n_goals);
+    for (int g = 0; g < n_goals; ++g) h_roots[g] = g;
+    GBMP_CUDA(cudaMemcpyAsync(D.size, h_init.data(), sizeof(int) * 2, cudaMemcpyHostToDevice, st));
     GBMP_CUDA(cudaMemcpyAsync(D.nodes[0], h_start, sizeof(float) * L, cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpyAsync(D.nodes[1], h_goal, sizeof(float) * L, cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpyAsync(D.parent[0], &h_root, sizeof(int), cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpyAsync(D.parent[1], &h_root, sizeof(int), cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpy2DAsync(D.nodes[1], sizeof(float) * p->stride, h_goals, sizeof(float) * L, sizeof(float) * L,
+                                n_goals, cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(D.parent[0], h_roots.data(), sizeof(int), cudaMemcpyHostToDevice, st));
+    GBMP_CUDA(cudaMemcpyAsync(D.parent[1], h_roots.data(), sizeof(int) * n_goals, cudaMemcpyHostToDevice, st));
 
     const DevEnv E = env->dev();
     DevRobot DR = r->dev;
@@ -676,7 +705,7 @@ gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, 
     prm.max_iters = s->max_iters;
     prm.rule = s->step_rule;
     prm.range = s->range;
-    prm.res = s->resolution > 0.f ? s->resolution : r->resolution;
+    prm.res = step_res;
     prm.seed = s->seed;
     // device deadline from the host clock offset: read %globaltimer through a 1-thread probe
     unsigned long long now_ns = 0;
@@ -765,7 +794,6 @@ gbmp_status gbmp_rrtc_solve(gbmp_planner p, gbmp_env env, const float *h_start, 
 }
 
 }  // extern "C"
-
 
 // ---------------------------------------------------------------------------------
 // Batched planning (many heterogeneous problems in one persistent launch).
@@ -920,7 +948,9 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
     GBMP_CHECK_ARG(lanes_per_problem >= 1 && lanes_per_problem <= 4096, "lanes_per_problem outside [1, 4096]");
     GBMP_CHECK_ARG((long long)n * lanes_per_problem <= (1LL << 30), "too many blocks");
     GBMP_CHECK_ARG(s->range > 0.f && s->max_iters >= 1, "bad settings");
-    GBMP_CHECK_ARG(s->step_rule == GBMP_STEP_L2 || s->step_rule == GBMP_STEP_LINF, "unknown step rule");
+    float step_res = 0.f;
+    GBMP_CHECK_ARG(plan_step(s, problems[0].robot ? problems[0].robot->resolution : 0.f, &step_res),
+                   "unknown step rule or resolution out of range");
     int spl = 1;
     bool cull = true;
     size_t smem = 0;
@@ -973,7 +1003,7 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
     prm.max_iters = s->max_iters;
     prm.rule = s->step_rule;
     prm.range = s->range;
-    prm.res = s->resolution > 0.f ? s->resolution : problems[0].robot->resolution;
+    prm.res = step_res;
     prm.seed = 0;
     prm.deadline_ns = 0;
     prm.deadline_ptr = b->d_deadline;
