@@ -41,6 +41,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -289,10 +290,11 @@ PlannerResult<Robot> solve(typename Robot::Configuration &start, std::vector<typ
     s.step_rule = GBMP_STEP_COUNT;
     s.seed = 1;
     s.time_limit_s = 3600.0;
-    std::vector<float> path((std::size_t)path_cap * L);
+    // uninitialised: only the rows of the returned path are ever written or read
+    std::unique_ptr<float[]> path(new float[(std::size_t)path_cap * L]);
     gbmp_rrtc_result r{};
     const auto t1 = Clock::now();
-    st = gbmp_rrtc_solve_goals(planner, env, h_start.data(), h_goals.data(), (int32_t)goals.size(), &s, path.data(),
+    st = gbmp_rrtc_solve_goals(planner, env, h_start.data(), h_goals.data(), (int32_t)goals.size(), &s, path.get(),
                                path_cap, &r, nullptr);
     const auto t2 = Clock::now();
     gbmp_planner_destroy(planner);
