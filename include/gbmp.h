@@ -165,9 +165,11 @@ GBMP_API gbmp_status gbmp_check_states(gbmp_robot robot, gbmp_env env, const flo
  * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read). */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
-/* Planners only: every edge is checked at a fixed count of equal steps, `resolution`
- * rounded down to an integer G >= 1 (the states at k / G of the edge for k = 1..G, the
- * last one the edge's end), pRRTC's `granularity` (pRRTC/src/planning/pRRTC.cu:430-440). */
+/* pRRTC's `granularity` (pRRTC/src/planning/pRRTC.cu:430-440): every edge is checked at
+ * a fixed count of equal steps, `resolution` rounded down to an integer G in [1, 1e6]:
+ * the states at k / G of the edge (k = 0..G in gbmp_check_edges, k = 1..G in the
+ * planners, whose edge start is already a tree node).  Not accepted by
+ * gbmp_check_edges_noalloc. */
 #define GBMP_STEP_COUNT 2
 GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const float *d_from, const float *d_to,
                              int64_t n_edges, float resolution, int32_t step_rule, uint8_t *d_ok,

@@ -138,9 +138,12 @@ __global__ void k_edge_setup(const float *__restrict__ from, const float *__rest
         dinf = fmaxf(dinf, fabsf(d));
     }
     const float len = __fsqrt_rn(d2);
+    // checkMotions: n = floor(metric / res) + 1 states, dir = (to - from) / n; the count
+    // rule (pRRTC's granularity G = res): n = G + 1 states at k / G, dir = (to - from) / G
+    const bool count = rule == GBMP_STEP_COUNT;
     const float metric = rule == GBMP_STEP_LINF ? dinf : len;
-    const int n = (int)__fdiv_rn(metric, res) + 1;
-    const float fn = (float)n;
+    const int n = count ? (int)res + 1 : (int)__fdiv_rn(metric, res) + 1;
+    const float fn = count ? (float)(n - 1) : (float)n;
     for (int j = 0; j < L; ++j) dir[k * L + j] = __fdiv_rn(__fadd_rn(t[j], -f[j]), fn);
     nsteps[k] = n;
     first_hit[k] = INT_MAX;
@@ -783,9 +786,12 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
                              int32_t *d_num_steps, void *stream) {
     GBMP_CHECK_ARG(r && env, "robot/env is NULL");
     GBMP_CHECK_ARG(E >= 0 && E < INT_MAX, "edge count %lld outside [0, 2^31)", (long long)E);
-    GBMP_CHECK_ARG(rule == GBMP_STEP_L2 || rule == GBMP_STEP_LINF, "unknown step rule %d", rule);
+    GBMP_CHECK_ARG(rule == GBMP_STEP_L2 || rule == GBMP_STEP_LINF || rule == GBMP_STEP_COUNT, "unknown step rule %d",
+                   rule);
+    GBMP_CHECK_ARG(rule != GBMP_STEP_COUNT || (res >= 1.f && res <= 1e6f), "step count %g outside [1, 1e6]", res);
     if (E == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
+    if (rule == GBMP_STEP_COUNT) res = floorf(res);
     if (!(res > 0.f)) res = r->resolution;
     GBMP_CHECK_ARG(std::isfinite(res), "resolution is not finite");
     cudaStream_t s = (cudaStream_t)stream;
@@ -805,7 +811,7 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
     const int tb = 256;
     const unsigned blocks = (unsigned)((E + tb - 1) / tb);
-    if (r->use_cg) {
+    if (r->use_cg && rule != GBMP_STEP_COUNT) {   // the generated set-up knows the checkMotions rules
         st = codegen_edge_setup(r, d_from, d_to, E, res, rule, nsteps, dir, fh, liveA, ctr, d_length, d_num_steps, s);
         if (st) return st;
     } else {

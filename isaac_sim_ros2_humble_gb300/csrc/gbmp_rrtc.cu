@@ -166,10 +166,11 @@ __device__ int block_nearest(const float *__restrict__ nodes, int size, int stri
 }
 
 // Validate the edge a -> b (full joint vectors in shared memory) with the step rule of
-// checkMotions: n = floor(metric / res) + 1 states (for GBMP_STEP_COUNT n = res + 1,
-// pRRTC's granularity), state k = a + dir * k, the last state is b; state 0 (= a,
-// already in the tree) is skipped unless n == 1.  One warp per state.  Returns true if
-// every state is collision-free.
+// checkMotions: n = floor(metric / res) + 1 states, dir = (b - a) / n, state k = a +
+// dir * k, the last state is b (for GBMP_STEP_COUNT, pRRTC's granularity G = res:
+// n = G + 1 and dir = (b - a) / G, so the states are at k / G); state 0 (= a, already in
+// the tree) is skipped unless n == 1.  One warp per state.  Returns true if every
+// state is collision-free.
 template <int SPL, bool CULL>
 __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                 const float *a, const float *b, float res, int rule, int *s_flag, float *s_dir,
@@ -193,7 +194,10 @@ __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const De
     }
     __syncthreads();
     const int n = *s_n;
-    for (int j = threadIdx.x; j < R.L; j += blockDim.x) s_dir[j] = __fdiv_rn(__fadd_rn(b[j], -a[j]), (float)n);
+    // checkMotions divides the edge by n (its last state replaced by b); the count rule
+    // by n - 1 = G, so that state k lies at k / G of the edge
+    const float parts = rule == GBMP_STEP_COUNT ? (float)(n - 1) : (float)n;
+    for (int j = threadIdx.x; j < R.L; j += blockDim.x) s_dir[j] = __fdiv_rn(__fadd_rn(b[j], -a[j]), parts);
     __syncthreads();
     for (int k0 = (n == 1 ? 0 : 1); k0 < n; k0 += kRrtcWarps) {
         const int k = k0 + warp;

@@ -471,6 +471,12 @@ int32_t or_edge_steps(const float *from, const float *to, int32_t J, float res, 
     }
     float d = sqrtf(d2);
     if (length) *length = d;
+    if (rule == OR_STEP_COUNT) {   /* pRRTC.cu:430-440: granularity equal steps */
+        int32_t g = (int32_t)res;
+        if (dir)
+            for (int j = 0; j < J; ++j) dir[j] = (to[j] - from[j]) / (float)g;
+        return g + 1;
+    }
     float metric = (rule == OR_STEP_LINF) ? dinf : d;
     int32_t n = (int32_t)(metric / res) + 1;
     if (dir)

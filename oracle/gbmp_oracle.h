@@ -75,6 +75,7 @@ void or_clearance_f64(const or_robot *r, const or_env *e, int32_t npairs, const 
 /* ---- edges ---- */
 #define OR_STEP_L2 0
 #define OR_STEP_LINF 1
+#define OR_STEP_COUNT 2   /* `res` equal steps (pRRTC granularity): n = res + 1, dir = (to - from) / res */
 int32_t or_edge_steps(const float *from, const float *to, int32_t J, float res, int32_t rule,
                       float *dir, float *length);
 void or_edge_state(const float *from, const float *to, const float *dir, int32_t J, int32_t n,

@@ -17,7 +17,7 @@ if _HERE not in sys.path:
     sys.path.insert(0, _HERE)
 import build as _build  # noqa: E402
 
-STEP_L2, STEP_LINF = 0, 1
+STEP_L2, STEP_LINF, STEP_COUNT = 0, 1, 2
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from isaac_sim_ros2_humble_gb300 import api, workloads as W
+from isaac_sim_ros2_humble_gb300 import _lib, api, workloads as W
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -129,6 +129,28 @@ def test_check_edges(edge, rule):
     _edge_parity(m, qf, qt, res, rule, ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(),
                  ns.cpu().numpy())
     assert ok.sum().item() > 0 and ok.sum().item() < n
+
+
+def test_check_edges_count_rule(edge):
+    """pRRTC's granularity as an edge rule: G + 1 states at k / G of every edge, whatever
+    its length, with the same first hits as the oracle; a count outside [1, 1e6] is an
+    argument error."""
+    robot, env, qf, qt, m, R, E = edge
+    n = 256
+    ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    fh = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(n, device="cuda")
+    ns = torch.zeros(n, dtype=torch.int32, device="cuda")
+    api.check_edges(R, E, dev(qf[:n]), dev(qt[:n]), 7, _lib.STEP_COUNT, ok, fh, ln, ns)
+    torch.cuda.synchronize()
+    nsn = ns.cpu().numpy()
+    assert np.all(nsn == 8)
+    _edge_parity(m, qf[:n], qt[:n], 7, O.STEP_COUNT, ok.cpu().numpy().astype(bool), fh.cpu().numpy(),
+                 ln.cpu().numpy(), nsn)
+    st = m.edge_states(qf[0], qt[0], 7, O.STEP_COUNT)
+    np.testing.assert_allclose(st[3], qf[0] + 3 * (qt[0] - qf[0]) / 7, atol=1e-6)   # k / G
+    with pytest.raises(_lib.GbmpError):
+        api.check_edges(R, E, dev(qf[:4]), dev(qt[:4]), 0.5, _lib.STEP_COUNT, ok[:4])
 
 
 def test_check_edges_plain_robot_reference_rule(plain):

@@ -79,3 +79,23 @@ def test_rrtc_node_cap(scene):
     if not res["solved"]:
         assert res["status"] == 2 and res["status_code"] == 7
         assert res["start_tree_size"] <= 16 and res["goal_tree_size"] <= 16
+
+
+def test_rrtc_count_rule_several_goals(scene):
+    """pRRTC's form of a solve: several goals (each a root of the goal tree) and edges
+    checked at a fixed count of equal steps.  The path ends at one of the goals and every
+    state the planner checked on it is collision-free by the oracle."""
+    robot, env, m, free, edge_free, R, E = scene
+    start, g0 = W.pick_problem(free, edge_free, 4)
+    goals = np.stack([g0, free[5], free[9]])
+    G = 8
+    planner = api.Planner(R, max_nodes=200_000, path_cap=8192)
+    res, path = planner.solve(E, start, goals, lanes=512, range_=0.1, resolution=G, rule=_lib.STEP_COUNT, seed=4,
+                              time_limit_s=20.0)
+    assert res["solved"] == 1, res
+    np.testing.assert_array_equal(path[0], start)
+    assert any(np.array_equal(path[-1], g) for g in goals)
+    states = np.concatenate([m.edge_states(a, b, G, O.STEP_COUNT)[1:] for a, b in zip(path[:-1], path[1:])])
+    assert np.all(m.clearance(states) > -1e-4)
+    with pytest.raises(_lib.GbmpError):
+        planner.solve(E, start, goals, resolution=0.5, rule=_lib.STEP_COUNT)

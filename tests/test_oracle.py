@@ -206,3 +206,19 @@ def test_projection_restatement_converges_where_the_method_is_consistent():
     general = O.projection(task_link=tip, reference=[T[0, 3], T[1, 3], T[2, 3]] + rpy,
                            tolerance=(1e-3,) * 3 + (1e-2,) * 3, use_boundary=False)
     assert (m.project(near, general)[1] == 0).mean() < 0.5
+
+
+def test_count_rule_steps():
+    """pRRTC's granularity rule (pRRTC.cu:430-440): G equal steps whatever the edge
+    length, G + 1 states from the start to the end."""
+    robot = W.edge_workload(n_edges=1)[0]
+    m = O.OracleModel(robot)
+    q = robot.sample_full(np.random.default_rng(1), 2)
+    for G in (1, 5, 64):
+        n, d = m.edge_steps(q[0], q[1], G, O.STEP_COUNT)
+        assert n == G + 1
+        st = m.edge_states(q[0], q[1], G, O.STEP_COUNT)
+        np.testing.assert_array_equal(st[0], q[0])
+        np.testing.assert_array_equal(st[-1], q[1])
+        k = min(2, G - 1)
+        np.testing.assert_allclose(st[k], q[0] + k * (q[1] - q[0]) / G, atol=1e-6)
