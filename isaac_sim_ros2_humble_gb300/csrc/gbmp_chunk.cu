@@ -102,6 +102,7 @@ __device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const f
     // is the previous link, else its own earlier store, so no lane waits on another.
     // Rows and joint-local transforms are 16-byte aligned (48-byte poses in a block
     // carved on 16 bytes) and move as float4.
+    static_assert(3 * K <= kWarp, "one lane per pose row of every state of a chunk");
     const int kr = lane / 3, rr = lane - 3 * kr;
     if (lane < 3 * ks) {
         float4 *rowp = reinterpret_cast<float4 *>(lpK + kr * 12 * L) + rr;   // row rr of link 0
