@@ -266,6 +266,15 @@ typedef struct gbmp_rrtc_settings {
     int32_t step_rule;      /* GBMP_STEP_L2, GBMP_STEP_LINF or GBMP_STEP_COUNT             */
     uint64_t seed;          /* Philox key; sample (lane, iteration, joint)                */
     double time_limit_s;    /* device-side deadline (<= 0: 10 s)                          */
+    /* pRRTC's dynamic domain (pRRTC/src/planning/pRRTC.cu:418-424, :456-467, :584-596),
+     * single-problem solves only: a sample farther from its nearest node than that node's
+     * radius is skipped; a failed extension sets the node's radius to dd_radius, or
+     * shrinks it by (1 - dd_alpha) down to dd_min_radius; a successful one grows it by
+     * (1 + dd_alpha).  0 = off (the other three are then ignored). */
+    int32_t dynamic_domain;
+    float dd_alpha;
+    float dd_radius;
+    float dd_min_radius;
 } gbmp_rrtc_settings;
 
 typedef struct gbmp_rrtc_result {

@@ -8,7 +8,8 @@
  * gbmp_rrtc_solve_goals: every goal a root of the goal tree (pRRTC.cu:686-693), each
  * edge checked at `granularity` equal steps (GBMP_STEP_COUNT), `num_new_configs`
  * extension lanes, `range` steering, `max_samples` nodes per tree, `max_iters` lane
- * iterations, Philox samples with key 1 (pRRTC seeds its generators with 1).
+ * iterations, Philox samples with key 1 (pRRTC seeds its generators with 1), and the
+ * dynamic domain with its dd_* settings.
  *
  * The reference's Robot types carry generated FK and collision code.  Here a Robot type
  * names the libgbmp robot model to plan for and the configuration layout:
@@ -29,9 +30,9 @@
  *     first two axes and the z axis, as sphere_z_aligned_cuboid does;
  *   - `cylinders` are not tested by the reference's sphere_environment_in_collision and
  *     are not converted either.
- * Not reproduced: balance strategy 2, tree_ratio, and the dynamic domain (dd_*); they
- * change which samples are kept, not what a valid path is.  Errors other than "no
- * path" are thrown as std::runtime_error with gbmp_last_error().
+ * Not reproduced: balance strategy 2 and tree_ratio (lanes share the trees by the
+ * balance-1 rule); they change which tree a lane grows, not what a valid path is.
+ * Errors other than "no path" are thrown as std::runtime_error with gbmp_last_error().
  */
 #pragma once
 
@@ -290,6 +291,10 @@ PlannerResult<Robot> solve(typename Robot::Configuration &start, std::vector<typ
     s.step_rule = GBMP_STEP_COUNT;
     s.seed = 1;
     s.time_limit_s = 3600.0;
+    s.dynamic_domain = settings.dynamic_domain ? 1 : 0;
+    s.dd_alpha = settings.dd_alpha;
+    s.dd_radius = settings.dd_radius;
+    s.dd_min_radius = settings.dd_min_radius;
     // uninitialised: only the rows of the returned path are ever written or read
     std::unique_ptr<float[]> path(new float[(std::size_t)path_cap * L]);
     gbmp_rrtc_result r{};

@@ -43,7 +43,9 @@ class RobotDesc(C.Structure):
 
 class RrtcSettings(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("max_iters", C.c_int32), ("range", C.c_float), ("resolution", C.c_float),
-                ("step_rule", C.c_int32), ("seed", C.c_uint64), ("time_limit_s", C.c_double)]
+                ("step_rule", C.c_int32), ("seed", C.c_uint64), ("time_limit_s", C.c_double),
+                ("dynamic_domain", C.c_int32), ("dd_alpha", C.c_float), ("dd_radius", C.c_float),
+                ("dd_min_radius", C.c_float)]
 
 
 class RrtcResult(C.Structure):

@@ -200,12 +200,15 @@ class Planner:
 
     def solve(self, env: Env, start, goal, lanes: int = 1024, max_iters: int = 100000, range_: float = 0.1,
               resolution: float = 0.0, rule: int = _lib.STEP_L2, seed: int = 0, time_limit_s: float = 10.0,
-              stream=None, raise_on_failure: bool = False):
+              stream=None, raise_on_failure: bool = False, dynamic_domain: bool = False, dd_alpha: float = 1e-4,
+              dd_radius: float = 4.0, dd_min_radius: float = 1.0):
         """Returns (result, path): result is a dict of the C result struct, path the
         [path_len, L] float32 waypoints (empty when not solved).  `goal` is one full joint
-        vector [L] or several [n, L] (every one a root of the goal tree)."""
+        vector [L] or several [n, L] (every one a root of the goal tree).  dynamic_domain
+        turns on pRRTC's dynamic-domain sampling with its dd_* parameters."""
         st = _lib.RrtcSettings(int(lanes), int(max_iters), float(range_), float(resolution), int(rule), int(seed),
-                               float(time_limit_s))
+                               float(time_limit_s), int(bool(dynamic_domain)), float(dd_alpha), float(dd_radius),
+                               float(dd_min_radius))
         res = _lib.RrtcResult()
         s0 = _c(start, np.float32).reshape(-1)
         g0 = _c(goal, np.float32).reshape(-1, self.robot.L)

@@ -37,6 +37,7 @@ enum : int { kStRunning = 0, kStSolved = 1, kStNodeCap = 2, kStIterCap = 3, kStD
 
 struct RrtcDev {
     float *nodes[2];          // [cap * stride], NaN until written
+    float *radii[2];          // [cap] dynamic-domain radii (kRadiusUnset until a failure), or null
     int *parent[2];           // [cap]
     int *size;                // [2] allocated slots per tree
     int *state;               // [0] status, [1] winning lane, [2] tree of the new node,
@@ -54,7 +55,33 @@ struct RrtcParams {
     unsigned long long seed;
     unsigned long long deadline_ns;   // absolute %globaltimer value, or
     const unsigned long long *deadline_ptr;   // read from device memory when non-null
+    int dd = 0;                       // dynamic domain on (needs RrtcDev::radii)
+    float dd_alpha = 0.f, dd_radius = 0.f, dd_min = 0.f;
 };
+
+// Dynamic-domain radius of a node that has not failed yet (the bytes 0x7f of a memset;
+// 3.4e38, so it never rejects a sample).
+constexpr unsigned kRadiusUnset = 0x7f7f7f7fu;
+
+// Bounded compare-and-swap update of a node's radius: after a failed extension (set to
+// dd_radius if unset, else shrink towards dd_min) or a successful one (grow if set).  A
+// radius is a sampling heuristic, so an update that loses 64 races in a row is dropped.
+__device__ void dd_update(float *radius, bool failed, const RrtcParams &prm) {
+    unsigned *p = reinterpret_cast<unsigned *>(radius);
+    for (int tries = 0; tries < 64; ++tries) {
+        const unsigned old = *(volatile unsigned *)p;
+        float nw;
+        if (old == kRadiusUnset) {
+            if (!failed) return;
+            nw = prm.dd_radius;
+        } else {
+            const float r = __uint_as_float(old);
+            nw = failed ? fmaxf(__fmul_rn(r, __fadd_rn(1.f, -prm.dd_alpha)), prm.dd_min)
+                        : __fmul_rn(r, __fadd_rn(1.f, prm.dd_alpha));
+        }
+        if (atomicCAS(p, old, __float_as_uint(nw)) == old) return;
+    }
+}
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -342,19 +369,26 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
                 if (act[j]) { const float d = __fadd_rn(q_s[j], -q_a[j]); s = __fmaf_rn(d, d, s); }
             const float d = __fsqrt_rn(s);
             s_d[0] = d > prm.range ? __fdiv_rn(prm.range, d) : 1.f;
+            // dynamic domain: a sample beyond the nearest node's radius is skipped
+            s_i[1] = (prm.dd && __uint_as_float(*(volatile unsigned *)(P.radii[tr] + nn)) < d) ? 1 : 0;
         }
         __syncthreads();
         const float scale = s_d[0];
+        const bool outside = s_i[1] != 0;
         __syncthreads();
+        if (outside) continue;
         for (int j = threadIdx.x; j < L; j += blockDim.x)
             if (act[j] && scale < 1.f) q_s[j] = __fmaf_rn(scale, __fadd_rn(q_s[j], -q_a[j]), q_a[j]);
         __syncthreads();
         // 5. validate nn -> new
-        if (!block_edge_free<SPL, CULL>(t, R, E, w, q_a, q_s, prm.res, prm.rule, s_misc + 4, s_dir, s_misc + 5))
+        if (!block_edge_free<SPL, CULL>(t, R, E, w, q_a, q_s, prm.res, prm.rule, s_misc + 4, s_dir, s_misc + 5)) {
+            if (prm.dd && threadIdx.x == 0) dd_update(P.radii[tr] + nn, true, prm);
             continue;
+        }
         // 6. append
         int cur = block_append(P, tr, q_s, nn, L, s_misc + 6);
         if (cur < 0) break;
+        if (prm.dd && threadIdx.x == 0) dd_update(P.radii[tr] + nn, false, prm);
         // 7. connect towards the nearest node of the other tree
         const int tgt = block_nearest(P.nodes[ot], size_o, P.stride, L, act, q_s, s_d, s_i);
         if (tgt < 0) continue;
@@ -417,7 +451,7 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
 }
 
 template <int SPL, bool CULL>
-__global__ void __launch_bounds__(kRrtcThreads) k_rrtc(DevRobot R, DevEnv E, RrtcDev P, RrtcParams prm) {
+__global__ void __launch_bounds__(kRrtcThreads, 5) k_rrtc(DevRobot R, DevEnv E, RrtcDev P, RrtcParams prm) {
     rrtc_lane<SPL, CULL>(R, E, P, prm, blockIdx.x);
 }
 
@@ -636,7 +670,9 @@ gbmp_status gbmp_planner_create(gbmp_robot r, int32_t max_nodes, int32_t path_ca
     p->path_cap = path_cap;
     const size_t nodes_b = align16(sizeof(float) * (size_t)max_nodes * p->stride);
     const size_t par_b = align16(sizeof(int) * (size_t)max_nodes);
-    const size_t bytes = 2 * nodes_b + 2 * par_b + 256 + align16(sizeof(float) * (size_t)path_cap * r->L);
+    const size_t path_b = align16(sizeof(float) * (size_t)path_cap * r->L);
+    const size_t rad_b = align16(sizeof(float) * (size_t)max_nodes);   // dynamic-domain radii, per tree
+    const size_t bytes = 2 * nodes_b + 2 * par_b + 256 + path_b + 2 * rad_b;
     cudaError_t e = cudaMalloc(&p->block, bytes);
     if (e != cudaSuccess) {
         delete p;
@@ -651,6 +687,8 @@ gbmp_status gbmp_planner_create(gbmp_robot r, int32_t max_nodes, int32_t path_ca
     D.size = ints; D.state = ints + 4; D.path_len = ints + 16;
     D.path = (float *)(b + 2 * nodes_b + 2 * par_b + 256);
     D.cap = max_nodes; D.stride = p->stride; D.path_cap = path_cap;
+    D.radii[0] = (float *)(b + 2 * nodes_b + 2 * par_b + 256 + path_b);
+    D.radii[1] = (float *)(b + 2 * nodes_b + 2 * par_b + 256 + path_b + rad_b);
     *out = p;
     return GBMP_OK;
 }
@@ -680,6 +718,9 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     GBMP_CHECK_ARG(s->max_iters >= 1, "max_iters < 1");
     float step_res = 0.f;
     GBMP_CHECK_ARG(plan_step(s, r->resolution, &step_res), "unknown step rule or resolution out of range");
+    GBMP_CHECK_ARG(!s->dynamic_domain || (s->dd_alpha >= 0.f && s->dd_alpha < 1.f && s->dd_radius > 0.f &&
+                                          s->dd_min_radius > 0.f && std::isfinite(s->dd_radius)),
+                   "dynamic domain needs 0 <= dd_alpha < 1 and positive radii");
     for (int j = 0; j < L; ++j) GBMP_CHECK_ARG(std::isfinite(h_start[j]), "start not finite");
     for (long long j = 0; j < (long long)n_goals * L; ++j) GBMP_CHECK_ARG(std::isfinite(h_goals[j]), "goal not finite");
     memset(res, 0, sizeof *res);
@@ -689,6 +730,10 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     GBMP_CUDA(cudaMemsetAsync(D.nodes[0], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
     GBMP_CUDA(cudaMemsetAsync(D.nodes[1], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
     GBMP_CUDA(cudaMemsetAsync(D.size, 0, 256, st));
+    if (s->dynamic_domain) {   // every radius unset (kRadiusUnset = bytes 0x7f)
+        GBMP_CUDA(cudaMemsetAsync(D.radii[0], 0x7f, sizeof(float) * (size_t)p->cap, st));
+        GBMP_CUDA(cudaMemsetAsync(D.radii[1], 0x7f, sizeof(float) * (size_t)p->cap, st));
+    }
     // the goal tree starts with every goal as a root (a node that is its own parent)
     std::vector<int> h_init{1, n_goals}, h_roots(n_goals);
     for (int g = 0; g < n_goals; ++g) h_roots[g] = g;
@@ -711,6 +756,10 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     prm.range = s->range;
     prm.res = step_res;
     prm.seed = s->seed;
+    prm.dd = s->dynamic_domain ? 1 : 0;
+    prm.dd_alpha = s->dd_alpha;
+    prm.dd_radius = s->dd_radius;
+    prm.dd_min = s->dd_min_radius;
     // device deadline from the host clock offset: read %globaltimer through a 1-thread probe
     unsigned long long now_ns = 0;
     {
@@ -988,6 +1037,7 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
         bp.P.path = (float *)(base + 2 * nodes_b + 2 * par_b + 256);
         bp.P.cap = b->cap;
         bp.P.stride = (pr.robot->L + 3) & ~3;   // its own joints, padded to float4 words
+        bp.P.radii[0] = bp.P.radii[1] = nullptr;  // no dynamic domain in batched solves
         bp.P.path_cap = b->path_cap;
         bp.P.flag = b->d_flags + i;
         bp.seed = pr.seed;

@@ -99,3 +99,20 @@ def test_rrtc_count_rule_several_goals(scene):
     assert np.all(m.clearance(states) > -1e-4)
     with pytest.raises(_lib.GbmpError):
         planner.solve(E, start, goals, resolution=0.5, rule=_lib.STEP_COUNT)
+
+
+def test_rrtc_dynamic_domain_paths_are_valid(scene):
+    """pRRTC's dynamic domain (samples beyond a node's radius skipped, radii set, shrunk
+    and grown as extensions fail and succeed) changes which samples are used, not what a
+    valid path is; bad parameters are argument errors."""
+    robot, env, m, free, edge_free, R, E = scene
+    start, goal = W.pick_problem(free, edge_free, 1)
+    planner = api.Planner(R, max_nodes=200_000, path_cap=8192)
+    for dd_radius in (4.0, 0.3):
+        res, path = planner.solve(E, start, goal, lanes=512, range_=0.1, resolution=RES, rule=RULE, seed=1,
+                                  time_limit_s=20.0, dynamic_domain=True, dd_alpha=1e-3, dd_radius=dd_radius,
+                                  dd_min_radius=0.2)
+        assert res["solved"] == 1, res
+        _validate_path(m, path, start, goal)
+    with pytest.raises(_lib.GbmpError):
+        planner.solve(E, start, goal, resolution=RES, rule=RULE, dynamic_domain=True, dd_alpha=1.5)
