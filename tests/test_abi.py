@@ -102,3 +102,33 @@ def test_other_invalid_descriptors():
     assert lib.gbmp_check_states(None, None, None, 1, 0, None, None, None, None) == 1
     assert lib.gbmp_check_edges(None, None, None, None, 1, 0.0, 0, None, None, None, None, None) == 1
     assert lib.gbmp_robot_destroy(None) == 0
+
+
+def test_struct_layouts_match_ctypes(tmp_path):
+    """Every struct of the C-ABI has the size and field offsets the ctypes binding
+    declares (gcc compiles a program that prints them from include/gbmp.h)."""
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    pairs = {"gbmp_robot_desc": _lib.RobotDesc, "gbmp_limits": _lib.Limits, "gbmp_projection": _lib.Projection,
+             "gbmp_rrtc_settings": _lib.RrtcSettings, "gbmp_rrtc_result": _lib.RrtcResult,
+             "gbmp_rrtc_problem": _lib.RrtcProblem, "gbmp_server_config": _lib.ServerConfig,
+             "gbmp_request_info": _lib.RequestInfo, "gbmp_server_metrics": _lib.ServerMetrics}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "gbmp.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", inc, str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (ln.split() for ln in out if ln)}
+    for cname, cls in pairs.items():
+        assert got[(cname, "sizeof")] == C.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
