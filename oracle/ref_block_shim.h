@@ -36,6 +36,10 @@ inline std::barrier<> *ref_block_barrier = nullptr;
 
 inline void __syncthreads() { ref_block_barrier->arrive_and_wait(); }
 
+// CUDA's device overloads of min / max for floats (fminf / fmaxf semantics).
+inline float max(float a, float b) { return fmaxf(a, b); }
+inline float min(float a, float b) { return fminf(a, b); }
+
 // Host stand-ins for the allocation calls of the constructors (host memory).
 enum RefMemcpyKind { cudaMemcpyHostToDevice = 1, cudaMemcpyDeviceToHost = 2, cudaMemcpyDeviceToDevice = 3 };
 template <class T>
@@ -50,6 +54,20 @@ inline int cudaMemcpy(void *dst, const void *src, size_t bytes, int) {
 inline int cudaFree(void *p) {
     std::free(p);
     return 0;
+}
+
+// Runs `kernel()` for every (block, thread) of a launch on the calling thread, in order;
+// for kernels without barriers or shared memory.
+template <class F>
+inline void ref_serial_launch(int grid, int block, F kernel) {
+    blockDim = {(unsigned)block, 1, 1};
+    for (int b = 0; b < grid; ++b) {
+        blockIdx = {(unsigned)b, 0, 0};
+        for (int t = 0; t < block; ++t) {
+            threadIdx = {(unsigned)t, 0, 0};
+            kernel();
+        }
+    }
 }
 
 // Runs `kernel()` as a launch of `grid` blocks of `block` threads.

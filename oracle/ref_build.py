@@ -359,5 +359,131 @@ def manager_kernels():
     return lib
 
 
+# SingleArmSpace::projectStates (SingleArmSpace.cu:1631-1712): the table FK kernel and its
+# helpers (SingleArmStates.cu:11-221), the task-space and boundary gradient and cost
+# kernels (TaskSpaceConstraint.cu, BoundaryConstraint.cu), the gradient sum
+# (SingleArmStates.cu:819-845) and update_with_grad (SingleArmSpace.cu:1604-1626), taken
+# the same way.  Each source's kernels sit in a namespace of their own (the two
+# constraint files both name their kernel computeGradientErrorKernel and both define
+# multiply4x4).
+REF_SPACE = "/root/reference/cudampl/CUDAMPLib/src/spaces/SingleArmSpace.cu"
+REF_TASK = os.path.join(REF_SRC, "TaskSpaceConstraint.cu")
+REF_BOUND = os.path.join(REF_SRC, "BoundaryConstraint.cu")
+
+_PROJECT_HARNESS = r'''
+#include "ref_block_shim.h"
+#include <vector>
+
+#define CUDAMPLib_UNKNOWN 0
+#define CUDAMPLib_REVOLUTE 1
+#define CUDAMPLib_PRISMATIC 2
+#define CUDAMPLib_FIXED 5
+
+namespace CUDAMPLib {
+namespace fk {
+%(fk)s
+}
+namespace ts {
+%(ts)s
+}
+namespace bd {
+%(bd)s
+}
+namespace sp {
+%(sp)s
+}
+}  // namespace CUDAMPLib
+
+// `iterations` rounds of projectStates on q [n*L] (in place), then the final costs of
+// both constraints (each output optional; a disabled constraint's cost is 0).
+extern "C" void ref_project(int n, int L, int *types, float *poses, float *axes, int *parent, int *active,
+                            float *lower, float *upper, int task_link, float *offset, float *reference,
+                            float *tolerance, int use_boundary, int iterations, float *q, float *task_cost,
+                            float *bound_cost) {
+    using namespace CUDAMPLib;
+    int A = 0;
+    for (int j = 0; j < L; ++j) A += active[j] != 0;
+    std::vector<float> lp((size_t)n * L * 16), jac((size_t)n * L * 6), jinv((size_t)n * A * 6 + 1);
+    std::vector<float> grad(2 * (size_t)n * L, 0.f), cost(2 * (size_t)n, 0.f), tgrad((size_t)n * L, 0.f);
+    std::vector<int> idx;
+    if (task_link >= 0) idx.push_back(0);
+    if (use_boundary) idx.push_back(1);
+    const int nb = (n + 255) / 256, nbj = (n * L + 255) / 256;
+    auto fk_all = [&] {
+        ref_serial_launch(nb, 256, [&] { fk::kin_forward_kernel(q, L, n, types, poses, L, axes, parent, lp.data()); });
+    };
+    for (int it = 0; it < iterations; ++it) {
+        fk_all();
+        if (task_link >= 0)
+            ref_serial_launch(nb, 256, [&] {
+                ts::computeGradientErrorKernel(n, lp.data(), L, L, types, axes, task_link, offset, reference, tolerance,
+                                               active, A, jac.data(), jinv.data(), grad.data(), cost.data());
+            });
+        if (use_boundary)
+            ref_serial_launch(nb, 256, [&] {
+                bd::computeGradientErrorKernel(q, active, lower, upper, n, L, cost.data() + n,
+                                               grad.data() + (size_t)n * L);
+            });
+        if (idx.empty()) continue;
+        ref_serial_launch(nbj, 256, [&] {
+            fk::sum_gradients_kernel(n, L, 2, idx.data(), (int)idx.size(), grad.data(), tgrad.data());
+        });
+        ref_serial_launch(nbj, 256, [&] { sp::update_with_grad(q, tgrad.data(), 1.0f, n, L, active); });
+    }
+    fk_all();
+    if (task_cost) {
+        if (task_link >= 0)
+            ref_serial_launch(nb, 256, [&] {
+                ts::computeTaskSpaceCostKernel(n, lp.data(), L, task_link, offset, reference, tolerance, 0.0001f,
+                                               task_cost);
+            });
+        else
+            for (int i = 0; i < n; ++i) task_cost[i] = 0.f;
+    }
+    if (bound_cost) {
+        if (use_boundary)
+            ref_serial_launch(nb, 256, [&] {
+                bd::computeBoundaryCostKernel(q, active, lower, upper, n, L, 0.0001f, bound_cost);
+            });
+        else
+            for (int i = 0; i < n; ++i) bound_cost[i] = 0.f;
+    }
+}
+'''
+
+
+def project_available() -> bool:
+    return all(os.path.exists(f) for f in (REF_STATES, REF_SPACE, REF_TASK, REF_BOUND))
+
+
+def project_kernels():
+    """ctypes library with ref_project (the reference's projection kernels), or None
+    without the reference tree."""
+    if not project_available():
+        return None
+    st, sp_, ts_, bd_ = (open(f).read() for f in (REF_STATES, REF_SPACE, REF_TASK, REF_BOUND))
+    fk_names = ["__device__ __forceinline__ void multiply4x4(", "__device__ __forceinline__ void set_identity(",
+                "__device__ __forceinline__ void fixed_joint_fn_cuda(",
+                "__device__ __forceinline__ void make_rotation_axis_angle(",
+                "__device__ __forceinline__ void revolute_joint_fn_cuda(",
+                "__device__ __forceinline__ void prism_joint_fn_cuda(", "__global__ void kin_forward_kernel(",
+                "__global__ void sum_gradients_kernel("]
+    parts = dict(
+        fk="\n\n".join(_extract(st, n) for n in fk_names),
+        ts="\n\n".join(_extract(ts_, n) for n in ("__device__ __forceinline__ void multiply4x4(",
+                                                   "__global__ void computeTaskSpaceCostKernel(",
+                                                   "__global__ void computeGradientErrorKernel(")),
+        bd="\n\n".join(_extract(bd_, n) for n in ("__global__ void computeBoundaryCostKernel(",
+                                                   "__global__ void computeGradientErrorKernel(")),
+        sp=_extract(sp_, "__global__ void update_with_grad("),
+    )
+    lib = C.CDLL(_host_library("ref_project", _PROJECT_HARNESS % parts, "-std=c++20"))
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    lib.ref_project.argtypes = [C.c_int, C.c_int, i32p, f32p, f32p, i32p, i32p, f32p, f32p, C.c_int, f32p, f32p,
+                                f32p, C.c_int, C.c_int, f32p, f32p, f32p]
+    return lib
+
+
 if __name__ == "__main__":
     print(build(force=True))

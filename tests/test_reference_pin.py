@@ -158,3 +158,71 @@ def test_sphere_transform_matches_reference_kernel(idx):
     assert np.mean(out == o) > 0.9
     p64 = m.sphere_centers(m.fk(q.astype(np.float64), f64=True))
     assert np.abs(out - p64).max() < 1e-6
+
+
+@pytest.mark.skipif(not ref_build.project_available(), reason="reference projection sources not present")
+def test_projection_matches_reference_kernels():
+    """SingleArmSpace::projectStates from the reference's own kernels (table FK, the
+    task-space and boundary gradients, their sum, update_with_grad, then the two cost
+    kernels), run on the host, against the oracle's restatement.  The step solves a
+    damped 6x6 system whose conditioning (up to ~1e4) amplifies last-bit differences of
+    compiled arithmetic, so: the joint-limit pull alone is compared to the bit; costs
+    with no iteration within 1e-5; one iteration on the states whose oracle step moves
+    less than 1e-5 when the joints move by one ulp, within 1e-4; ten iterations on
+    position targets reach the region on the same states but for at most 6 %."""
+    import math
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    m = O.OracleModel(robot)
+    ref = ref_build.project_kernels()
+    L = robot.num_links
+    tip = L - 1
+    q0 = robot.sample_full(np.random.default_rng(3), 1)
+    T = W.fk_numpy(robot, q0)[0][tip]
+    off = np.eye(4, dtype=np.float32)
+    off[:3, :3] = T[:3, :3].T
+    target = [float(T[0, 3]), float(T[1, 3]), float(T[2, 3]), 0.0, 0.0, 0.0]
+    f32 = lambda a: np.ascontiguousarray(a, np.float32).reshape(-1)
+    i32 = lambda a: np.ascontiguousarray(a, np.int32).reshape(-1)
+
+    def run_ref(q, task_link, tol, use_boundary, iterations):
+        qq = np.ascontiguousarray(q, np.float32).copy()
+        tc, bc = np.zeros(len(q), np.float32), np.zeros(len(q), np.float32)
+        ref.ref_project(len(q), L, i32(robot.joint_types), f32(robot.joint_poses), f32(robot.joint_axes),
+                        i32(robot.parent), i32(robot.active), f32(robot.lower), f32(robot.upper), task_link,
+                        f32(off), f32(target), f32(tol), int(use_boundary), iterations, qq.reshape(-1), tc, bc)
+        return qq, tc, bc
+
+    def run_oracle(q, task_link, tol, use_boundary, iterations):
+        return m.project(q, O.projection(task_link=task_link, offset=off, reference=target, tolerance=tol,
+                                         use_boundary=use_boundary, iterations=iterations))
+
+    rng = np.random.default_rng(8)
+    act = robot.active.astype(bool)
+    # joint-limit pull alone: to the bit
+    q = robot.sample_full(rng, 400)
+    q[:, act] += rng.uniform(-1.0, 1.0, size=(400, act.sum())).astype(np.float32)
+    zero_tol = (0.0,) * 6
+    a, b = run_ref(q, -1, zero_tol, True, 1), run_oracle(q, -1, zero_tol, True, 1)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[2], b[2])
+    # costs with no iteration
+    q = (q0 + 0.1 * rng.standard_normal((600, L)) * robot.active).astype(np.float32)
+    tol = (1e-3,) * 3 + (1e-2,) * 3
+    a, b = run_ref(q, tip, tol, True, 0), run_oracle(q, tip, tol, True, 0)
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(a[2], b[2], rtol=1e-4, atol=1e-5)
+    # one iteration, on the states whose oracle step is insensitive to rounding
+    a, b = run_ref(q, tip, tol, True, 1), run_oracle(q, tip, tol, True, 1)
+    q_ulp = q.copy()
+    q_ulp[:, act] = np.nextafter(q[:, act], np.float32(np.inf))
+    bu = run_oracle(q_ulp, tip, tol, True, 1)
+    stable = np.abs(bu[0] - b[0]).max(axis=1) < 1e-5
+    assert stable.mean() > 0.8
+    assert np.abs(a[0][stable] - b[0][stable]).max() < 1e-4
+    # ten iterations on a position target: the same states reach the region
+    tol = (1e-3,) * 3 + (2 * math.pi,) * 3
+    q = (q0 + 0.15 * rng.standard_normal((600, L)) * robot.active).astype(np.float32)
+    a, b = run_ref(q, tip, tol, False, 10), run_oracle(q, tip, tol, False, 10)
+    reached_a, reached_b = a[1] == 0, b[1] == 0
+    assert reached_b.mean() > 0.5
+    assert np.mean(reached_a != reached_b) <= 0.06
