@@ -394,6 +394,15 @@ namespace sp {
 }
 }  // namespace CUDAMPLib
 
+// The table-driven FK kernel alone (SingleArmStates::calculateForwardKinematics):
+// link poses [n*L*16] of q [n*L].
+extern "C" void ref_table_fk(int n, int L, int *types, float *poses, float *axes, int *parent, float *q,
+                             float *out) {
+    ref_serial_launch((n + 255) / 256, 256, [&] {
+        CUDAMPLib::fk::kin_forward_kernel(q, L, n, types, poses, L, axes, parent, out);
+    });
+}
+
 // `iterations` rounds of projectStates on q [n*L] (in place), then the final costs of
 // both constraints (each output optional; a disabled constraint's cost is 0).
 extern "C" void ref_project(int n, int L, int *types, float *poses, float *axes, int *parent, int *active,
@@ -457,8 +466,8 @@ def project_available() -> bool:
 
 
 def project_kernels():
-    """ctypes library with ref_project (the reference's projection kernels), or None
-    without the reference tree."""
+    """ctypes library with ref_project (the reference's projection kernels) and
+    ref_table_fk (its table-driven FK kernel), or None without the reference tree."""
     if not project_available():
         return None
     st, sp_, ts_, bd_ = (open(f).read() for f in (REF_STATES, REF_SPACE, REF_TASK, REF_BOUND))
@@ -480,6 +489,7 @@ def project_kernels():
     lib = C.CDLL(_host_library("ref_project", _PROJECT_HARNESS % parts, "-std=c++20"))
     f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
     i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    lib.ref_table_fk.argtypes = [C.c_int, C.c_int, i32p, f32p, f32p, i32p, f32p, f32p]
     lib.ref_project.argtypes = [C.c_int, C.c_int, i32p, f32p, f32p, i32p, i32p, f32p, f32p, C.c_int, f32p, f32p,
                                 f32p, C.c_int, C.c_int, f32p, f32p, f32p]
     return lib

@@ -226,3 +226,23 @@ def test_projection_matches_reference_kernels():
     reached_a, reached_b = a[1] == 0, b[1] == 0
     assert reached_b.mean() > 0.5
     assert np.mean(reached_a != reached_b) <= 0.06
+
+
+@pytest.mark.skipif(not ref_build.project_available(), reason="reference state sources not present")
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_table_fk_matches_reference_kernel(idx):
+    """The reference's table-driven FK kernel (SingleArmStates.cu:11-221, used by
+    calculateForwardKinematics and the projection) against the oracle: within 1e-5 of
+    FP64 like the oracle's own FP32 FK, and within 1e-5 of it."""
+    robot = robots()[idx]
+    q = robot.sample_full(np.random.default_rng(40 + idx), 2000)
+    out = np.zeros((q.shape[0], robot.num_links, 16), np.float32)
+    f32 = lambda a: np.ascontiguousarray(a, np.float32).reshape(-1)
+    i32 = lambda a: np.ascontiguousarray(a, np.int32).reshape(-1)
+    ref_build.project_kernels().ref_table_fk(q.shape[0], robot.num_links, i32(robot.joint_types),
+                                             f32(robot.joint_poses), f32(robot.joint_axes), i32(robot.parent),
+                                             f32(q), out.reshape(-1))
+    m = O.OracleModel(robot)
+    p64 = m.fk(q.astype(np.float64), f64=True)
+    assert np.abs(out[:, :, :12] - p64[:, :, :12]).max() < 1e-5
+    assert np.abs(out[:, :, :12] - m.fk(q)[:, :, :12]).max() < 1e-5
