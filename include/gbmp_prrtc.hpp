@@ -216,7 +216,8 @@ struct SceneArrays {
     }
 };
 
-inline gbmp_env make_env(const ppln::collision::Environment<float> &e) {
+// The libgbmp form of a pRRTC environment (pure conversion, no device work).
+inline SceneArrays scene_arrays(const ppln::collision::Environment<float> &e) {
     SceneArrays a;
     for (unsigned i = 0; i < e.num_spheres; ++i) a.sphere(e.spheres[i].x, e.spheres[i].y, e.spheres[i].z, e.spheres[i].r);
     for (unsigned i = 0; i < e.num_capsules; ++i) {
@@ -239,6 +240,11 @@ inline gbmp_env make_env(const ppln::collision::Environment<float> &e) {
                     a3[3] = {0.f, 0.f, 1.f};
         a.cuboid(c.x, c.y, c.z, a1, a2, a3, c.axis_1_r, c.axis_2_r, c.axis_3_r);
     }
+    return a;
+}
+
+inline gbmp_env make_env(const ppln::collision::Environment<float> &e) {
+    SceneArrays a = scene_arrays(e);
     gbmp_env env = nullptr;
     check(gbmp_env_create((int32_t)a.sph_r.size(), a.sph_pos.data(), a.sph_r.data(), (int32_t)a.box_min.size() / 3,
                           a.box_pos.data(), a.box_rot.data(), a.box_min.data(), a.box_max.data(),

@@ -495,5 +495,102 @@ def project_kernels():
     return lib
 
 
+# pRRTC's sphere-versus-environment test (pRRTC/src/planning/utils.cuh:15-242: the shape
+# distance functions and sphere_environment_in_collision), over the reference's own
+# shape and environment types (pRRTC/src/collision/shapes.hh, environment.hh, math.hh,
+# included where they lie).
+REF_PRRTC = "/root/reference/pRRTC/src"
+
+_PRRTC_HARNESS = r'''
+#include <array>
+#include "ref_block_shim.h"
+#include "shapes.hh"
+#include "environment.hh"
+
+namespace ppln::device_utils {
+// the device overload of abs for floats
+constexpr float abs(float x) { return x < 0.f ? -x : x; }
+}
+
+%(utils)s
+}  // namespace ppln::device_utils
+
+// Per configuration, 1 if any of its S spheres (centres cen [n*S*3], radii rad [S])
+// collides with the environment: spheres [ns*4] (x y z r), capsules and z-aligned
+// capsules [*7] (x1 y1 z1 xv yv zv r), cuboids and z-aligned cuboids [*15] (x y z,
+// three axes, three half extents).
+extern "C" void ref_prrtc_collide(int n, int S, float *cen, float *rad, int ns, float *sph, int nc, float *cap,
+                                  int nzc, float *zcap, int nb, float *cub, int nzb, float *zcub,
+                                  unsigned char *out) {
+    using namespace ppln::collision;
+    Environment<float> env;
+    env.spheres = new Sphere<float>[ns];
+    env.num_spheres = ns;
+    for (int i = 0; i < ns; ++i) env.spheres[i] = Sphere<float>(sph[4 * i], sph[4 * i + 1], sph[4 * i + 2], sph[4 * i + 3]);
+    auto caps = [](float *c, int k) {
+        Capsule<float> *a = new Capsule<float>[k];
+        for (int i = 0; i < k; ++i) {
+            float *v = c + 7 * i;
+            a[i] = Capsule<float>(v[0], v[1], v[2], v[3], v[4], v[5], v[6], 1.f / (v[3] * v[3] + v[4] * v[4] + v[5] * v[5]));
+        }
+        return a;
+    };
+    auto cubs = [](float *c, int k) {
+        Cuboid<float> *a = new Cuboid<float>[k];
+        for (int i = 0; i < k; ++i) {
+            float *v = c + 15 * i;
+            a[i] = Cuboid<float>(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12],
+                                 v[13], v[14]);
+        }
+        return a;
+    };
+    env.capsules = caps(cap, nc);
+    env.num_capsules = nc;
+    env.z_aligned_capsules = caps(zcap, nzc);
+    env.num_z_aligned_capsules = nzc;
+    env.cylinders = nullptr;
+    env.num_cylinders = 0;
+    env.cuboids = cubs(cub, nb);
+    env.num_cuboids = nb;
+    env.z_aligned_cuboids = cubs(zcub, nzb);
+    env.num_z_aligned_cuboids = nzb;
+    for (int s = 0; s < n; ++s) {
+        bool hit = false;
+        for (int k = 0; k < S && !hit; ++k) {
+            const float *c = cen + 3 * ((size_t)s * S + k);
+            hit = ppln::device_utils::sphere_environment_in_collision(&env, c[0], c[1], c[2], rad[k]);
+        }
+        out[s] = hit ? 1 : 0;
+    }
+}
+'''
+
+
+def prrtc_available() -> bool:
+    return os.path.exists(os.path.join(REF_PRRTC, "planning", "utils.cuh")) and \
+        os.path.exists(os.path.join(REF_PRRTC, "collision", "shapes.hh"))
+
+
+def prrtc_collision():
+    """ctypes library with ref_prrtc_collide (pRRTC's own sphere / capsule / cuboid
+    tests), or None without the reference tree."""
+    if not prrtc_available():
+        return None
+    text = open(os.path.join(REF_PRRTC, "planning", "utils.cuh")).read()
+    sig = "__device__ __forceinline__ bool sphere_environment_in_collision("
+    i = text.index("namespace ppln::device_utils {")
+    end = text.index(sig) + len(_extract(text, sig))
+    src = _PRRTC_HARNESS % dict(utils=text[i:end])
+    so_path = _host_library("ref_prrtc", src.replace('#include "shapes.hh"', '#include "%s"' % os.path.join(
+        REF_PRRTC, "collision", "shapes.hh")).replace('#include "environment.hh"', '#include "%s"' % os.path.join(
+            REF_PRRTC, "collision", "environment.hh")), "-std=c++20")
+    lib = C.CDLL(so_path)
+    f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+    u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+    lib.ref_prrtc_collide.argtypes = [C.c_int, C.c_int, f32p, f32p, C.c_int, f32p, C.c_int, f32p, C.c_int, f32p,
+                                      C.c_int, f32p, C.c_int, f32p, u8p]
+    return lib
+
+
 if __name__ == "__main__":
     print(build(force=True))

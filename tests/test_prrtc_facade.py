@@ -162,3 +162,50 @@ def test_prrtc_solve_multi_goal_path_is_valid(tmp_path):
     assert pen.max() <= BAND, pen.max()
     self_only = O.OracleModel(robot)
     assert np.all(self_only.clearance(states) > -BAND)
+
+
+def test_scene_conversion_matches_prrtc_collision(tmp_path):
+    """The scene the header builds from a pRRTC environment (gbmp_prrtc_detail::
+    scene_arrays, printed by a program without device work) collides, by the oracle,
+    with the same robot configurations as pRRTC's own sphere_environment_in_collision
+    (pRRTC/src/planning/utils.cuh, compiled for the host over the reference's shape
+    types) says, but for configurations within 1e-4 m of contact."""
+    import shutil
+    import ref_build
+    if not ref_build.prrtc_available() or shutil.which("g++") is None:
+        pytest.skip("pRRTC sources or g++ not present")
+    exe = tmp_path / "dump"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "prrtc_scene_dump.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    shapes = _scene()
+    f = lambda a: " ".join("%.9g" % v for v in np.asarray(a, np.float64).ravel())
+    lines = []
+    for arr in shapes:
+        lines.append(str(len(arr)))
+        lines += [f(row) for row in arr]
+    (tmp_path / "s.txt").write_text("\n".join(lines) + "\n")
+    r = subprocess.run([str(exe), str(tmp_path / "s.txt"), str(tmp_path / "o.txt")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = _read_results(tmp_path / "o.txt")
+    f32 = lambda k, s: np.asarray(got[k], np.float32).reshape(s)
+    env = W.Environment(f32("sph_pos", (-1, 3)), f32("sph_r", (-1,)), f32("box_pos", (-1, 3)),
+                        f32("box_rot", (-1, 3, 3)), f32("box_min", (-1, 3)), f32("box_max", (-1, 3)),
+                        f32("cyl_pos", (-1, 3)), f32("cyl_rot", (-1, 3, 3)), f32("cyl_r", (-1,)), f32("cyl_h", (-1,)))
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    m = O.OracleModel(robot, env)
+    q = robot.sample_full(np.random.default_rng(0), 3000)
+    oc, _ = m.check_states(q)
+    env_hit = (oc[1] + oc[2] + oc[3]) > 0
+    cen = np.ascontiguousarray(m.sphere_centers(m.fk(q)), np.float32)
+    rad = np.ascontiguousarray(robot.sphere_r, np.float32)
+    c = lambda a: np.ascontiguousarray(a, np.float32).reshape(-1)
+    sph, cap, zcap, cub, zcub = shapes
+    out = np.zeros(len(q), np.uint8)
+    ref_build.prrtc_collision().ref_prrtc_collide(len(q), robot.num_spheres, c(cen), rad, len(sph), c(sph), len(cap),
+                                                  c(cap), len(zcap), c(zcap), len(cub), c(cub), len(zcub), c(zcub), out)
+    assert 0.1 < env_hit.mean() < 0.9
+    bad = (out != 0) != env_hit
+    pen = _penetration(cen.astype(np.float64), rad.astype(np.float64), *[s.astype(np.float64) for s in shapes])
+    assert np.all(np.abs(pen[bad]) <= BAND), (bad.sum(), np.abs(pen[bad]).max() if bad.any() else 0)
