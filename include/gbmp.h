@@ -162,7 +162,10 @@ GBMP_API gbmp_status gbmp_check_states(gbmp_robot robot, gbmp_env env, const flo
  * colliding state index or -1; d_length[E] L2 length (the reference's motion cost);
  * d_num_steps[E] interpolated state count.  step_rule GBMP_STEP_L2 is the reference
  * rule; GBMP_STEP_LINF bounds the per-joint step by `resolution` instead.
- * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read). */
+ * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read).
+ * Robots of up to 32 sphere-carrying links are validated by chunks of 8 consecutive
+ * states a warp, others state by state; the environment variable GBMP_EDGE_CHUNK
+ * overrides the form for tuning and tests (0 or 1: state by state, 4 or 8: chunks). */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
 /* pRRTC's `granularity` (pRRTC/src/planning/pRRTC.cu:430-440): every edge is checked at
