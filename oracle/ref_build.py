@@ -592,5 +592,19 @@ def prrtc_collision():
     return lib
 
 
+def build_all():
+    """Every reference-pinning tool that the reference tree allows (none without it):
+    the kernel generator, the collision-cost, state, projection and pRRTC collision
+    libraries.  Returns the names built."""
+    built = []
+    if build() is not None:
+        built.append("ref_gen")
+    for name, fn in (("costs", cost_kernels), ("manager", manager_kernels), ("project", project_kernels),
+                     ("prrtc", prrtc_collision)):
+        if fn() is not None:
+            built.append(name)
+    return built
+
+
 if __name__ == "__main__":
-    print(build(force=True))
+    print(build(force=True), build_all())
