@@ -3,10 +3,10 @@
 // The interpolated states of one edge lie millimetres apart, so the obstacles near one
 // state are the obstacles near its neighbours.  A warp takes K consecutive states of
 // one edge (a chunk) and
-//   A. runs the FK of all K states together (the K link chains advance in lock step,
-//      each lane owning (state, pose element) slots), keeping the link poses in shared
-//      memory, and bounds the centre of every sphere group (a link's bounding sphere)
-//      over the chunk by an axis-aligned box;
+//   A. runs the FK of all K states together (the joint-local transforms spread over the
+//      lanes, then one lane per pose row of each state walking the chain), keeping the
+//      link poses in shared memory, and bounds the centre of every sphere group (a
+//      link's bounding sphere) over the chunk by an axis-aligned box;
 //   B. turns each box into a swept group sphere: centre = box centre, radius = half the
 //      box diagonal + the group radius (which already carries kBroadMargin);
 //   C. runs the broad phase ONCE for the chunk: the bounding sphere of every run of 32
