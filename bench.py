@@ -1,21 +1,35 @@
 #!/usr/bin/env python
-"""Benchmark: interpolated-edge validation (FK + sphere collision) on one GB300.
+"""Benchmark of the motion-planning hot path on one GB300.
 
-Workload: 65,536 random edges of an 8-DOF arm (prismatic torso 0-0.4 m + 7 revolute
-joints, 110 link spheres) in a scene of 256 spheres, 64 oriented boxes and 16
-cylinders, interpolated at 0.01 rad maximum joint step; output per edge: collision
-flag and first-collision state index.  Synthetic, seeded inputs (no dataset).
+Headline (`value`, `e2e`): interpolated-edge validation (FK + sphere collision).
+65,536 random edges of an 8-DOF arm (prismatic torso 0-0.4 m + 7 revolute joints, 110
+link spheres) in a scene of 256 spheres, 64 oriented boxes and 16 cylinders,
+interpolated at 0.01 rad maximum joint step; output per edge: collision flag and
+first-collision state index.  Synthetic, seeded inputs (no dataset).
 
-Metric: FK+collision checks/s, where the checks of a batch are the interpolated
-states the reference's checkMotions validates for it (every state of every edge).
-`value` is measured on device-resident inputs; `e2e` goes through the same C-ABI
-call with host buffers (H2D of the edge endpoints and D2H of the results inside the
-timed region).
+Metric: FK+collision checks/s, where the checks of a batch are the interpolated states
+the reference's checkMotions validates for it (every state of every edge).  `value` is
+measured on device-resident inputs; `e2e` goes through the same C-ABI call with host
+buffers (H2D of the edge endpoints and D2H of the results inside the timed region).
+
+The same line carries `secondary`: the other four workloads of the benchmark set, each
+with its own clock record taken during its timed region:
+  plain_fk_collision  4,096 configurations of a 7-DOF arm (59 spheres) against 32
+                      spheres + 8 boxes: one collision flag and the link poses per
+                      configuration, from one launch;
+  plan                single-problem parallel RRT-Connect on 100 seeded shelf problems:
+                      time to solution p50 / p99;
+  uneven_batch        256 heterogeneous planning problems in one persistent launch
+                      against 256 sequential single-problem solves;
+  serving             a Poisson request stream over 4 resident robots and 16 resident
+                      scenes against the per-request path.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbmp|reference]
+                  [--workload all|edges|plain|plan|batch|serve]
 
-N > 1 runs under torchrun: every rank validates its own 65,536 edges (weak scaling,
-no collective on the data path); the step time is the max over ranks.
+N > 1 runs under torchrun: every rank validates its own 65,536 edges (weak scaling, no
+collective on the data path); the step time is the max over ranks.  The secondary
+workloads run on rank 0 at N = 1 only.
 """
 from __future__ import annotations
 
@@ -42,23 +56,26 @@ WORKLOAD = "edge_validation_8dof_65536_edges"
 STEP = 0.01
 RULE = 1              # L-infinity: at most 0.01 rad per joint between consecutive states
 CPU_SAMPLE_EDGES = 1536
+PLAN_RES = 0.01
+PLAN_RANGE = 0.1
+L2_FLUSH_BYTES = 384 * 1024 * 1024   # > L2 (126 MB)
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
     ap.add_argument("--edges", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="edges", choices=["edges", "plan", "batch", "serve"],
-                    help="edges: the headline edge-validation batch; plan: single-problem RRT-Connect "
-                         "time-to-solution over seeded shelf problems")
+    ap.add_argument("--workload", default="all", choices=["all", "edges", "plain", "plan", "batch", "serve"],
+                    help="all: the headline edge line with every secondary workload; otherwise one workload's "
+                         "own line")
     ap.add_argument("--plan-seeds", type=int, default=100)
-    ap.add_argument("--lanes", default="1024,2048,4096,8192")
+    ap.add_argument("--lanes", default="1024,2048,4096")
     ap.add_argument("--rates", default="200,1000,2000", help="serve: Poisson arrival rates (req/s)")
-    ap.add_argument("--duration", type=float, default=3.0, help="serve: seconds of arrivals per rate")
+    ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
 
 
@@ -111,6 +128,7 @@ class ClockSampler:
         except Exception:
             self.proc = None
         self.t_begin = self.t_end = None
+        return self
 
     def mark_begin(self):
         self.t_begin = time.time()
@@ -207,6 +225,115 @@ def cpu_baseline(robot, env, qf, qt):
                       f"(all states, all pairs, cost mode), OpenMP, {dt:.1f} s"}
 
 
+def _pct(v, p):
+    return float(np.percentile(v, p)) if len(v) else None
+
+
+# ---------------------------------------------------------------------------------------
+# Secondary workloads (rank 0, one GPU).  Each returns a dict with its own metric, unit,
+# direction, config and clock record.
+# ---------------------------------------------------------------------------------------
+def bench_plain(args, flush, fp32_peak):
+    """Plain batched FK + collision: 4,096 configurations of a 7-DOF revolute arm (59
+    spheres, all-pairs self mask without adjacent links) against 32 obstacle spheres and
+    8 axis-aligned boxes; one collision flag plus the link poses per configuration, both
+    from one launch (gbmp_check_states_fk)."""
+    import torch
+    import oracle as O
+    from isaac_sim_ros2_humble_gb300 import _lib, api, roofline, workloads as W
+    robot, env, q = W.plain_check_workload(n=4096)
+    R, E = api.Robot(robot), api.Env(env)
+    n, L = q.shape
+    d_q = torch.from_numpy(q).cuda()
+    verdict = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    poses = torch.zeros((n, L, 16), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        api.check_states(R, E, d_q, verdict=verdict, poses=poses)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(50, args.steps)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    clk = ClockSampler(torch.cuda.current_device()).start()
+    _lib.profile_reset()
+    launches0 = _lib.launch_count()
+    torch.cuda.synchronize()
+    clk.mark_begin()
+    _lib.profile_enable(True)
+    for i in range(steps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    clk.mark_end()
+    _lib.profile_enable(False)
+    clocks = clk.stop()
+    launches = _lib.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    k_ms, k_launches = _lib.profile_read(_lib.PROF_CHECK_STATES)
+    k_ms_per = k_ms / max(k_launches, 1)
+    _lib.work_counting(True)
+    step()
+    torch.cuda.synchronize()
+    exec_flops, exec_states = _lib.work_read()
+    _lib.work_counting(False)
+    flops_state = roofline.flops_per_state(robot, env, R.P)
+    # end to end: configurations from pinned host memory, flags and poses back
+    h_q = torch.from_numpy(q).pin_memory()
+    h_v = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h_p = torch.empty((n, L, 16), dtype=torch.float32).pin_memory()
+    e2e_ms = []
+    for i in range(3 + steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d_q.copy_(h_q, non_blocking=True)
+        step()
+        h_v.copy_(verdict, non_blocking=True)
+        h_p.copy_(poses, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= 3:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    ms = float(np.median(step_ms))
+    out = {"metric": "FK+collision checks/s", "value": n / (ms / 1e3), "unit": "configs/s",
+           "higher_is_better": True, "ms_per_step": ms, "steps": steps,
+           "config": {"workload": "plain_fk_collision_7dof_4096", "configs": n, "dof": robot.dim, "links": L,
+                      "robot_spheres": robot.num_spheres, "self_pairs": R.P,
+                      "obstacles": {"spheres": env.counts[0], "boxes": env.counts[1]},
+                      "outputs": "collision flag + 4x4 link poses per configuration, one launch",
+                      "colliding": int(verdict.sum().item()), "l2_flush": "384 MB buffer written between steps"},
+           "e2e": {"value": n / (float(np.median(e2e_ms)) / 1e3), "unit": "configs/s",
+                   "h2d_bytes_per_step": int(n * L * 4), "d2h_bytes_per_step": int(n + n * L * 64),
+                   "ms_per_step": float(np.median(e2e_ms))},
+           "roofline": {"bound": "fp32", "kernel": "k_check_states", "unit": "TFLOP/s", "peak": fp32_peak,
+                        "achieved": exec_flops / (k_ms_per / 1e3) / 1e12 if k_ms_per > 0 else None,
+                        "achieved_is": "flops executed by k_check_states (counted in-kernel in an untimed step) / "
+                                       "its device time",
+                        "effective": n * flops_state / (k_ms_per / 1e3) / 1e12 if k_ms_per > 0 else None,
+                        "effective_is": "reference-equivalent work (all pairs of every configuration) / its device "
+                                        "time",
+                        "flops_per_config": flops_state, "executed_flops_per_launch": exec_flops,
+                        "kernel_ms": k_ms_per, "hbm_bytes_algorithmic": int(n * (L * 4 + L * 64 + 1))},
+           "gpu_launches": int(launches), "clocks": clocks}
+    rf = out["roofline"]
+    rf["frac"] = rf["achieved"] / fp32_peak if rf["achieved"] and fp32_peak else None
+    rf["effective_frac"] = rf["effective"] / fp32_peak if rf["effective"] and fp32_peak else None
+    if not args.no_cpu_baseline:
+        m = O.OracleModel(robot, env)
+        m.check_states(q[:64])
+        t0 = time.perf_counter()
+        m.check_states(q)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "configs/s", "cores": O.num_threads(), "kind": "port",
+                               "sample": f"all {n} configurations, reference algorithm (FK, every pair, cost mode), "
+                                         f"OpenMP, {dt * 1e3:.1f} ms"}
+    return out
+
+
 def gpu_problem_set(n_seeds, R, robot, api, W, torch):
     """Seeded shelf problems with collision-free start/goal whose direct edge collides,
     selected with the GPU checker (product path)."""
@@ -235,32 +362,27 @@ def gpu_problem_set(n_seeds, R, robot, api, W, torch):
     return envs, problems
 
 
-PLAN_RES = 0.01
-PLAN_RANGE = 0.1
-
-
-def run_plan(args):
+def bench_plan(args, flush):
     """Single-problem parallel RRT-Connect: time to first solution over seeded shelf
     problems (7-DOF arm, 5 slabs + 40 boxes), for several lane counts."""
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return 0
     import torch
     import oracle as O
     from isaac_sim_ros2_humble_gb300 import api, workloads as W
-    torch.cuda.set_device(0)
     robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
     R = api.Robot(robot)
     envs, problems = gpu_problem_set(args.plan_seeds, R, robot, api, W, torch)
     planner = api.Planner(R, max_nodes=1_000_000, path_cap=65536)
     lanes_list = [int(x) for x in args.lanes.split(",")]
     per_lanes = {}
+    clk = ClockSampler(torch.cuda.current_device()).start()
+    clk.mark_begin()
     for lanes in lanes_list:
-        for seed, sc, start, goal in problems[: max(args.warmup, 1)]:
+        for seed, sc, start, goal in problems[: max(args.warmup, 3)]:
             planner.solve(envs[sc][1], start, goal, lanes=lanes, range_=PLAN_RANGE, resolution=PLAN_RES, rule=RULE,
                           seed=seed)
         ms, costs, ok, kms = [], [], 0, []
         for seed, sc, start, goal in problems:
+            flush.fill_(float(seed))
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             res, path = planner.solve(envs[sc][1], start, goal, lanes=lanes, range_=PLAN_RANGE, resolution=PLAN_RES,
@@ -270,19 +392,22 @@ def run_plan(args):
             if res["solved"]:
                 ok += 1
                 costs.append(res["cost"])
-        per_lanes[lanes] = {"p50_ms": float(np.percentile(ms, 50)), "p95_ms": float(np.percentile(ms, 95)),
-                            "p99_ms": float(np.percentile(ms, 99)), "mean_ms": float(np.mean(ms)),
-                            "kernel_p50_ms": float(np.percentile(kms, 50)), "success": ok / len(problems),
-                            "path_length_mean": float(np.mean(costs)) if costs else None,
-                            "path_length_p50": float(np.percentile(costs, 50)) if costs else None}
+        per_lanes[str(lanes)] = {"p50_ms": _pct(ms, 50), "p95_ms": _pct(ms, 95), "p99_ms": _pct(ms, 99),
+                                 "mean_ms": float(np.mean(ms)), "kernel_p50_ms": _pct(kms, 50),
+                                 "success": ok / len(problems),
+                                 "path_length_mean": float(np.mean(costs)) if costs else None,
+                                 "path_length_p50": _pct(costs, 50)}
+    clk.mark_end()
+    clocks = clk.stop()
     best = min(per_lanes, key=lambda k: per_lanes[k]["p50_ms"])
-    line = {"metric": "plan p50 latency", "value": per_lanes[best]["p50_ms"], "unit": "ms",
-            "n_gpus": 1, "steps": len(problems), "warmup": args.warmup, "ms_per_step": per_lanes[best]["mean_ms"],
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded shelf scenes)",
-            "config": {"workload": f"rrtc_shelf_7dof_{len(problems)}_seeds", "best_lanes": best,
-                       "range": PLAN_RANGE, "resolution": PLAN_RES, "step_rule": "linf", "max_nodes": 1_000_000,
-                       "per_lanes": per_lanes}}
+    out = {"metric": "plan time to solution p50", "value": per_lanes[best]["p50_ms"], "unit": "ms",
+           "higher_is_better": False, "p99_ms": per_lanes[best]["p99_ms"], "steps": len(problems),
+           "config": {"workload": f"rrtc_shelf_7dof_{len(problems)}_seeds", "best_lanes": int(best),
+                      "range": PLAN_RANGE, "resolution": PLAN_RES, "step_rule": "linf", "max_nodes": 1_000_000,
+                      "timing": "host wall time of each gbmp_rrtc_solve call (reset, launch, path read back); "
+                                "L2 flushed before each solve",
+                      "per_lanes": per_lanes},
+           "clocks": clocks}
     if not args.no_cpu_baseline:
         k = min(10, len(problems))
         t_cpu, c_cpu, s_cpu = [], [], 0
@@ -295,24 +420,19 @@ def run_plan(args):
             s_cpu += r_["solved"]
             if r_["solved"]:
                 c_cpu.append(r_["cost"])
-        line["cpu_baseline"] = {"value": float(np.percentile(t_cpu, 50)), "unit": "ms", "cores": 1, "kind": "port",
-                                "sample": f"first {k} problems, sequential RRT-Connect with the same primitives "
-                                          f"(oracle), success {s_cpu}/{k}, path length mean "
-                                          f"{float(np.mean(c_cpu)) if c_cpu else None}"}
-    print(json.dumps(line), flush=True)
-    return 0
+        out["cpu_baseline"] = {"value": _pct(t_cpu, 50), "unit": "ms", "cores": 1, "kind": "port",
+                               "sample": f"first {k} problems, sequential RRT-Connect with the same primitives "
+                                         f"(oracle), success {s_cpu}/{k}, path length mean "
+                                         f"{float(np.mean(c_cpu)) if c_cpu else None}"}
+    return out
 
 
-def run_batch(args):
+def bench_batch(args, flush):
     """Uneven batch: 256 heterogeneous planning problems (DOF 6-9, 30-120 spheres,
     10-500 obstacles) in one persistent, graph-captured launch with autotuned lanes per
     problem, against 256 sequential plain single-problem solves on the same GPU."""
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return 0
     import torch
     from isaac_sim_ros2_humble_gb300 import api, workloads as W
-    torch.cuda.set_device(0)
     n = 256
 
     def feasible(robot, env):
@@ -343,7 +463,7 @@ def run_batch(args):
         problems.append((R, E, s0, g0, 1000 + i))
     kw = dict(range_=PLAN_RANGE, resolution=PLAN_RES, rule=RULE, time_limit_s=10.0)
     bp = api.BatchPlanner(max_problems=n, max_nodes=32768, max_links=16, path_cap=4096)
-    # autotune lanes per problem on the batch itself (replays of the captured graph)
+    # lanes per problem chosen on the batch itself (replays of the captured graph)
     tune = {}
     for lpp in (4, 8, 16, 32):
         bp.solve(problems, lanes_per_problem=lpp, use_graph=True, **kw)
@@ -351,60 +471,65 @@ def run_batch(args):
         out = bp.solve(problems, lanes_per_problem=lpp, use_graph=True, **kw)
         tune[lpp] = ((time.perf_counter() - t0) * 1e3, sum(r["solved"] for r, _ in out))
     best = min(tune, key=lambda k: tune[k][0])
+    steps = max(3, min(args.steps, 5))
+    clk = ClockSampler(torch.cuda.current_device()).start()
     times, solved = [], []
-    for rep in range(max(args.warmup, 1) + args.steps):
+    for rep in range(max(args.warmup, 1) + steps):
+        flush.fill_(float(rep))
+        torch.cuda.synchronize()
+        if rep == max(args.warmup, 1):
+            clk.mark_begin()
         t0 = time.perf_counter()
         out = bp.solve(problems, lanes_per_problem=best, use_graph=True, **kw)
-        if rep >= args.warmup:
+        if rep >= max(args.warmup, 1):
             times.append((time.perf_counter() - t0) * 1e3)
             solved.append(sum(r["solved"] for r, _ in out))
+    clk.mark_end()
+    clocks = clk.stop()
     batch_ms = float(np.median(times))
     # plain path: sequential single-problem solves
     plain = {}
+    clk2 = ClockSampler(torch.cuda.current_device()).start()
+    clk2.mark_begin()
     for lanes in (1024, 64):
         planners = {}
-        t_plain, s_plain = [], 0
-        for rep in range(2):
-            s_plain = 0
-            t0 = time.perf_counter()
-            for (R, E, s0, g0, seed) in problems:
-                pl = planners.get(id(R))
-                if pl is None:
-                    pl = planners[id(R)] = api.Planner(R, max_nodes=32768, path_cap=4096)
-                r, p = pl.solve(E, s0, g0, lanes=lanes, seed=seed, **kw)
-                s_plain += r["solved"]
-            t_plain.append((time.perf_counter() - t0) * 1e3)
-        plain[lanes] = (min(t_plain), s_plain)
+        s_plain = 0
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for (R, E, s0, g0, seed) in problems:
+            pl = planners.get(id(R))
+            if pl is None:
+                pl = planners[id(R)] = api.Planner(R, max_nodes=32768, path_cap=4096)
+            r, p = pl.solve(E, s0, g0, lanes=lanes, seed=seed, **kw)
+            s_plain += r["solved"]
+        plain[lanes] = ((time.perf_counter() - t0) * 1e3, s_plain)
         del planners
+    clk2.mark_end()
+    clocks_plain = clk2.stop()
     plain_best = min(plain, key=lambda k: plain[k][0])
     plain_ms = plain[plain_best][0]
-    line = {"metric": "uneven-batch planning throughput", "value": n / (batch_ms / 1e3), "unit": "problems/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded robots and scenes)",
+    return {"metric": "uneven-batch planning throughput", "value": n / (batch_ms / 1e3), "unit": "problems/s",
+            "higher_is_better": True, "ms_per_step": batch_ms, "steps": steps,
+            "speedup_vs_plain": plain_ms / batch_ms,
             "config": {"workload": "uneven_batch_256_rrtc", "problems": n, "lanes_per_problem": best,
                        "autotune_ms": {str(k): v[0] for k, v in tune.items()},
                        "solved_batched": int(np.median(solved)), "graph": True,
                        "plain_sequential_ms": plain_ms, "plain_lanes": plain_best,
                        "plain_solved": plain[plain_best][1],
-                       "plain_all": {str(k): v for k, v in plain.items()},
-                       "speedup_vs_plain": plain_ms / batch_ms}}
-    print(json.dumps(line), flush=True)
-    return 0
+                       "plain_all": {str(k): list(v) for k, v in plain.items()},
+                       "plain_clocks": clocks_plain,
+                       "timing": "host wall time of each batched call; plain = the 256 single solves back to back"},
+            "clocks": clocks}
 
 
-def run_serve(args):
+def bench_serve(args):
     """Serving: Poisson request stream over 4 resident robots (6-9 DOF) and 16 resident
     scenes (50-500 obstacles); 70 % FK+collision requests of log-uniform 1-65,536 states,
     30 % RRT-Connect plan requests.  The continuous-batching server against the plain
     per-request path (one request at a time, in arrival order)."""
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return 0
-    import threading
     import torch
-    from isaac_sim_ros2_humble_gb300 import _lib, api, workloads as W
-    torch.cuda.set_device(0)
+    from isaac_sim_ros2_humble_gb300 import api, workloads as W
     robots = [W.serial_arm(80 + i, dof=6 + i, n_spheres=40 + 25 * i, prismatic_torso=i >= 2, resolution=0.01)
               for i in range(4)]
     envs = [W.random_env(90 + k, *(lambda O: (O - round(O * 80 / 336), round(O * 64 / 336), round(O * 16 / 336)))
@@ -488,11 +613,12 @@ def run_serve(args):
             lat[kind].append((time.perf_counter() - t0 - ta) * 1e3)
         return lat, time.perf_counter() - t0
 
-    pct = lambda v, p: float(np.percentile(v, p)) if len(v) else None
     per_rate = {}
+    clk = ClockSampler(torch.cuda.current_device()).start()
+    run_served(make_stream(200.0, 1)[: 50])          # warm-up
+    clk.mark_begin()
     for rate in [float(x) for x in args.rates.split(",")]:
         stream = make_stream(rate, int(rate))
-        run_served(make_stream(rate, 1)[: 50])          # warm-up
         lat_s, el_s, st = run_served(stream)
         lat_p, el_p = run_plain(stream)
         all_s = lat_s["check"] + lat_s["plan"]
@@ -500,30 +626,39 @@ def run_serve(args):
         per_rate[str(int(rate))] = {
             "requests": len(stream), "served_throughput_rps": len(stream) / el_s,
             "plain_throughput_rps": len(stream) / el_p,
-            "served": {"p50_ms": pct(all_s, 50), "p95_ms": pct(all_s, 95), "p99_ms": pct(all_s, 99),
-                       "check_p99_ms": pct(lat_s["check"], 99), "plan_p99_ms": pct(lat_s["plan"], 99)},
-            "plain": {"p50_ms": pct(all_p, 50), "p95_ms": pct(all_p, 95), "p99_ms": pct(all_p, 99),
-                      "check_p99_ms": pct(lat_p["check"], 99), "plan_p99_ms": pct(lat_p["plan"], 99)},
+            "served": {"p50_ms": _pct(all_s, 50), "p95_ms": _pct(all_s, 95), "p99_ms": _pct(all_s, 99),
+                       "check_p99_ms": _pct(lat_s["check"], 99), "plan_p99_ms": _pct(lat_s["plan"], 99)},
+            "plain": {"p50_ms": _pct(all_p, 50), "p95_ms": _pct(all_p, 95), "p99_ms": _pct(all_p, 99),
+                      "check_p99_ms": _pct(lat_p["check"], 99), "plan_p99_ms": _pct(lat_p["plan"], 99)},
             "check_batches": st["batches"], "plan_batches": st["plan_batches"]}
+    clk.mark_end()
+    clocks = clk.stop()
     top = per_rate[max(per_rate, key=lambda k: float(k))]
-    line = {"metric": "served p99 latency", "value": top["served"]["p99_ms"], "unit": "ms", "n_gpus": 1,
-            "steps": sum(v["requests"] for v in per_rate.values()), "warmup": 50,
-            "ms_per_step": top["served"]["p50_ms"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded Poisson stream)",
+    return {"metric": "served p99 latency at the highest rate", "value": top["served"]["p99_ms"], "unit": "ms",
+            "higher_is_better": False, "p50_ms": top["served"]["p50_ms"], "p95_ms": top["served"]["p95_ms"],
+            "served_throughput_rps": top["served_throughput_rps"],
+            "plain_throughput_rps": top["plain_throughput_rps"],
+            "throughput_vs_plain": top["served_throughput_rps"] / top["plain_throughput_rps"],
+            "steps": sum(v["requests"] for v in per_rate.values()),
             "config": {"workload": "serving_4robots_16scenes_70check_30plan", "duration_s": args.duration,
-                       "per_rate": per_rate}}
-    print(json.dumps(line), flush=True)
-    return 0
+                       "rates": args.rates, "per_rate": per_rate,
+                       "timing": "host wall time from a request's scheduled arrival to its completion; the "
+                                 "served and plain paths replay the same stream"},
+            "clocks": clocks}
+
+
+def _standalone_line(d, args):
+    """A secondary workload as a line of its own (--workload plain|plan|batch|serve)."""
+    line = {"metric": d["metric"], "value": d["value"], "unit": d["unit"], "n_gpus": 1,
+            "steps": d.get("steps", args.steps), "warmup": args.warmup, "ms_per_step": d.get("ms_per_step"),
+            "higher_is_better": d["higher_is_better"], "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)"}
+    line.update({k: v for k, v in d.items() if k not in line})
+    return line
 
 
 def main():
     args = parse()
-    if args.workload == "serve":
-        return run_serve(args)
-    if args.workload == "plan":
-        return run_plan(args)
-    if args.workload == "batch":
-        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     import torch
@@ -538,6 +673,16 @@ def main():
     else:
         torch.cuda.set_device(0)
     dev = torch.device("cuda", torch.cuda.current_device())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    if args.workload in ("plain", "plan", "batch", "serve"):
+        if rank != 0:
+            return 0
+        fn = {"plain": lambda: bench_plain(args, flush, _lib.measure_fp32_peak(1.0)),
+              "plan": lambda: bench_plan(args, flush), "batch": lambda: bench_batch(args, flush),
+              "serve": lambda: bench_serve(args)}[args.workload]
+        print(json.dumps(_standalone_line(fn(), args)), flush=True)
+        return 0
 
     robot, env, qf, qt = W.edge_workload(n_edges=args.edges, shard=rank)
     R, E = api.Robot(robot), api.Env(env)
@@ -549,14 +694,13 @@ def main():
     fh = torch.zeros(n, dtype=torch.int32, device=dev)
     ln = torch.zeros(n, device=dev)
     ns = torch.zeros(n, dtype=torch.int32, device=dev)
-    flush = torch.empty(384 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (126 MB)
     stream = torch.cuda.current_stream()
 
     def step():
         api.check_edges(R, E, d_from, d_to, STEP, RULE, ok, fh, ln, ns)
 
     fp32_peak = _lib.measure_fp32_peak(1.0)
-    for _ in range(args.warmup):
+    for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
     checks = int(ns.sum().item())
@@ -601,7 +745,7 @@ def main():
     h_fh = torch.empty(n, dtype=torch.int32).pin_memory()
     h_ln = torch.empty(n, dtype=torch.float32).pin_memory()
     e2e_ms = []
-    for i in range(args.warmup + args.steps):
+    for i in range(max(args.warmup, 3) + args.steps):
         flush.fill_(float(i))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -612,7 +756,7 @@ def main():
         h_fh.copy_(fh, non_blocking=True)
         h_ln.copy_(ln, non_blocking=True)
         torch.cuda.synchronize()
-        if i >= args.warmup:
+        if i >= max(args.warmup, 3):
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = sum(e2e_ms) / 1e3
     total_s, all_checks, e2e_s = reduce_over_ranks(dist, ws, dev, total_s, checks, e2e_s)
@@ -625,7 +769,7 @@ def main():
         achieved = exec_flops / wave_s_per_step / 1e12 if wave_s_per_step > 0 else None
         effective = units * flops_state / wave_s_per_step / 1e12 if wave_s_per_step > 0 else None
         traffic = None
-        kernel = "k_edge_wave" if os.environ.get("GBMP_EDGE_CHUNK", "") == "1" else "k_edge_chunk"
+        kernel = "k_edge_chunk"
         tp = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
         if os.path.exists(tp):
             try:
@@ -667,6 +811,19 @@ def main():
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(robot, env, qf, qt)
+        if args.workload == "all" and ws == 1:
+            sec = {}
+            for name, fn in (("plain_fk_collision", lambda: bench_plain(args, flush, fp32_peak)),
+                             ("plan", lambda: bench_plan(args, flush)),
+                             ("uneven_batch", lambda: bench_batch(args, flush)),
+                             ("serving", lambda: bench_serve(args))):
+                t0 = time.perf_counter()
+                try:
+                    sec[name] = fn()
+                except Exception as e:   # a failed secondary workload is reported, not hidden
+                    sec[name] = {"error": f"{type(e).__name__}: {e}"}
+                sec[name]["wall_s"] = time.perf_counter() - t0
+            line["secondary"] = sec
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

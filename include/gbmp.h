@@ -153,6 +153,14 @@ GBMP_API gbmp_status gbmp_fk(gbmp_robot robot, const float *d_q, int64_t n, floa
 GBMP_API gbmp_status gbmp_check_states(gbmp_robot robot, gbmp_env env, const float *d_q, int64_t n,
                               int32_t mode, uint8_t *d_verdict, float *d_costs, float *d_total,
                               void *stream);
+/* gbmp_check_states that also writes the FK it computed, replacing the pair
+ * SingleArmStates::update (SingleArmStates.cu:696-723) + SingleArmSpace::checkStates
+ * (SingleArmSpace.cu:1572-1602) with one FK per state: d_poses [n*L*16] row-major 4x4
+ * link poses and d_centers [n*S*3] sphere centres, each NULL allowed, exactly as gbmp_fk
+ * writes them.  Verdicts and costs are those of gbmp_check_states. */
+GBMP_API gbmp_status gbmp_check_states_fk(gbmp_robot robot, gbmp_env env, const float *d_q, int64_t n,
+                                          int32_t mode, uint8_t *d_verdict, float *d_costs, float *d_total,
+                                          float *d_poses, float *d_centers, void *stream);
 
 /* Edge validation, replacing SingleArmSpace::checkMotions / checkUnconstrainedMotions
  * (SingleArmSpace.cu:628-848; step rule KernelGenerator.h:408-465, interpolation
@@ -164,24 +172,30 @@ GBMP_API gbmp_status gbmp_check_states(gbmp_robot robot, gbmp_env env, const flo
  * rule; GBMP_STEP_LINF bounds the per-joint step by `resolution` instead.
  * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read).
  * Robots of up to 32 sphere-carrying links are validated by chunks of 8 consecutive
- * states a warp, others state by state; the environment variable GBMP_EDGE_CHUNK
- * overrides the form for tuning and tests (0 or 1: state by state, 4 or 8: chunks). */
+ * states a warp (4 for robots of more than 16 links), others state by state;
+ * gbmp_robot_set_edge_form overrides the form for one robot handle. */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
 /* pRRTC's `granularity` (pRRTC/src/planning/pRRTC.cu:430-440): every edge is checked at
  * a fixed count of equal steps, `resolution` rounded down to an integer G in [1, 1e6]:
  * the states at k / G of the edge (k = 0..G in gbmp_check_edges, k = 1..G in the
- * planners, whose edge start is already a tree node).  Not accepted by
- * gbmp_check_edges_noalloc. */
+ * planners, whose edge start is already a tree node). */
 #define GBMP_STEP_COUNT 2
 GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const float *d_from, const float *d_to,
                              int64_t n_edges, float resolution, int32_t step_rule, uint8_t *d_ok,
                              int32_t *d_first_hit, float *d_length, int32_t *d_num_steps, void *stream);
 
-/* gbmp_check_edges without any allocation: same arguments, kernels and results, but its
- * working memory is a fixed 5 MiB device array inside the library (one per device)
- * instead of a buffer grown with cudaMalloc.  No counterpart in the reference, whose
- * checkMotions allocates and frees its state buffers on every call.
+/* Tuning and test control of the edge-validation form of one robot handle: 0 automatic
+ * (the default), 1 state by state, 4 or 8 consecutive states per chunk (chunks need a
+ * robot of at most 32 sphere-carrying links; others stay state by state).  Results do
+ * not depend on the form.  No counterpart in the reference. */
+GBMP_API gbmp_status gbmp_robot_set_edge_form(gbmp_robot robot, int32_t form);
+
+/* gbmp_check_edges without any allocation: same arguments, kernels and results (both
+ * entry points run one implementation), but its working memory is a fixed 5 MiB device
+ * array inside the library (one per device) instead of a buffer grown with cudaMalloc.
+ * No counterpart in the reference, whose checkMotions allocates and frees its state
+ * buffers on every call.
  * For callers that must not allocate device memory: a control loop with a latency bound
  * (cudaMalloc / cudaFree can block and cudaFree synchronises the device), a process whose
  * device memory is fully reserved up front, or code that runs while memory is exhausted.
@@ -194,7 +208,9 @@ GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const floa
  * synchronise between them.  Different devices do not share it.
  * The first call on each device (n_edges = 0 is enough) looks up the scratch's device
  * address with that device current; a caller that captures streams makes that first
- * call before it begins a capture.  Stream-synchronising like gbmp_check_edges. */
+ * call before it begins a capture.  The address belongs to the device's context and is
+ * kept for the life of the process: do not call this entry point on a device after
+ * cudaDeviceReset of that device.  Stream-synchronising like gbmp_check_edges. */
 GBMP_API gbmp_status gbmp_check_edges_noalloc(gbmp_robot robot, gbmp_env env, const float *d_from,
                                      const float *d_to, int64_t n_edges, float resolution,
                                      int32_t step_rule, uint8_t *d_ok, int32_t *d_first_hit,

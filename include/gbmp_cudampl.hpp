@@ -369,6 +369,8 @@ class SingleArmSpace {
         const int n = states1->getNumOfStates();
         if (n != states2->getNumOfStates()) throw std::runtime_error("Number of states in states1 and states2 are not equal");
         if (n == 0) throw std::runtime_error("No states to check");
+        // the reference switches to checkConstrainedMotions here (SingleArmSpace.cu:636-639)
+        if (projectable_) throw std::runtime_error("checkMotions with a projectable constraint is not supported");
         detail::DevArray ok((size_t)n), len(sizeof(float) * n);
         if (!ok.ok() || !len.ok()) {
             motion_feasibility.assign(n, false);
@@ -428,6 +430,9 @@ class SingleArmSpace {
     // Waypoints to a dense path at the space resolution (SingleArmSpace.cu:1411-1464,
     // interpolateVectors in util.cpp:205-248).
     BaseStatesPtr getPathFromWaypoints(const BaseStatesPtr &waypoints) {
+        // the reference switches to getConstrainedPathFromWaypoints here (SingleArmSpace.cu:1416-1419)
+        if (projectable_)
+            throw std::runtime_error("getPathFromWaypoints with a projectable constraint is not supported");
         auto w = waypoints->getJointStatesFullHost();
         std::vector<std::vector<float>> out;
         for (size_t i = 0; i + 1 < w.size(); ++i) {

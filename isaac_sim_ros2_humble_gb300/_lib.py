@@ -105,6 +105,8 @@ SIGNATURES = {
     "gbmp_env_counts": [_vp, _i32p, _i32p, _i32p],
     "gbmp_fk": [_vp, _vp, _i64, _vp, _vp, _vp],
     "gbmp_check_states": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp],
+    "gbmp_check_states_fk": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gbmp_robot_set_edge_form": [_vp, _i32],
     "gbmp_check_edges": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
     "gbmp_check_edges_noalloc": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
     "gbmp_nearest": [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp],

@@ -58,6 +58,11 @@ class Robot:
         check(_lib.load().gbmp_robot_self_pairs(self.handle, pairs.ctypes.data, thr.ctypes.data, max(self.P, 1)))
         return pairs[: 2 * self.P].reshape(-1, 2), thr[: self.P]
 
+    def set_edge_form(self, form: int):
+        """Edge-validation form of this handle: 0 automatic, 1 state by state, 4 or 8
+        states per chunk (tuning and tests; results do not depend on it)."""
+        check(_lib.load().gbmp_robot_set_edge_form(self.handle, int(form)))
+
     def use_codegen(self, enable: bool):
         check(_lib.load().gbmp_robot_use_codegen(self.handle, int(enable)))
 
@@ -115,10 +120,16 @@ def fk(robot: Robot, q, poses=None, centers=None, stream=None):
 
 
 def check_states(robot: Robot, env: Env, q, verdict=None, costs=None, total=None, mode=_lib.CHECK_VERDICT,
-                 stream=None):
+                 stream=None, poses=None, centers=None):
+    """Collision check of the states q [n, L]; with poses [n, L, 4, 4] and / or
+    centers [n, S, 3] the same FK is written out too (one launch)."""
     n = _n(q, robot.L)
-    check(_lib.load().gbmp_check_states(robot.handle, env.handle, ptr(q), n, mode, ptr(verdict), ptr(costs),
-                                        ptr(total), stream_handle(stream)))
+    if poses is None and centers is None:
+        check(_lib.load().gbmp_check_states(robot.handle, env.handle, ptr(q), n, mode, ptr(verdict), ptr(costs),
+                                            ptr(total), stream_handle(stream)))
+    else:
+        check(_lib.load().gbmp_check_states_fk(robot.handle, env.handle, ptr(q), n, mode, ptr(verdict), ptr(costs),
+                                               ptr(total), ptr(poses), ptr(centers), stream_handle(stream)))
 
 
 def check_edges(robot: Robot, env: Env, q_from, q_to, resolution: float = 0.0, rule: int = _lib.STEP_L2,

@@ -55,13 +55,17 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
     procs, objs = [], []
+    headers = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh"))
+               + glob.glob(os.path.join(INCLUDE, "*.h")) + [os.path.abspath(__file__)])
     for src in sources():
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+        objs.append(obj)
+        if not force and not extra_flags and not _stale(obj, [src] + headers):
+            continue   # object newer than its source and every header
         cmd = [nvcc()] + NVCC_FLAGS + list(extra_flags) + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
-        objs.append(obj)
     failed = []
     for src, p in procs:
         out, _ = p.communicate()

@@ -597,14 +597,9 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
         }                                                                                    \
     } while (0)
 
-int edge_chunk_states(const DevRobot &R) {
-    if (!R.cull) return 0;
-    const char *env = getenv("GBMP_EDGE_CHUNK");
-    if (env && *env) {
-        const int k = atoi(env);
-        if (k <= 1) return 0;
-        return k >= 8 ? 8 : 4;
-    }
+int edge_chunk_states(const DevRobot &R, int form) {
+    if (!R.cull || form == 1) return 0;
+    if (form == 4 || form == 8) return form;
     return R.L <= 16 ? 8 : 4;
 }
 
@@ -613,13 +608,8 @@ gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, 
     gbmp_status st = GBMP_OK;
     GBMP_CHUNK_SWITCH(R.spl, K, {
         const void *fn = R.work ? (const void *)k_edge_chunk<SPL, KK, true> : (const void *)k_edge_chunk<SPL, KK, false>;
-        static thread_local bool configured[2] = {false, false};
-        if (!configured[R.work != nullptr]) {
-            GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-            GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                           cudaSharedmemCarveoutMaxShared));
-            configured[R.work != nullptr] = true;
-        }
+        st = ensure_smem_optin(fn);
+        if (st) return st;
         int per_sm = 0;
         GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kChunkWarps * kWarp, *smem));
         if (per_sm < 1) {

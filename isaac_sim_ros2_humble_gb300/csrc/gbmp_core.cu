@@ -27,18 +27,22 @@ static size_t block_smem(const DevRobot &R, int nwords) {
     return smem_tables_bytes(R, nwords) + smem_warp_bytes(R) * kWarpsPerBlock;
 }
 
+static DeviceKernelSet g_smem_optin;
+
+gbmp_status ensure_smem_optin(const void *fn) {
+    int dev = 0;
+    GBMP_CUDA(cudaGetDevice(&dev));
+    if (g_smem_optin.contains(dev, fn)) return GBMP_OK;
+    GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+    g_smem_optin.insert(dev, fn);
+    return GBMP_OK;
+}
+
 template <typename K>
 static gbmp_status persistent_grid(K kernel, size_t smem, int num_sms, int *grid) {
-    static thread_local const void *configured[64];
-    static thread_local int n_configured = 0;
-    bool seen = false;
-    for (int i = 0; i < n_configured; ++i) seen |= configured[i] == (const void *)kernel;
-    if (!seen) {
-        GBMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-        GBMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                       cudaSharedmemCarveoutMaxShared));
-        if (n_configured < 64) configured[n_configured++] = (const void *)kernel;
-    }
+    gbmp_status st = ensure_smem_optin((const void *)kernel);
+    if (st) return st;
     int per_sm = 0;
     GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerBlock * kWarp, smem));
     if (per_sm < 1) {
@@ -52,6 +56,27 @@ static gbmp_status persistent_grid(K kernel, size_t smem, int num_sms, int *grid
 // ---------------------------------------------------------------------------------
 // Kernels.
 // ---------------------------------------------------------------------------------
+
+// Link poses [L*16] (row-major 4x4, last row 0 0 0 1) and sphere centres [S*3] of the
+// state whose FK is in w.lp, written to HBM by the warp.
+__device__ inline void store_fk(const SmemTables &t, const DevRobot &R, const WarpScratch &w, long long s,
+                                float *__restrict__ poses, float *__restrict__ centers, int lane) {
+    if (poses) {
+        float *P = poses + s * R.L * 16;
+        for (int e = lane; e < R.L * 16; e += kWarp) {
+            const int li = e >> 4, k = e & 15;
+            P[e] = k < 12 ? w.lp[12 * li + k] : (k == 15 ? 1.f : 0.f);
+        }
+    }
+    if (centers) {
+        float *C = centers + s * R.S * 3;
+        for (int k = lane; k < R.S; k += kWarp) {
+            const float4 sp = t.sph[k];
+            const float3 p = xform_point(w.lp + 12 * t.slink[k], sp.x, sp.y, sp.z);
+            C[3 * k] = p.x; C[3 * k + 1] = p.y; C[3 * k + 2] = p.z;
+        }
+    }
+}
 
 // FK (+ sphere centres) of n states; one warp per state.
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
@@ -69,30 +94,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
         for (int j = lane; j < R.L; j += kWarp) w.q[j] = q[s * R.L + j];
         __syncwarp();
         warp_fk(t, R.L, w, lane);
-        if (poses) {
-            float *P = poses + s * R.L * 16;
-            for (int e = lane; e < R.L * 16; e += kWarp) {
-                const int li = e >> 4, k = e & 15;
-                P[e] = k < 12 ? w.lp[12 * li + k] : (k == 15 ? 1.f : 0.f);
-            }
-        }
-        if (centers) {
-            float *C = centers + s * R.S * 3;
-            for (int k = lane; k < R.S; k += kWarp) {
-                const float4 sp = t.sph[k];
-                const float3 p = xform_point(w.lp + 12 * t.slink[k], sp.x, sp.y, sp.z);
-                C[3 * k] = p.x; C[3 * k + 1] = p.y; C[3 * k + 2] = p.z;
-            }
-        }
+        store_fk(t, R, w, s, poses, centers, lane);
         __syncwarp();
     }
 }
 
-// Collision check of n states; one warp per state.
+// Collision check of n states; one warp per state.  With poses / centers non-null the
+// FK of each state is also written out (the reference's update() and checkStates() from
+// one FK).
 template <bool COST, int SPL>
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     k_check_states(DevRobot R, DevEnv E, const float *__restrict__ q, long long n,
-                   unsigned char *__restrict__ verdict, float *__restrict__ costs, float *__restrict__ total) {
+                   unsigned char *__restrict__ verdict, float *__restrict__ costs, float *__restrict__ total,
+                   float *__restrict__ poses, float *__restrict__ centers) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
@@ -105,6 +119,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
         for (int j = lane; j < R.L; j += kWarp) w.q[j] = q[s * R.L + j];
         __syncwarp();
         warp_fk(t, R.L, w, lane);
+        if (poses || centers) store_fk(t, R, w, s, poses, centers, lane);
         float c[4] = {0.f, 0.f, 0.f, 0.f};
         const bool hit = (!COST && R.cull) ? warp_collide_culled<SPL>(t, R, E, w, lane)
                                            : warp_collide<SPL, COST>(t, R, E, w, lane, c);
@@ -745,8 +760,9 @@ gbmp_status gbmp_fk(gbmp_robot r, const float *d_q, int64_t n, float *d_poses, f
     return GBMP_OK;
 }
 
-gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int64_t n, int32_t mode,
-                              uint8_t *d_verdict, float *d_costs, float *d_total, void *stream) {
+gbmp_status gbmp_check_states_fk(gbmp_robot r, gbmp_env env, const float *d_q, int64_t n, int32_t mode,
+                                 uint8_t *d_verdict, float *d_costs, float *d_total, float *d_poses,
+                                 float *d_centers, void *stream) {
     GBMP_CHECK_ARG(r && env, "robot/env is NULL");
     GBMP_CHECK_ARG(n >= 0, "n < 0");
     GBMP_CHECK_ARG(mode == GBMP_CHECK_VERDICT || mode == GBMP_CHECK_COST, "unknown mode %d", mode);
@@ -766,51 +782,79 @@ gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int6
             if (st) return st;
             if (need < grid) grid = (int)need;
             ProfScope ps(GBMP_PROF_CHECK_STATES, s);
-            k_check_states<true, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(D, E, d_q, n, d_verdict,
-                                                                                 d_costs, d_total);
+            k_check_states<true, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(D, E, d_q, n, d_verdict, d_costs,
+                                                                                 d_total, d_poses, d_centers);
         } else {
             st = persistent_grid(k_check_states<false, SPL>, smem, r->num_sms, &grid);
             if (st) return st;
             if (need < grid) grid = (int)need;
             ProfScope ps(GBMP_PROF_CHECK_STATES, s);
-            k_check_states<false, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(D, E, d_q, n, d_verdict,
-                                                                                  nullptr, nullptr);
+            k_check_states<false, SPL><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(D, E, d_q, n, d_verdict, nullptr,
+                                                                                  nullptr, d_poses, d_centers);
         }
     });
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
 }
 
-gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to, int64_t E,
-                             float res, int32_t rule, uint8_t *d_ok, int32_t *d_first_hit, float *d_length,
-                             int32_t *d_num_steps, void *stream) {
+gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int64_t n, int32_t mode,
+                              uint8_t *d_verdict, float *d_costs, float *d_total, void *stream) {
+    return gbmp_check_states_fk(r, env, d_q, n, mode, d_verdict, d_costs, d_total, nullptr, nullptr, stream);
+}
+
+gbmp_status gbmp_robot_set_edge_form(gbmp_robot r, int32_t form) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    GBMP_CHECK_ARG(form == 0 || form == 1 || form == 4 || form == 8, "edge form %d is not 0, 1, 4 or 8", form);
+    r->edge_form = form;
+    return GBMP_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Edge validation (replaces SingleArmSpace::checkMotions, SingleArmSpace.cu:628-848).
+// Both entry points run the same kernels; they differ only in where the working memory
+// comes from: gbmp_check_edges grows a buffer owned by the robot handle, and
+// gbmp_check_edges_noalloc uses one fixed array that the library holds on each device.
+// Working memory of E edges of L links:
+//   nsteps[E], first_hit[E], liveA[E]   int    written by the set-up kernel
+//   liveB[E]                            int    written by k_edge_compact
+//   dir[E*L]                            float  written by the set-up kernel
+//   ctr[kMaxWaves + 2]                  int    MUST START AT ZERO (ctr[0] longest edge,
+//                                              ctr[1 + w] live edges entering wave w):
+//                                              zeroed on the stream by every call
+// ---------------------------------------------------------------------------------
+namespace gbmp {
+
+struct EdgeScratch {
+    int *nsteps, *fh, *liveA, *liveB;
+    float *dir;
+    int *ctr;
+};
+
+// Argument checks shared by the edge entry points; on success *res is the step to use.
+static gbmp_status edge_args(gbmp_robot r, gbmp_env env, long long E, float *res, int rule) {
     GBMP_CHECK_ARG(r && env, "robot/env is NULL");
-    GBMP_CHECK_ARG(E >= 0 && E < INT_MAX, "edge count %lld outside [0, 2^31)", (long long)E);
+    GBMP_CHECK_ARG(E >= 0 && E < INT_MAX, "edge count %lld outside [0, 2^31)", E);
     GBMP_CHECK_ARG(rule == GBMP_STEP_L2 || rule == GBMP_STEP_LINF || rule == GBMP_STEP_COUNT, "unknown step rule %d",
                    rule);
-    GBMP_CHECK_ARG(rule != GBMP_STEP_COUNT || (res >= 1.f && res <= 1e6f), "step count %g outside [1, 1e6]", res);
-    if (E == 0) return GBMP_OK;
-    GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
-    if (rule == GBMP_STEP_COUNT) res = floorf(res);
-    if (!(res > 0.f)) res = r->resolution;
-    GBMP_CHECK_ARG(std::isfinite(res), "resolution is not finite");
-    cudaStream_t s = (cudaStream_t)stream;
-    std::lock_guard<std::mutex> lock(r->scratch_mu);
+    GBMP_CHECK_ARG(rule != GBMP_STEP_COUNT || (*res >= 1.f && *res <= 1e6f), "step count %g outside [1, 1e6]", *res);
+    if (rule == GBMP_STEP_COUNT) *res = floorf(*res);
+    if (!(*res > 0.f)) *res = r->resolution;
+    GBMP_CHECK_ARG(std::isfinite(*res), "resolution is not finite");
+    return GBMP_OK;
+}
+
+static gbmp_status edge_validate(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to, long long E,
+                                 float res, int rule, uint8_t *d_ok, int32_t *d_first_hit, float *d_length,
+                                 int32_t *d_num_steps, cudaStream_t s, const EdgeScratch &sc) {
+    int *nsteps = sc.nsteps, *fh = sc.fh, *liveA = sc.liveA, *liveB = sc.liveB, *ctr = sc.ctr;
+    float *dir = sc.dir;
     const int L = r->L;
-    // scratch: nsteps[E], first_hit[E], liveA[E], liveB[E], dir[E*L], ctr[kMaxWaves + 2]
-    // (ctr[0] = longest edge, ctr[1 + w] = live edges entering wave w)
-    const size_t eb = align16(sizeof(int) * (size_t)E);
-    const size_t bytes = 4 * eb + align16(sizeof(float) * (size_t)E * L) + (kMaxWaves + 2) * sizeof(int);
-    gbmp_status st = r->scratch.reserve(bytes);
-    if (st) return st;
-    auto *base = static_cast<unsigned char *>(r->scratch.ptr);
-    int *nsteps = (int *)base, *fh = (int *)(base + eb), *liveA = (int *)(base + 2 * eb),
-        *liveB = (int *)(base + 3 * eb);
-    float *dir = (float *)(base + 4 * eb);
-    int *ctr = (int *)(base + 4 * eb + align16(sizeof(float) * (size_t)E * L));
     GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
     const int tb = 256;
     const unsigned blocks = (unsigned)((E + tb - 1) / tb);
+    gbmp_status st = GBMP_OK;
     if (r->use_cg && rule != GBMP_STEP_COUNT) {   // the generated set-up knows the checkMotions rules
         st = codegen_edge_setup(r, d_from, d_to, E, res, rule, nsteps, dir, fh, liveA, ctr, d_length, d_num_steps, s);
         if (st) return st;
@@ -839,7 +883,7 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
     int grid = 0;
     const bool cull = r->dev.cull != 0;
-    int K = edge_chunk_states(D);
+    int K = edge_chunk_states(D, r->edge_form);
     if (K) {
         st = edge_chunk_prepare(D, Ev, r->num_sms, K, &smem, &grid);
         if (st == GBMP_ERR_CAPACITY) {   // chunk scratch does not fit next to a large scene
@@ -888,29 +932,27 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
         b0 = b1;
         ++wave;
     }
-    { ProfScope ps(GBMP_PROF_OTHER, s);
-    k_edge_finish<<<blocks, tb, 0, s>>>(E, fh, d_ok, d_first_hit); }
+    {
+        ProfScope ps(GBMP_PROF_OTHER, s);
+        k_edge_finish<<<blocks, tb, 0, s>>>(E, fh, d_ok, d_first_hit);
+    }
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
 }
 
-}  // extern "C"
-
 // ---------------------------------------------------------------------------------
-// Edge validation without allocation.  The scratch of gbmp_check_edges lives in one
-// file-scope device array instead of the robot's growable buffer:
-//   [0, 4 Ei)            nsteps[E]      int   written by k_edge_setup
-//   [4 Ei, 8 Ei)         first_hit[E]   int   written by k_edge_setup
-//   [8 Ei, 12 Ei)        liveA[E]       int   written by k_edge_setup
-//   [12 Ei, 16 Ei)       liveB[E]       int   written by k_edge_compact
-//   [16 Ei, +4 D)        dir[E*L]       float written by k_edge_setup
-//   [.., +4 (W+2))       ctr[W+2]       int   MUST START AT ZERO: zeroed on the stream
-//                                             at the start of every call
-// with Ei = kNoAllocMaxEdges, D = kNoAllocMaxDirFloats, W = kMaxWaves.  The array is
-// shared by every call on a device, so calls that overlap on the device race.
+// The fixed working memory of gbmp_check_edges_noalloc: one file-scope device array,
+// laid out as EdgeScratch for up to kNoAllocMaxEdges edges and kNoAllocMaxDirFloats
+// edges x links:
+//   [0, 4 Ei)            nsteps[E]
+//   [4 Ei, 8 Ei)         first_hit[E]
+//   [8 Ei, 12 Ei)        liveA[E]
+//   [12 Ei, 16 Ei)       liveB[E]
+//   [16 Ei, +4 D)        dir[E*L]
+//   [.., +4 (W+2))       ctr[W+2]   zeroed on the stream at the start of every call
+// with Ei = kNoAllocMaxEdges, D = kNoAllocMaxDirFloats, W = kMaxWaves.  Every call on a
+// device shares the array, so calls that overlap on the device race.
 // ---------------------------------------------------------------------------------
-namespace gbmp {
-
 constexpr long long kNoAllocMaxEdges = 65536;
 constexpr long long kNoAllocMaxDirFloats = 1LL << 20;   // n_edges * links
 constexpr size_t kNoAllocEdgeInts = sizeof(int) * kNoAllocMaxEdges;
@@ -923,7 +965,9 @@ static __device__ __align__(256) unsigned char g_edge_scratch[kNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
 
-// Device address of g_edge_scratch on the current device, looked up once per device.
+// Device address of g_edge_scratch on the current device, looked up once per device with
+// that device current (the host-side name g_edge_scratch is not a device address).  The
+// address belongs to the device's context: it is not valid after cudaDeviceReset.
 static gbmp_status noalloc_scratch(unsigned char **out) {
     static std::mutex mu;
     static unsigned char *addr[kNoAllocMaxDevices] = {};
@@ -952,12 +996,30 @@ static gbmp_status noalloc_scratch(unsigned char **out) {
 
 extern "C" {
 
+gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to, int64_t E,
+                             float res, int32_t rule, uint8_t *d_ok, int32_t *d_first_hit, float *d_length,
+                             int32_t *d_num_steps, void *stream) {
+    gbmp_status st = edge_args(r, env, E, &res, rule);
+    if (st) return st;
+    if (E == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lock(r->scratch_mu);
+    const size_t eb = align16(sizeof(int) * (size_t)E);
+    const size_t db = align16(sizeof(float) * (size_t)E * r->L);
+    st = r->scratch.reserve(4 * eb + db + (kMaxWaves + 2) * sizeof(int));
+    if (st) return st;
+    auto *base = static_cast<unsigned char *>(r->scratch.ptr);
+    EdgeScratch sc{(int *)base, (int *)(base + eb), (int *)(base + 2 * eb), (int *)(base + 3 * eb),
+                   (float *)(base + 4 * eb), (int *)(base + 4 * eb + db)};
+    return edge_validate(r, env, d_from, d_to, E, res, rule, d_ok, d_first_hit, d_length, d_num_steps, s, sc);
+}
+
 gbmp_status gbmp_check_edges_noalloc(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to,
                                      int64_t E, float res, int32_t rule, uint8_t *d_ok, int32_t *d_first_hit,
                                      float *d_length, int32_t *d_num_steps, void *stream) {
-    GBMP_CHECK_ARG(r && env, "robot/env is NULL");
-    GBMP_CHECK_ARG(rule == GBMP_STEP_L2 || rule == GBMP_STEP_LINF, "unknown step rule %d", rule);
-    GBMP_CHECK_ARG(E >= 0, "edge count %lld < 0", (long long)E);
+    gbmp_status st = edge_args(r, env, E, &res, rule);
+    if (st) return st;
     if (E > kNoAllocMaxEdges || E * (long long)r->L > kNoAllocMaxDirFloats) {
         set_error("%lld edges x %d links exceed the allocation-free scratch (at most %lld edges and %lld "
                   "edges x links); use gbmp_check_edges or split the call",
@@ -965,78 +1027,15 @@ gbmp_status gbmp_check_edges_noalloc(gbmp_robot r, gbmp_env env, const float *d_
         return GBMP_ERR_CAPACITY;
     }
     unsigned char *base = nullptr;
-    gbmp_status st = noalloc_scratch(&base);   // also the set-up when E == 0
+    st = noalloc_scratch(&base);   // also the per-device set-up when E == 0
     if (st) return st;
     if (E == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
-    if (!(res > 0.f)) res = r->resolution;
-    GBMP_CHECK_ARG(std::isfinite(res), "resolution is not finite");
-    cudaStream_t s = (cudaStream_t)stream;
-    const int L = r->L;
-    int *nsteps = (int *)base, *fh = (int *)(base + kNoAllocEdgeInts), *liveA = (int *)(base + 2 * kNoAllocEdgeInts),
-        *liveB = (int *)(base + 3 * kNoAllocEdgeInts);
-    float *dir = (float *)(base + kNoAllocDirOffset);
-    int *ctr = (int *)(base + kNoAllocCtrOffset);
-    GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
-    const int tb = 256;
-    const unsigned blocks = (unsigned)((E + tb - 1) / tb);
-    k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, fh, liveA, ctr, d_length,
-                                      d_num_steps);
-    GBMP_CUDA(cudaGetLastError());
-    count_launch(1);
-    int n_max = 0;
-    GBMP_CUDA(cudaMemcpyAsync(&n_max, ctr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GBMP_CUDA(cudaStreamSynchronize(s));
-    {
-        int b = 0, waves = 0;
-        while (b < n_max && waves <= kMaxWaves) { b = wave_end(b); ++waves; }
-        if (waves > kMaxWaves) {
-            set_error("an edge has %d interpolated states; at most %d are supported per call", n_max,
-                      max_edge_states());
-            return GBMP_ERR_CAPACITY;
-        }
-    }
-
-    const DevEnv Ev = env->dev();
-    DevRobot D = r->dev;
-    D.work = work_counter();
-    const size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
-    int grid = 0;
-    const bool cull = r->dev.cull != 0;
-    GBMP_SPL_SWITCH(r->dev.spl, {
-        st = cull ? persistent_grid(k_edge_wave<SPL, true>, smem, r->num_sms, &grid)
-                  : persistent_grid(k_edge_wave<SPL, false>, smem, r->num_sms, &grid);
-    });
-    if (st) return st;
-    int b0 = 0, wave = 0;
-    int *live_in = liveA, *live_out = liveB;
-    while (b0 < n_max) {
-        const int b1 = wave_end(b0);
-        int *cnt_in = ctr + 1 + wave, *cnt_out = ctr + 2 + wave;
-        GBMP_SPL_SWITCH(r->dev.spl, {
-            if (cull)
-                k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                    D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
-            else
-                k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                    D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
-        });
-        GBMP_CUDA(cudaGetLastError());
-        count_launch(1);
-        if (b1 < n_max) {
-            k_edge_compact<<<(unsigned)std::min<long long>(blocks, 4LL * r->num_sms), tb, 0, s>>>(
-                live_in, cnt_in, fh, nsteps, b1, live_out, cnt_out);
-            GBMP_CUDA(cudaGetLastError());
-            count_launch(1);
-        }
-        std::swap(live_in, live_out);
-        b0 = b1;
-        ++wave;
-    }
-    k_edge_finish<<<blocks, tb, 0, s>>>(E, fh, d_ok, d_first_hit);
-    GBMP_CUDA(cudaGetLastError());
-    count_launch(1);
-    return GBMP_OK;
+    EdgeScratch sc{(int *)base, (int *)(base + kNoAllocEdgeInts), (int *)(base + 2 * kNoAllocEdgeInts),
+                   (int *)(base + 3 * kNoAllocEdgeInts), (float *)(base + kNoAllocDirOffset),
+                   (int *)(base + kNoAllocCtrOffset)};
+    return edge_validate(r, env, d_from, d_to, E, res, rule, d_ok, d_first_hit, d_length, d_num_steps,
+                         (cudaStream_t)stream, sc);
 }
 
 }  // extern "C"

@@ -12,6 +12,7 @@
 
 #include "../../include/gbmp.h"
 #include "gbmp_device.cuh"
+#include "gbmp_devset.h"
 
 namespace gbmp {
 
@@ -34,6 +35,10 @@ void set_error(const char *fmt, ...);
             return GBMP_ERR_INVALID_ARGUMENT;     \
         }                                         \
     } while (0)
+
+// Raises the dynamic shared-memory limit of kernel `fn` to 227 KB (with the largest
+// shared-memory carveout) on the current device, once per (device, kernel).
+gbmp_status ensure_smem_optin(const void *fn);
 
 constexpr int kMaxSelfPairs = 65535 * 4;
 constexpr int kMaxEnvWords = 12 * 1024;     // 192 KB of float4 staged in shared memory
@@ -114,6 +119,8 @@ struct gbmp_robot_s {
     // device tables (one allocation)
     void *d_block = nullptr;
     gbmp::DevRobot dev{};
+    // edge validation form: 0 automatic, 1 state by state, 4 or 8 states per chunk
+    int edge_form = 0;
     // edge-check scratch
     std::mutex scratch_mu;
     gbmp::DevBuf scratch;
@@ -130,8 +137,9 @@ gbmp_status codegen_edge_setup(const gbmp_robot_s *r, const float *from, const f
                                int rule, int *nsteps, float *dir, int *first_hit, int *live, int *ctr,
                                float *length_out, int *nsteps_out, cudaStream_t s);
 // Edge validation by chunks of consecutive states (gbmp_chunk.cu).  K = states per
-// chunk for this robot (0: use the per-state kernels); GBMP_EDGE_CHUNK=1|4|8 overrides.
-int edge_chunk_states(const DevRobot &R);
+// chunk for this robot (0: use the per-state kernels); `form` is the robot handle's
+// edge_form (0 automatic, 1 per state, 4 or 8 states per chunk).
+int edge_chunk_states(const DevRobot &R, int form);
 gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid);
 gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int grid, size_t smem, cudaStream_t s,
                               const float *from, const float *to, const int *nsteps, const float *dir,

@@ -1,0 +1,75 @@
+// gbmp_rrtc.cuh -- types and kernel declarations of the parallel RRT-Connect planner
+// (gbmp_rrtc.cu).  The planning kernels are defined in gbmp_rrtc_device.cuh and
+// instantiated, one spheres-per-lane range each, in the gbmp_rrtc_k*.cu / gbmp_rrtc_b*.cu
+// translation units so that they compile in parallel.
+#pragma once
+
+#include "gbmp_internal.h"
+
+namespace gbmp {
+
+constexpr int kRrtcWarps = 4;
+constexpr int kRrtcThreads = kRrtcWarps * kWarp;
+
+enum : int { kStRunning = 0, kStSolved = 1, kStNodeCap = 2, kStIterCap = 3, kStDeadline = 4 };
+
+struct RrtcDev {
+    float *nodes[2];          // [cap * stride], NaN until written
+    float *radii[2];          // [cap] dynamic-domain radii (kRadiusUnset until a failure), or null
+    int *parent[2];           // [cap]
+    int *size;                // [2] allocated slots per tree
+    int *state;               // [0] status, [1] winning lane, [2] tree of the new node,
+                              // [3] node in that tree, [4] node in the other tree, [5] max iteration
+    float *path;              // [path_cap * L]
+    int *path_len;            // [1], -1 if the path buffer was too small
+    int cap, stride, path_cap;
+    volatile int *flag;       // host-mapped completion word (batched solves) or null:
+                              // path length + 1 when solved, -status when ended without a path
+};
+
+struct RrtcParams {
+    int lanes, max_iters, rule;
+    float range, res;
+    unsigned long long seed;
+    unsigned long long deadline_ns;   // absolute %globaltimer value, or
+    const unsigned long long *deadline_ptr;   // read from device memory when non-null
+    int dd = 0;                       // dynamic domain on (needs RrtcDev::radii)
+    float dd_alpha = 0.f, dd_radius = 0.f, dd_min = 0.f;
+};
+
+// Dynamic-domain radius of a node that has not failed yet (the bytes 0x7f of a memset;
+// 3.4e38, so it never rejects a sample).
+constexpr unsigned kRadiusUnset = 0x7f7f7f7fu;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// A problem of a batched launch: its robot, scene, trees and Philox key.
+struct BatchProblem {
+    DevRobot R;
+    DevEnv E;
+    RrtcDev P;
+    unsigned long long seed;
+    const float *start, *goal;      // device copies of the roots
+    int prev[2];                    // node words the previous solve wrote (to reset)
+};
+
+// Launchers of the planning kernels, defined by the instantiation units: *_lo for 1 to 4
+// spheres per lane, *_hi for 5 to 8.  Each sets the kernel's dynamic shared-memory limit
+// to `smem` and launches `grid` blocks of kRrtcThreads on `st`; the CUDA error of either
+// step is returned.
+cudaError_t rrtc_launch_lo(int spl, bool cull, int grid, size_t smem, cudaStream_t st, const DevRobot &R,
+                           const DevEnv &E, const RrtcDev &P, const RrtcParams &prm);
+cudaError_t rrtc_launch_hi(int spl, bool cull, int grid, size_t smem, cudaStream_t st, const DevRobot &R,
+                           const DevEnv &E, const RrtcDev &P, const RrtcParams &prm);
+cudaError_t rrtc_batch_launch_lo(int spl, bool cull, int grid, size_t smem, cudaStream_t st,
+                                 const BatchProblem *probs, int n, int lanes_per_problem, const RrtcParams &prm,
+                                 int *rr);
+cudaError_t rrtc_batch_launch_hi(int spl, bool cull, int grid, size_t smem, cudaStream_t st,
+                                 const BatchProblem *probs, int n, int lanes_per_problem, const RrtcParams &prm,
+                                 int *rr);
+
+}  // namespace gbmp

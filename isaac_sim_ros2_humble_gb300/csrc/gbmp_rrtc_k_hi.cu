@@ -1,0 +1,8 @@
+// gbmp_rrtc_k_hi.cu -- single-problem planning kernels for 5 to 8 spheres per lane (one of the
+// four translation units that instantiate the planner's kernels, so that they compile in
+// parallel).
+#include "gbmp_rrtc_device.cuh"
+
+namespace gbmp {
+GBMP_RRTC_DEFINE_LAUNCHER(rrtc_launch_hi, 5)
+}  // namespace gbmp

@@ -23,7 +23,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_INCLUDE = "/root/reference/cudampl/CUDAMPLib/include"
+# The reference tree (read-only); GBMP_REFERENCE_ROOT points elsewhere when it lies elsewhere.
+REF_ROOT = os.environ.get("GBMP_REFERENCE_ROOT", "/root/reference")
+REF_INCLUDE = os.path.join(REF_ROOT, "cudampl/CUDAMPLib/include")
 GEN = os.path.join(OUT, "ref_gen")
 
 _HARNESS = r'''
@@ -128,7 +130,7 @@ def robot_kernels(robot):
 # inverse-pose helpers and the body of the self-collision constructor (the pair list),
 # and compiles those for the host with oracle/ref_block_shim.h.
 # ---------------------------------------------------------------------------------
-REF_SRC = "/root/reference/cudampl/CUDAMPLib/src/constraints"
+REF_SRC = os.path.join(REF_ROOT, "cudampl/CUDAMPLib/src/constraints")
 
 _COST_HARNESS = r'''
 #include "ref_block_shim.h"
@@ -298,7 +300,7 @@ def cost_kernels():
 # The state manager's nearest-neighbour and steer kernels and the sphere transform of
 # SingleArmStates::update (cudampl/CUDAMPLib/src/states/SingleArmStates.cu), taken the
 # same way.
-REF_STATES = "/root/reference/cudampl/CUDAMPLib/src/states/SingleArmStates.cu"
+REF_STATES = os.path.join(REF_ROOT, "cudampl/CUDAMPLib/src/states/SingleArmStates.cu")
 
 _MANAGER_HARNESS = r'''
 #include "ref_block_shim.h"
@@ -366,7 +368,7 @@ def manager_kernels():
 # the same way.  Each source's kernels sit in a namespace of their own (the two
 # constraint files both name their kernel computeGradientErrorKernel and both define
 # multiply4x4).
-REF_SPACE = "/root/reference/cudampl/CUDAMPLib/src/spaces/SingleArmSpace.cu"
+REF_SPACE = os.path.join(REF_ROOT, "cudampl/CUDAMPLib/src/spaces/SingleArmSpace.cu")
 REF_TASK = os.path.join(REF_SRC, "TaskSpaceConstraint.cu")
 REF_BOUND = os.path.join(REF_SRC, "BoundaryConstraint.cu")
 
@@ -499,7 +501,7 @@ def project_kernels():
 # distance functions and sphere_environment_in_collision), over the reference's own
 # shape and environment types (pRRTC/src/collision/shapes.hh, environment.hh, math.hh,
 # included where they lie).
-REF_PRRTC = "/root/reference/pRRTC/src"
+REF_PRRTC = os.path.join(REF_ROOT, "pRRTC/src")
 
 _PRRTC_HARNESS = r'''
 #include <array>

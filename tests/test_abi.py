@@ -132,3 +132,15 @@ def test_struct_layouts_match_ctypes(tmp_path):
         assert got[(cname, "sizeof")] == C.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
+def test_kernel_setup_is_recorded_per_device(tmp_path):
+    """The record of kernels whose shared-memory limit was raised is keyed by (device,
+    kernel): configuring a kernel on one device does not count for another."""
+    exe = tmp_path / "devset_check"
+    src = os.path.join(ROOT, "tests", "cpp", "devset_check.cpp")
+    inc = os.path.join(ROOT, "isaac_sim_ros2_humble_gb300", "csrc")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-pthread", "-I", inc, src, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "devset ok" in out.stdout

@@ -99,6 +99,35 @@ def test_check_states_costs(plain, edge):
         np.testing.assert_array_equal(v.cpu().numpy().astype(bool)[clear], (ot > 0)[clear])
 
 
+def test_check_states_fk_is_one_fk_for_both_outputs(plain, edge):
+    """gbmp_check_states_fk (the reference's update() + checkStates() as one launch):
+    poses and sphere centres bit-identical to gbmp_fk's, verdicts and costs identical to
+    gbmp_check_states', on the 4,096-configuration plain workload and the edge arm."""
+    for robot, q, R, E in ((plain[0], plain[2], plain[4], plain[5]), (edge[0], edge[2], edge[5], edge[6])):
+        n, L, S = q.shape[0], robot.num_links, robot.num_spheres
+        p_ref = torch.zeros((n, L, 16), device="cuda")
+        c_ref = torch.zeros((n, S, 3), device="cuda")
+        api.fk(R, dev(q), p_ref, c_ref)
+        for mode in (_lib.CHECK_VERDICT, _lib.CHECK_COST):
+            v_ref = torch.zeros(n, dtype=torch.uint8, device="cuda")
+            t_ref = torch.zeros(n, device="cuda")
+            api.check_states(R, E, dev(q), verdict=v_ref, total=t_ref if mode else None, mode=mode)
+            poses = torch.full((n, L, 16), float("nan"), device="cuda")
+            cen = torch.full((n, S, 3), float("nan"), device="cuda")
+            v = torch.zeros(n, dtype=torch.uint8, device="cuda")
+            t = torch.zeros(n, device="cuda")
+            api.check_states(R, E, dev(q), verdict=v, total=t if mode else None, mode=mode, poses=poses, centers=cen)
+            torch.cuda.synchronize()
+            assert torch.equal(poses, p_ref) and torch.equal(cen, c_ref)
+            assert torch.equal(v, v_ref) and torch.equal(t, t_ref)
+        # one output alone
+        poses = torch.zeros((n, L, 16), device="cuda")
+        v = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        api.check_states(R, E, dev(q), verdict=v, poses=poses)
+        torch.cuda.synchronize()
+        assert torch.equal(poses, p_ref)
+
+
 def _edge_parity(m, qf, qt, res, rule, ok, fh, ln, ns):
     o_ok, o_fh, o_ns, o_ln = m.check_motions(qf, qt, res, rule, early_exit=True)
     np.testing.assert_array_equal(ns, o_ns)
@@ -304,6 +333,24 @@ def test_check_edges_full_size_sampled_parity():
     assert len(ok) == 65536
     np.testing.assert_array_equal(ok, fh < 0)
     assert 0 < ok.sum() < len(ok)
-    pick = np.sort(np.random.default_rng(11).choice(len(qf), size=384, replace=False))
+    pick = np.sort(np.random.default_rng(11).choice(len(qf), size=2048, replace=False))
     m = O.OracleModel(robot, env)
     _edge_parity(m, qf[pick], qt[pick], 0.01, 1, ok[pick], fh[pick], ln[pick], ns[pick])
+
+
+def test_edge_forms_agree_on_every_edge_of_the_benchmark_call():
+    """All 65,536 edges of the benchmark call validated state by state (k_edge_wave) and by
+    chunks of 4 and 8 states (k_edge_chunk): identical verdicts, first hits, state counts
+    and lengths on every edge (the chunk form's narrow tests are the per-state tests)."""
+    robot, env, qf, qt = W.edge_workload()
+    R, E = api.Robot(robot), api.Env(env)
+    out = {}
+    for form in (1, 4, 8):
+        R.set_edge_form(form)
+        out[form] = _run_edges(R, E, qf, qt, 0.01, 1)
+    R.set_edge_form(0)
+    for form in (4, 8):
+        for a, b in zip(out[form], out[1]):
+            np.testing.assert_array_equal(a, b)
+    with pytest.raises(_lib.GbmpError):
+        R.set_edge_form(3)

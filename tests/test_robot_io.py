@@ -184,7 +184,7 @@ def test_loaded_robot_runs_on_the_gpu():
     np.testing.assert_array_equal(v.cpu().numpy().astype(bool)[clear], (m.check_states(q)[1] > 0)[clear])
 
 
-REF = "/root/reference"
+from ref_build import REF_ROOT as REF  # noqa: E402  (oracle/ref_build.py: the reference tree, if present)
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "problems")), reason="reference tree not present")

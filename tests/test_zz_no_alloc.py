@@ -73,17 +73,29 @@ def test_noalloc_matches_check_edges_on_two_calls(cases):
 
 
 def test_noalloc_takes_no_device_memory(cases):
+    """A robot handle that only ever sees the allocation-free entry point: after the
+    per-device set-up call (no edges), neither its first real call nor later ones take
+    device memory.  The module fixture already ran gbmp_check_edges with a robot of the
+    same tables, so the kernels this call uses are loaded."""
     lib, cs = cases
-    R, E, qf, qt, res, rule = cs[0]
+    _, E, qf, qt, res, rule = cs[0]
+    robot, _, _, _ = W.edge_workload(n_edges=8)
+    R = api.Robot(robot)
     outs = outputs(qf.shape[0])
-    _lib.check(call(lib.gbmp_check_edges_noalloc, R, E, qf, qt, res, rule, outs))
+    torch.cuda.synchronize()
+    assert lib.gbmp_check_edges_noalloc(R.handle, E.handle, None, None, 0, 0.01, rule, None, None, None, None,
+                                        None) == _lib.OK
     torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info()
+    _lib.check(call(lib.gbmp_check_edges_noalloc, R, E, qf, qt, res, rule, outs))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "the first call took device memory"
     for _ in range(2):
         _lib.check(call(lib.gbmp_check_edges_noalloc, R, E, qf, qt, res, rule, outs))
     torch.cuda.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
-    assert free1 == free0
+    free2, _ = torch.cuda.mem_get_info()
+    assert free2 == free0, "later calls took device memory"
 
 
 def test_noalloc_rejects_calls_beyond_its_scratch(cases):
