@@ -255,7 +255,7 @@ def bench_plain(args, flush, fp32_peak):
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
-    steps = max(50, args.steps)
+    steps = max(2000, args.steps)   # a ~0.3 s timed region, long enough for the clock samples
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     clk = ClockSampler(torch.cuda.current_device()).start()
     _lib.profile_reset()
@@ -287,7 +287,7 @@ def bench_plain(args, flush, fp32_peak):
     h_v = torch.empty(n, dtype=torch.uint8).pin_memory()
     h_p = torch.empty((n, L, 16), dtype=torch.float32).pin_memory()
     e2e_ms = []
-    for i in range(3 + steps):
+    for i in range(3 + min(steps, 200)):
         flush.fill_(float(i))
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -286,7 +286,7 @@ typedef struct gbmp_rrtc_settings {
     uint64_t seed;          /* Philox key; sample (lane, iteration, joint)                */
     double time_limit_s;    /* device-side deadline (<= 0: 10 s)                          */
     /* pRRTC's dynamic domain (pRRTC/src/planning/pRRTC.cu:418-424, :456-467, :584-596),
-     * single-problem solves only: a sample farther from its nearest node than that node's
+     * in single-problem and batched solves: a sample farther from its nearest node than that node's
      * radius is skipped; a failed extension sets the node's radius to dd_radius, or
      * shrinks it by (1 - dd_alpha) down to dd_min_radius; a successful one grows it by
      * (1 + dd_alpha).  0 = off (the other three are then ignored). */
@@ -294,7 +294,21 @@ typedef struct gbmp_rrtc_settings {
     float dd_alpha;
     float dd_radius;
     float dd_min_radius;
+    /* pRRTC's tree balancing (pRRTC/src/planning/pRRTC.cu:348-371, pRRTC_settings.hh:10-11),
+     * the tree each lane grows per iteration: GBMP_BALANCE_DEFAULT (0) and GBMP_BALANCE_SIZE
+     * pRRTC strategy 1: lanes split in proportion to the other tree's share while the
+     * trees differ by less than 1.5 x lanes nodes, else every lane grows tree 0 when its
+     * share of the nodes is below tree_ratio and tree 1 otherwise; GBMP_BALANCE_SWAP
+     * strategy 2: a lane keeps its tree and swaps while the size difference relative to
+     * its tree is below tree_ratio; GBMP_BALANCE_NONE (pRRTC's 0): half the lanes per tree.
+     * tree_ratio <= 0 takes pRRTC's default for the strategy (0.5, or 1.0 for strategy 2). */
+    int32_t balance;
+    float tree_ratio;
 } gbmp_rrtc_settings;
+#define GBMP_BALANCE_DEFAULT 0
+#define GBMP_BALANCE_SIZE 1
+#define GBMP_BALANCE_SWAP 2
+#define GBMP_BALANCE_NONE 3
 
 typedef struct gbmp_rrtc_result {
     int32_t solved;

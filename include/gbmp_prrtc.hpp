@@ -8,8 +8,9 @@
  * gbmp_rrtc_solve_goals: every goal a root of the goal tree (pRRTC.cu:686-693), each
  * edge checked at `granularity` equal steps (GBMP_STEP_COUNT), `num_new_configs`
  * extension lanes, `range` steering, `max_samples` nodes per tree, `max_iters` lane
- * iterations, Philox samples with key 1 (pRRTC seeds its generators with 1), and the
- * dynamic domain with its dd_* settings.
+ * iterations, Philox samples with key 1 (pRRTC seeds its generators with 1), the
+ * dynamic domain with its dd_* settings, and tree balancing by `balance` (0 none, 1
+ * size, 2 swap) with `tree_ratio` (pRRTC.cu:348-371).
  *
  * The reference's Robot types carry generated FK and collision code.  Here a Robot type
  * names the libgbmp robot model to plan for and the configuration layout:
@@ -30,8 +31,6 @@
  *     first two axes and the z axis, as sphere_z_aligned_cuboid does;
  *   - `cylinders` are not tested by the reference's sphere_environment_in_collision and
  *     are not converted either.
- * Not reproduced: balance strategy 2 and tree_ratio (lanes share the trees by the
- * balance-1 rule); they change which tree a lane grows, not what a valid path is.
  * Errors other than "no path" are thrown as std::runtime_error with gbmp_last_error().
  */
 #pragma once
@@ -265,6 +264,8 @@ PlannerResult<Robot> solve(typename Robot::Configuration &start, std::vector<typ
     const auto t0 = Clock::now();
     PlannerResult<Robot> out;
     if (goals.empty()) throw std::invalid_argument("pRRTC::solve: no goals");
+    if (settings.balance != 0 && settings.balance != 1 && settings.balance != 2)
+        throw std::invalid_argument("pRRTC::solve: balance must be 0, 1 or 2");
     gbmp_robot robot = Robot::handle();
     int32_t L = 0, S = 0, P = 0, dim = 0, cg = 0;
     check(gbmp_robot_info(robot, &L, &S, &P, &dim, &cg));
@@ -301,6 +302,8 @@ PlannerResult<Robot> solve(typename Robot::Configuration &start, std::vector<typ
     s.dd_alpha = settings.dd_alpha;
     s.dd_radius = settings.dd_radius;
     s.dd_min_radius = settings.dd_min_radius;
+    s.balance = settings.balance == 0 ? GBMP_BALANCE_NONE : (settings.balance == 2 ? GBMP_BALANCE_SWAP : GBMP_BALANCE_SIZE);
+    s.tree_ratio = settings.tree_ratio;
     // uninitialised: only the rows of the returned path are ever written or read
     std::unique_ptr<float[]> path(new float[(std::size_t)path_cap * L]);
     gbmp_rrtc_result r{};

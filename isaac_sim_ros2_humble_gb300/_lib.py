@@ -19,6 +19,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "CUDA er
           8: "unsupported"}
 CHECK_VERDICT, CHECK_COST = 0, 1
 STEP_L2, STEP_LINF, STEP_COUNT = 0, 1, 2
+BALANCE_DEFAULT, BALANCE_SIZE, BALANCE_SWAP, BALANCE_NONE = 0, 1, 2, 3
 ROBOT_GENERIC, ROBOT_CODEGEN = 0, 1
 
 
@@ -45,7 +46,7 @@ class RrtcSettings(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("max_iters", C.c_int32), ("range", C.c_float), ("resolution", C.c_float),
                 ("step_rule", C.c_int32), ("seed", C.c_uint64), ("time_limit_s", C.c_double),
                 ("dynamic_domain", C.c_int32), ("dd_alpha", C.c_float), ("dd_radius", C.c_float),
-                ("dd_min_radius", C.c_float)]
+                ("dd_min_radius", C.c_float), ("balance", C.c_int32), ("tree_ratio", C.c_float)]
 
 
 class RrtcResult(C.Structure):

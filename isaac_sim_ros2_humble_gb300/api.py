@@ -212,14 +212,16 @@ class Planner:
     def solve(self, env: Env, start, goal, lanes: int = 1024, max_iters: int = 100000, range_: float = 0.1,
               resolution: float = 0.0, rule: int = _lib.STEP_L2, seed: int = 0, time_limit_s: float = 10.0,
               stream=None, raise_on_failure: bool = False, dynamic_domain: bool = False, dd_alpha: float = 1e-4,
-              dd_radius: float = 4.0, dd_min_radius: float = 1.0):
+              dd_radius: float = 4.0, dd_min_radius: float = 1.0, balance: int = _lib.BALANCE_DEFAULT,
+              tree_ratio: float = 0.0):
         """Returns (result, path): result is a dict of the C result struct, path the
         [path_len, L] float32 waypoints (empty when not solved).  `goal` is one full joint
         vector [L] or several [n, L] (every one a root of the goal tree).  dynamic_domain
-        turns on pRRTC's dynamic-domain sampling with its dd_* parameters."""
+        turns on pRRTC's dynamic-domain sampling with its dd_* parameters; balance and
+        tree_ratio choose pRRTC's tree-balancing strategy (gbmp_rrtc_settings)."""
         st = _lib.RrtcSettings(int(lanes), int(max_iters), float(range_), float(resolution), int(rule), int(seed),
                                float(time_limit_s), int(bool(dynamic_domain)), float(dd_alpha), float(dd_radius),
-                               float(dd_min_radius))
+                               float(dd_min_radius), int(balance), float(tree_ratio))
         res = _lib.RrtcResult()
         s0 = _c(start, np.float32).reshape(-1)
         g0 = _c(goal, np.float32).reshape(-1, self.robot.L)
@@ -260,7 +262,8 @@ class BatchPlanner:
 
     def solve(self, problems, lanes_per_problem: int = 8, use_graph: bool = True, max_iters: int = 100000,
               range_: float = 0.1, resolution: float = 0.0, rule: int = _lib.STEP_L2, time_limit_s: float = 10.0,
-              stream=None):
+              stream=None, dynamic_domain: bool = False, dd_alpha: float = 1e-4, dd_radius: float = 4.0,
+              dd_min_radius: float = 1.0, balance: int = _lib.BALANCE_DEFAULT, tree_ratio: float = 0.0):
         """problems: list of (Robot, Env, start[L], goal[L], seed).  Returns a list of
         (result dict, path [path_len, L])."""
         n = len(problems)
@@ -270,7 +273,9 @@ class BatchPlanner:
             a, b = _c(s0, np.float32).reshape(-1), _c(g0, np.float32).reshape(-1)
             keep += [a, b]
             arr[i] = _lib.RrtcProblem(R.handle.value, E.handle.value, a.ctypes.data, b.ctypes.data, int(seed))
-        st = _lib.RrtcSettings(0, int(max_iters), float(range_), float(resolution), int(rule), 0, float(time_limit_s))
+        st = _lib.RrtcSettings(0, int(max_iters), float(range_), float(resolution), int(rule), 0, float(time_limit_s),
+                               int(bool(dynamic_domain)), float(dd_alpha), float(dd_radius), float(dd_min_radius),
+                               int(balance), float(tree_ratio))
         res = (_lib.RrtcResult * n)()
         paths = self._paths[:n]
         check(_lib.load().gbmp_rrtc_solve_batch(self.handle, n, arr, C.byref(st), int(lanes_per_problem),

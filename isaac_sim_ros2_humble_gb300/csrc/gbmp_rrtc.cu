@@ -44,6 +44,13 @@ __global__ void k_rrtc_batch_reset(BatchProblem *__restrict__ probs, int n, unsi
         for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < words;
              i += (long long)gridDim.x * blockDim.x)
             b.P.nodes[t][i] = __int_as_float(0xffffffff);
+        // dynamic-domain radii of at least as many nodes back to unset
+        if (b.P.radii[t]) {
+            const long long nodes = min(words, (long long)b.P.cap);
+            for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nodes;
+                 i += (long long)gridDim.x * blockDim.x)
+                b.P.radii[t][i] = __uint_as_float(kRadiusUnset);
+        }
     }
     __syncthreads();
     if (blockIdx.x == 0) {
@@ -147,6 +154,26 @@ static bool plan_step(const gbmp_rrtc_settings *s, float robot_res, float *res) 
     return *res > 0.f;
 }
 
+// Balance strategy of a solve in the device encoding (0 none, 1 size, 2 swap) and its
+// tree ratio; false on an unknown strategy or a non-finite ratio.
+static bool plan_balance(const gbmp_rrtc_settings *s, int *balance, float *ratio) {
+    switch (s->balance) {
+    case GBMP_BALANCE_DEFAULT:
+    case GBMP_BALANCE_SIZE: *balance = 1; break;
+    case GBMP_BALANCE_SWAP: *balance = 2; break;
+    case GBMP_BALANCE_NONE: *balance = 0; break;
+    default: return false;
+    }
+    if (!std::isfinite(s->tree_ratio)) return false;
+    *ratio = s->tree_ratio > 0.f ? s->tree_ratio : (*balance == 2 ? 1.0f : 0.5f);
+    return true;
+}
+
+static bool plan_dd_ok(const gbmp_rrtc_settings *s) {
+    return !s->dynamic_domain || (s->dd_alpha >= 0.f && s->dd_alpha < 1.f && s->dd_radius > 0.f &&
+                                  s->dd_min_radius > 0.f && std::isfinite(s->dd_radius));
+}
+
 struct gbmp_planner_s {
     gbmp_robot robot = nullptr;
     int cap = 0, stride = 0, path_cap = 0;
@@ -216,9 +243,10 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     GBMP_CHECK_ARG(s->max_iters >= 1, "max_iters < 1");
     float step_res = 0.f;
     GBMP_CHECK_ARG(plan_step(s, r->resolution, &step_res), "unknown step rule or resolution out of range");
-    GBMP_CHECK_ARG(!s->dynamic_domain || (s->dd_alpha >= 0.f && s->dd_alpha < 1.f && s->dd_radius > 0.f &&
-                                          s->dd_min_radius > 0.f && std::isfinite(s->dd_radius)),
-                   "dynamic domain needs 0 <= dd_alpha < 1 and positive radii");
+    GBMP_CHECK_ARG(plan_dd_ok(s), "dynamic domain needs 0 <= dd_alpha < 1 and positive radii");
+    int balance = 1;
+    float tree_ratio = 0.5f;
+    GBMP_CHECK_ARG(plan_balance(s, &balance, &tree_ratio), "unknown balance strategy %d or tree ratio", s->balance);
     for (int j = 0; j < L; ++j) GBMP_CHECK_ARG(std::isfinite(h_start[j]), "start not finite");
     for (long long j = 0; j < (long long)n_goals * L; ++j) GBMP_CHECK_ARG(std::isfinite(h_goals[j]), "goal not finite");
     memset(res, 0, sizeof *res);
@@ -258,6 +286,8 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     prm.dd_alpha = s->dd_alpha;
     prm.dd_radius = s->dd_radius;
     prm.dd_min = s->dd_min_radius;
+    prm.balance = balance;
+    prm.tree_ratio = tree_ratio;
     // device deadline from the host clock offset: read %globaltimer through a 1-thread probe
     unsigned long long now_ns = 0;
     {
@@ -362,7 +392,7 @@ struct gbmp_batch_planner_s {
     std::vector<int> prev;                // 2 per problem
     // captured graphs by launch shape (a few shapes, least recently used evicted)
     struct Captured {
-        long long key[8];
+        long long key[12];
         cudaGraphExec_t exec;
         long long used;
     };
@@ -426,7 +456,8 @@ gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, i
     b->stride = (max_links + 3) & ~3;
     const size_t nodes_b = align16(sizeof(float) * (size_t)max_nodes * b->stride);
     const size_t par_b = align16(sizeof(int) * (size_t)max_nodes);
-    b->per_problem = 2 * nodes_b + 2 * par_b + 256 + align16(sizeof(float) * (size_t)path_cap * max_links);
+    const size_t rad_b = align16(sizeof(float) * (size_t)max_nodes);   // dynamic-domain radii, per tree
+    b->per_problem = 2 * nodes_b + 2 * par_b + 256 + align16(sizeof(float) * (size_t)path_cap * max_links) + 2 * rad_b;
     cudaError_t e = cudaMalloc(&b->pool, b->per_problem * max_problems);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(BatchProblem) * max_problems);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_table, sizeof(BatchProblem) * max_problems);
@@ -446,6 +477,9 @@ gbmp_status gbmp_batch_planner_create(int32_t max_problems, int32_t max_nodes, i
     }
     // every tree starts fully reset once
     e = cudaMemset(b->pool, 0xff, b->per_problem * max_problems);
+    if (e == cudaSuccess)   // every dynamic-domain radius unset (kRadiusUnset = bytes 0x7f)
+        e = cudaMemset2D(static_cast<unsigned char *>(b->pool) + b->per_problem - 2 * rad_b, b->per_problem, 0x7f,
+                         2 * rad_b, max_problems);
     if (e != cudaSuccess) {
         set_error("batch planner reset failed: %s", cudaGetErrorString(e));
         gbmp_batch_planner_destroy(b);
@@ -494,6 +528,10 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
     GBMP_CHECK_ARG(lanes_per_problem >= 1 && lanes_per_problem <= 4096, "lanes_per_problem outside [1, 4096]");
     GBMP_CHECK_ARG((long long)n * lanes_per_problem <= (1LL << 30), "too many blocks");
     GBMP_CHECK_ARG(s->range > 0.f && s->max_iters >= 1, "bad settings");
+    GBMP_CHECK_ARG(plan_dd_ok(s), "dynamic domain needs 0 <= dd_alpha < 1 and positive radii");
+    int balance = 1;
+    float tree_ratio = 0.5f;
+    GBMP_CHECK_ARG(plan_balance(s, &balance, &tree_ratio), "unknown balance strategy %d or tree ratio", s->balance);
     float step_res = 0.f;
     GBMP_CHECK_ARG(plan_step(s, problems[0].robot ? problems[0].robot->resolution : 0.f, &step_res),
                    "unknown step rule or resolution out of range");
@@ -503,6 +541,7 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
     auto *pool = static_cast<unsigned char *>(b->pool);
     const size_t nodes_b = align16(sizeof(float) * (size_t)b->cap * b->stride);
     const size_t par_b = align16(sizeof(int) * (size_t)b->cap);
+    const size_t rad_b = align16(sizeof(float) * (size_t)b->cap);
     for (int i = 0; i < n; ++i) {
         const gbmp_rrtc_problem &pr = problems[i];
         GBMP_CHECK_ARG(pr.robot && pr.env && pr.start && pr.goal, "problem %d has a NULL field", i);
@@ -530,7 +569,10 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
         bp.P.path = (float *)(base + 2 * nodes_b + 2 * par_b + 256);
         bp.P.cap = b->cap;
         bp.P.stride = (pr.robot->L + 3) & ~3;   // its own joints, padded to float4 words
-        bp.P.radii[0] = bp.P.radii[1] = nullptr;  // no dynamic domain in batched solves
+        // dynamic-domain radii: the last two regions of the problem's block, reset by every
+        // solve (used only when the settings turn the dynamic domain on)
+        bp.P.radii[0] = (float *)(base + b->per_problem - 2 * rad_b);
+        bp.P.radii[1] = (float *)(base + b->per_problem - rad_b);
         bp.P.path_cap = b->path_cap;
         bp.P.flag = b->d_flags + i;
         bp.seed = pr.seed;
@@ -554,12 +596,25 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
     prm.seed = 0;
     prm.deadline_ns = 0;
     prm.deadline_ptr = b->d_deadline;
+    prm.dd = s->dynamic_domain ? 1 : 0;
+    prm.dd_alpha = s->dd_alpha;
+    prm.dd_radius = s->dd_radius;
+    prm.dd_min = s->dd_min_radius;
+    prm.balance = balance;
+    prm.tree_ratio = tree_ratio;
     const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
     b->cur_n = n;
     GBMP_CUDA(cudaEventRecord(b->ev0, st));
     if (use_graph) {
-        const long long key[8] = {n, lanes_per_problem, (long long)smem, spl, cull, s->max_iters,
-                                  (long long)(lim * 1e6), (long long)(prm.range * 1e6) ^ ((long long)(prm.res * 1e9) << 20)};
+        float dd_f[3] = {prm.dd_alpha, prm.dd_radius, prm.dd_min};
+        unsigned dd_bits[3];
+        memcpy(dd_bits, dd_f, sizeof dd_bits);
+        unsigned tr_bits = 0;
+        memcpy(&tr_bits, &prm.tree_ratio, sizeof tr_bits);
+        const long long key[12] = {n, lanes_per_problem, (long long)smem, spl, cull, s->max_iters,
+                                   (long long)(lim * 1e6), (long long)(prm.range * 1e6) ^ ((long long)(prm.res * 1e9) << 20),
+                                   prm.dd ? (long long)dd_bits[0] | ((long long)dd_bits[1] << 32) : -1,
+                                   prm.dd ? (long long)dd_bits[2] : -1, prm.balance, (long long)tr_bits};
         cudaGraphExec_t exec = nullptr;
         for (auto &g : b->graphs)
             if (memcmp(key, g.key, sizeof key) == 0) { exec = g.exec; g.used = ++b->use_clock; }

@@ -35,7 +35,35 @@ struct RrtcParams {
     const unsigned long long *deadline_ptr;   // read from device memory when non-null
     int dd = 0;                       // dynamic domain on (needs RrtcDev::radii)
     float dd_alpha = 0.f, dd_radius = 0.f, dd_min = 0.f;
+    int balance = 1;                  // pRRTC balance strategy: 0 none, 1 size, 2 swap
+    float tree_ratio = 0.5f;
 };
+
+// Lane hash in [0, 1) (Fibonacci hashing of the lane index): the share of lanes below h
+// stands for pRRTC's block index over the block count, whatever the lane count and
+// however batched lanes are numbered.
+__host__ __device__ inline float lane_hash(int lane) {
+    return (float)(((unsigned)lane * 2654435769u) >> 8) * (1.0f / 16777216.0f);
+}
+
+// Tree a lane grows (pRRTC.cu:348-371).  n0, n1: tree sizes; cur: the lane's tree in its
+// previous iteration, -1 at its first (half the lanes per tree, pRRTC's iteration 1).
+// Strategy 1 splits the lanes in proportion to the other tree's share while the trees
+// differ by less than 1.5 x lanes nodes, else grows tree 0 while its share is below
+// tree_ratio; strategy 2 swaps a lane's tree while the size difference relative to it
+// is below tree_ratio.
+__host__ __device__ inline int balance_tree(int balance, float tree_ratio, int lanes, int n0, int n1, float h,
+                                            int cur) {
+    if (cur < 0 || balance == 0) return h < 0.5f ? 0 : 1;
+    if (balance == 2) {
+        const int nt = cur == 0 ? n0 : n1, no = cur == 0 ? n1 : n0;
+        const float ratio = (float)abs(nt - no) / (float)(nt > 1 ? nt : 1);
+        return ratio < tree_ratio ? 1 - cur : cur;
+    }
+    const float ratio = (float)n0 / (float)(n0 + n1 > 1 ? n0 + n1 : 1);
+    if ((float)abs(n0 - n1) < 1.5f * (float)lanes) return h < 1.f - ratio ? 0 : 1;
+    return ratio < tree_ratio ? 0 : 1;
+}
 
 // Dynamic-domain radius of a node that has not failed yet (the bytes 0x7f of a memset;
 // 3.4e38, so it never rejects a sample).

@@ -260,6 +260,7 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
     __syncthreads();
 
     const int L = R.L;
+    int cur_tree = -1;   // thread 0: the tree of this lane's previous iteration
     for (int it = 0;; ++it) {
         if (threadIdx.x == 0) {
             int st = *(volatile int *)P.state;
@@ -269,13 +270,10 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
                 st = kStDeadline;
             }
             s_misc[0] = st;
-            // tree choice: a share of the lanes proportional to the other tree's size
+            // tree choice by pRRTC's balance rule from the current tree sizes
             const int n0 = *(volatile int *)(P.size), n1 = *(volatile int *)(P.size + 1);
-            const float ratio = (float)n0 / (float)max(n0 + n1, 1);
-            // lanes hashed to [0, 1) (Fibonacci hashing) grow tree 0 below 1 - ratio, so the
-            // smaller tree gets the larger share of lanes whatever the lane count
-            const float h = (float)(((unsigned)lane_id * 2654435769u) >> 8) * (1.0f / 16777216.0f);
-            s_misc[1] = h < 1.f - ratio ? 0 : 1;
+            cur_tree = balance_tree(prm.balance, prm.tree_ratio, prm.lanes, n0, n1, lane_hash(lane_id), cur_tree);
+            s_misc[1] = cur_tree;
             s_misc[2] = min(n0, P.cap);
             s_misc[3] = min(n1, P.cap);
         }

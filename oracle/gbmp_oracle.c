@@ -786,6 +786,228 @@ int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *p
 }
 
 /* ------------------------------------------------------------------------------------
+ * Lane-parallel RRT-Connect in synchronous rounds.
+ *
+ * The device planner runs `lanes` extension lanes at once (one CUDA block each, as the
+ * reference's CPRRTC kernel runs one block per sampled motion, RobotSolver.cu:562-796,
+ * and pRRTC one block per new configuration, pRRTC.cu:340-601).  This restatement runs
+ * the same per-lane rule in rounds: in round `it` every lane
+ *   1. picks its tree by the balance rule from the tree sizes at the start of the round
+ *      (pRRTC.cu:348-371; see or_balance_tree),
+ *   2. draws its sample with Philox counter (lane << 32 | it), key seed,
+ *   3. extends from the nearest node of that tree (as the round began) by at most
+ *      `range`, checking the edge with the planner's step rule (state 0 skipped);
+ * the new nodes are appended in lane order; then every lane that extended
+ *   4. connects: finds the nearest node of the other tree (as it stands after the
+ *      round's extensions) and walks towards it in ceil(d / range) checked steps
+ *      (RobotSolver.cu:686-794, pRRTC.cu:478-551), keeping every checked step;
+ * the connection steps are appended in lane order.  Of the lanes that reach the other
+ * tree in a round, the one that needed the fewest steps wins (ties: lowest lane),
+ * standing for the device's first connection to finish.  Lanes within a round are
+ * independent, so they run in parallel (OpenMP); the commits keep lane order, so the
+ * result does not depend on the thread count.
+ * ---------------------------------------------------------------------------------- */
+
+/* Lane hash in [0, 1) (Fibonacci hashing of the lane index): the share of lanes below h
+ * stands for the reference's block index over the block count. */
+static float lane_hash(int32_t lane)
+{
+    return (float)(((uint32_t)lane * 2654435769u) >> 8) * (1.0f / 16777216.0f);
+}
+
+/* Tree grown by a lane (pRRTC.cu:348-371).  balance: 0 none (half the lanes each), 1
+ * proportional while the trees are within 1.5 x lanes nodes of each other and the
+ * smaller one (by tree_ratio) otherwise, 2 VAMP (swap trees while the size difference
+ * relative to the grown tree is below tree_ratio).  cur: the lane's tree in its previous
+ * round, -1 in its first. */
+int32_t or_balance_tree(int32_t balance, float tree_ratio, int32_t lanes, int32_t n0, int32_t n1, float h,
+                        int32_t cur)
+{
+    if (cur < 0 || balance == 0) return h < 0.5f ? 0 : 1;
+    if (balance == 2) {
+        int32_t nt = cur == 0 ? n0 : n1, no = cur == 0 ? n1 : n0;
+        float ratio = (float)abs(nt - no) / (float)(nt > 1 ? nt : 1);
+        return ratio < tree_ratio ? 1 - cur : cur;
+    }
+    float ratio = (float)n0 / (float)(n0 + n1 > 1 ? n0 + n1 : 1);
+    if ((float)abs(n0 - n1) < 1.5f * (float)lanes) return h < 1.f - ratio ? 0 : 1;
+    return ratio < tree_ratio ? 0 : 1;
+}
+
+typedef struct lane_out {
+    int32_t tr, nn, ext;          /* tree, nearest node, 1 if the extension is free */
+    int32_t tgt, n_ext, n_chain;  /* connect target, steps needed, steps kept       */
+    int32_t connected;
+    int32_t chain_cap;
+    float *qs;                    /* [J] new node                                   */
+    float *chain;                 /* [chain_cap * J] connection steps               */
+} lane_out;
+
+int32_t or_rrtc_lanes(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs, const float *thr,
+                      const float *start, const float *goal, const uint8_t *active, const float *lower,
+                      const float *upper, const float *defv, float range, float res, int32_t rule, uint64_t seed,
+                      int32_t lanes, int32_t balance, float tree_ratio, int32_t max_nodes, int32_t max_iters,
+                      float *path, int32_t path_cap, int32_t *path_len, float *cost, int32_t *iters,
+                      int32_t *tree_sizes, int32_t nthreads)
+{
+    const int J = r->L;
+    float *nodes[2];
+    int32_t *par[2], size[2] = {1, 1};
+    for (int t = 0; t < 2; ++t) {
+        nodes[t] = (float *)malloc(sizeof(float) * (size_t)max_nodes * J);
+        par[t] = (int32_t *)malloc(sizeof(int32_t) * (size_t)max_nodes);
+    }
+    memcpy(nodes[0], start, sizeof(float) * J);
+    memcpy(nodes[1], goal, sizeof(float) * J);
+    par[0][0] = 0; par[1][0] = 0;
+    lane_out *lo = (lane_out *)calloc((size_t)lanes, sizeof(lane_out));
+    int32_t *cur_tree = (int32_t *)malloc(sizeof(int32_t) * (size_t)lanes);
+    int32_t *ext_idx = (int32_t *)malloc(sizeof(int32_t) * (size_t)lanes);
+    for (int32_t l = 0; l < lanes; ++l) {
+        cur_tree[l] = -1;
+        lo[l].qs = (float *)malloc(sizeof(float) * J);
+        lo[l].chain_cap = 16;
+        lo[l].chain = (float *)malloc(sizeof(float) * 16 * J);
+    }
+    int nth = nthreads > 0 ? nthreads : or_num_threads();
+    int32_t solved = 0, ca = -1, cb = -1, tr_win = 0, it, full = 0;
+    for (it = 0; it < max_iters && !solved && !full; ++it) {
+        const int32_t n0 = size[0], n1 = size[1];
+        /* 1-3: extensions against the trees as the round began */
+        #pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+        for (int32_t l = 0; l < lanes; ++l) {
+            lane_out *o = &lo[l];
+            float P[16 * 64], C[3 * 257], dir[64], st[64], qn[64];
+            float *P_ = J <= 64 && r->S <= 256 ? P : (float *)malloc(sizeof(float) * 16 * J);
+            float *C_ = J <= 64 && r->S <= 256 ? C : (float *)malloc(sizeof(float) * 3 * (r->S + 1));
+            o->tr = or_balance_tree(balance, tree_ratio, lanes, n0, n1, lane_hash(l), cur_tree[l]);
+            cur_tree[l] = o->tr;
+            o->ext = 0;
+            o->connected = 0;
+            o->n_chain = 0;
+            const int32_t tr = o->tr, sz = tr == 0 ? n0 : n1;
+            const uint64_t ctr = ((uint64_t)(uint32_t)l << 32) | (uint32_t)it;
+            for (int j = 0; j < J; ++j) {
+                if (!active[j]) { o->qs[j] = defv[j]; continue; }
+                uint32_t c4[4] = {(uint32_t)ctr, (uint32_t)(ctr >> 32), (uint32_t)j, 0u};
+                philox(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
+                float u = (float)(c4[0] >> 8) * (1.0f / 16777216.0f);
+                o->qs[j] = fmaf(u, upper[j] - lower[j], lower[j]);
+            }
+            o->nn = tree_nearest(nodes[tr], sz, J, active, o->qs);
+            memcpy(qn, nodes[tr] + (int64_t)o->nn * J, sizeof(float) * J);
+            float d = active_dist(qn, o->qs, J, active);
+            if (d > range) {
+                float sc = range / d;
+                for (int j = 0; j < J; ++j) if (active[j]) o->qs[j] = fmaf(sc, o->qs[j] - qn[j], qn[j]);
+            }
+            o->ext = edge_free(r, e, np, pairs, thr, qn, o->qs, res, rule, P_, C_, dir, st);
+            if (P_ != P) free(P_);
+            if (C_ != C) free(C_);
+        }
+        for (int32_t l = 0; l < lanes; ++l) {
+            ext_idx[l] = -1;
+            if (!lo[l].ext) continue;
+            const int32_t tr = lo[l].tr;
+            if (size[tr] >= max_nodes) { full = 1; lo[l].ext = 0; continue; }
+            ext_idx[l] = size[tr]++;
+            memcpy(nodes[tr] + (int64_t)ext_idx[l] * J, lo[l].qs, sizeof(float) * J);
+            par[tr][ext_idx[l]] = lo[l].nn;
+        }
+        const int32_t s0 = size[0], s1 = size[1];
+        /* 4: connections against the trees after the round's extensions */
+        #pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+        for (int32_t l = 0; l < lanes; ++l) {
+            lane_out *o = &lo[l];
+            if (!o->ext) continue;
+            float P[16 * 64], C[3 * 257], dir[64], st[64], qa[64], qb[64], qc[64];
+            float *P_ = J <= 64 && r->S <= 256 ? P : (float *)malloc(sizeof(float) * 16 * J);
+            float *C_ = J <= 64 && r->S <= 256 ? C : (float *)malloc(sizeof(float) * 3 * (r->S + 1));
+            const int32_t ot = 1 - o->tr, szo = ot == 0 ? s0 : s1;
+            o->tgt = tree_nearest(nodes[ot], szo, J, active, o->qs);
+            memcpy(qb, nodes[ot] + (int64_t)o->tgt * J, sizeof(float) * J);
+            memcpy(qa, o->qs, sizeof(float) * J);
+            float dd = active_dist(o->qs, qb, J, active);
+            int32_t n_ext = (int32_t)ceilf(dd / range);
+            if (n_ext < 1) n_ext = 1;
+            o->n_ext = n_ext;
+            int ok = 1;
+            for (int32_t k = 1; k <= n_ext && ok; ++k) {
+                for (int j = 0; j < J; ++j)
+                    qc[j] = (k == n_ext) ? qb[j] : fmaf((qb[j] - o->qs[j]) / (float)n_ext, (float)k, o->qs[j]);
+                if (!edge_free(r, e, np, pairs, thr, qa, qc, res, rule, P_, C_, dir, st)) { ok = 0; break; }
+                if (k < n_ext) {
+                    if (o->n_chain == o->chain_cap) {
+                        o->chain_cap *= 2;
+                        o->chain = (float *)realloc(o->chain, sizeof(float) * (size_t)o->chain_cap * J);
+                    }
+                    memcpy(o->chain + (int64_t)o->n_chain * J, qc, sizeof(float) * J);
+                    ++o->n_chain;
+                    memcpy(qa, qc, sizeof(float) * J);
+                }
+            }
+            o->connected = ok;
+            if (P_ != P) free(P_);
+            if (C_ != C) free(C_);
+        }
+        int32_t win = -1;
+        for (int32_t l = 0; l < lanes; ++l) {
+            lane_out *o = &lo[l];
+            if (!o->ext) continue;
+            const int32_t tr = o->tr;
+            int32_t cur = ext_idx[l], kept = 1;
+            for (int32_t k = 0; k < o->n_chain; ++k) {
+                if (size[tr] >= max_nodes) { full = 1; kept = 0; break; }
+                int32_t nx = size[tr]++;
+                memcpy(nodes[tr] + (int64_t)nx * J, o->chain + (int64_t)k * J, sizeof(float) * J);
+                par[tr][nx] = cur;
+                cur = nx;
+            }
+            if (o->connected && kept && (win < 0 || o->n_ext < lo[win].n_ext)) {
+                win = l;
+                ca = cur;
+            }
+        }
+        if (win >= 0) {
+            solved = 1;
+            tr_win = lo[win].tr;
+            cb = lo[win].tgt;
+        }
+    }
+    *iters = it;
+    tree_sizes[0] = size[0];
+    tree_sizes[1] = size[1];
+    *path_len = 0;
+    *cost = 0.f;
+    if (solved) {
+        int32_t na = tr_win == 0 ? ca : cb, nb = tr_win == 0 ? cb : ca;
+        int32_t l0 = 0, l1 = 0;
+        for (int32_t i = na;; i = par[0][i]) { ++l0; if (par[0][i] == i) break; }
+        for (int32_t i = nb;; i = par[1][i]) { ++l1; if (par[1][i] == i) break; }
+        if (l0 + l1 <= path_cap) {
+            int32_t k = l0 - 1;
+            for (int32_t i = na;; i = par[0][i], --k) {
+                memcpy(path + (int64_t)k * J, nodes[0] + (int64_t)i * J, sizeof(float) * J);
+                if (par[0][i] == i) break;
+            }
+            k = l0;
+            for (int32_t i = nb;; i = par[1][i], ++k) {
+                memcpy(path + (int64_t)k * J, nodes[1] + (int64_t)i * J, sizeof(float) * J);
+                if (par[1][i] == i) break;
+            }
+            *path_len = l0 + l1;
+            double c = 0.0;
+            for (int32_t q = 1; q < l0 + l1; ++q) c += active_dist(path + (int64_t)(q - 1) * J, path + (int64_t)q * J, J, active);
+            *cost = (float)c;
+        }
+    }
+    for (int32_t l = 0; l < lanes; ++l) { free(lo[l].qs); free(lo[l].chain); }
+    free(lo); free(cur_tree); free(ext_idx);
+    for (int t = 0; t < 2; ++t) { free(nodes[t]); free(par[t]); }
+    return solved;
+}
+
+/* ------------------------------------------------------------------------------------
  * Constraint projection.
  * ---------------------------------------------------------------------------------- */
 

@@ -98,6 +98,18 @@ int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *p
                 const float *upper, const float *defv, float range, float res, int32_t rule, uint64_t seed,
                 int32_t max_nodes, int32_t max_iters, float *path, int32_t path_cap, int32_t *path_len,
                 float *cost, int32_t *iters, int32_t *tree_sizes);
+/* Tree a lane grows, pRRTC.cu:348-371 (balance 0 none, 1 proportional / smaller tree,
+ * 2 VAMP swap); h the lane's hash in [0, 1); cur its previous tree or -1. */
+int32_t or_balance_tree(int32_t balance, float tree_ratio, int32_t lanes, int32_t n0, int32_t n1, float h,
+                        int32_t cur);
+/* Lane-parallel RRT-Connect in synchronous rounds (the device planner's per-lane rule:
+ * RobotSolver.cu:562-796, pRRTC.cu:340-601).  Returns 1 when solved. */
+int32_t or_rrtc_lanes(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs, const float *thr,
+                      const float *start, const float *goal, const uint8_t *active, const float *lower,
+                      const float *upper, const float *defv, float range, float res, int32_t rule, uint64_t seed,
+                      int32_t lanes, int32_t balance, float tree_ratio, int32_t max_nodes, int32_t max_iters,
+                      float *path, int32_t path_cap, int32_t *path_len, float *cost, int32_t *iters,
+                      int32_t *tree_sizes, int32_t nthreads);
 
 int32_t or_num_threads(void);
 

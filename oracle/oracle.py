@@ -68,6 +68,13 @@ def lib():
                               C.c_float, C.c_float, C.c_int32, C.c_uint64, C.c_int32, C.c_int32, _f32p, C.c_int32,
                               C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32), _i32p]
         L.or_rrtc.restype = C.c_int32
+        L.or_rrtc_lanes.argtypes = [vp, vp, C.c_int32, _i32p, _f32p, _f32p, _f32p, _u8p, _f32p, _f32p, _f32p,
+                                    C.c_float, C.c_float, C.c_int32, C.c_uint64, C.c_int32, C.c_int32, C.c_float,
+                                    C.c_int32, C.c_int32, _f32p, C.c_int32, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_float), C.POINTER(C.c_int32), _i32p, C.c_int32]
+        L.or_rrtc_lanes.restype = C.c_int32
+        L.or_balance_tree.argtypes = [C.c_int32, C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int32]
+        L.or_balance_tree.restype = C.c_int32
         L.or_num_threads.restype = C.c_int32
         L.or_project.argtypes = [vp, _u8p, _f32p, _f32p, vp, _f32p, C.c_int64, vp, vp, C.c_int32]
         _lib = L
@@ -238,6 +245,28 @@ def rrtc(model, start, goal, range_=0.1, res=0.01, rule=STEP_LINF, seed=0, max_n
                        C.byref(it), sizes)
     return {"solved": int(ok), "path_len": pl.value, "cost": cost.value, "iterations": it.value,
             "tree_sizes": sizes.tolist()}, path[: pl.value].copy()
+
+
+def rrtc_lanes(model, start, goal, lanes=64, range_=0.1, res=0.01, rule=STEP_LINF, seed=0, balance=1,
+               tree_ratio=0.5, max_nodes=200000, max_iters=20000, path_cap=65536, nthreads=0):
+    """Lane-parallel RRT-Connect in synchronous rounds: the device planner's per-lane rule
+    (same Philox streams, balance rule, step rules), `lanes` lanes per round."""
+    rb = model.robot
+    path = np.zeros((path_cap, model.L), np.float32)
+    pl, it = C.c_int32(), C.c_int32()
+    cost = C.c_float()
+    sizes = np.zeros(2, np.int32)
+    ok = lib().or_rrtc_lanes(C.byref(model.r), C.byref(model.e), model.npairs, model.pairs, model.thr_sq,
+                             _c(start, np.float32), _c(goal, np.float32), _c(rb.active, np.uint8),
+                             _c(rb.lower, np.float32), _c(rb.upper, np.float32), _c(rb.default, np.float32),
+                             range_, res, rule, seed, lanes, balance, tree_ratio, max_nodes, max_iters, path,
+                             path_cap, C.byref(pl), C.byref(cost), C.byref(it), sizes, nthreads)
+    return {"solved": int(ok), "path_len": pl.value, "cost": cost.value, "iterations": it.value,
+            "tree_sizes": sizes.tolist()}, path[: pl.value].copy()
+
+
+def balance_tree(balance, tree_ratio, lanes, n0, n1, h, cur):
+    return lib().or_balance_tree(balance, tree_ratio, lanes, n0, n1, h, cur)
 
 
 def nearest(tree, queries, active=None, cand=None, nthreads=0):

@@ -222,3 +222,43 @@ def test_count_rule_steps():
         np.testing.assert_array_equal(st[-1], q[1])
         k = min(2, G - 1)
         np.testing.assert_allclose(st[k], q[0] + k * (q[1] - q[0]) / G, atol=1e-6)
+
+
+def test_balance_rule_follows_prrtc():
+    """The oracle's tree choice (pRRTC.cu:348-371): half the lanes per tree at a lane's
+    first iteration and with balancing off; strategy 1 proportional while the trees are
+    within 1.5 x lanes nodes, else the smaller tree by tree_ratio; strategy 2 swaps
+    while the relative size difference is below tree_ratio."""
+    assert O.balance_tree(1, 0.5, 64, 10, 500, 0.3, -1) == 0
+    assert O.balance_tree(1, 0.5, 64, 10, 500, 0.7, -1) == 1
+    assert O.balance_tree(0, 0.5, 64, 10, 500, 0.7, 0) == 1
+    # strategy 1, trees within 1.5 x 64 nodes: tree 0 below 1 - n0 / (n0 + n1) = 0.6
+    assert O.balance_tree(1, 0.5, 64, 40, 60, 0.59, 1) == 0
+    assert O.balance_tree(1, 0.5, 64, 40, 60, 0.61, 0) == 1
+    # strategy 1, far apart: every lane grows the smaller tree
+    assert O.balance_tree(1, 0.5, 64, 100, 900, 0.99, 1) == 0
+    assert O.balance_tree(1, 0.5, 64, 900, 100, 0.01, 0) == 1
+    # strategy 2: swap while |nt - no| / nt < tree_ratio
+    assert O.balance_tree(2, 1.0, 64, 100, 90, 0.2, 0) == 1
+    assert O.balance_tree(2, 0.05, 64, 100, 90, 0.2, 0) == 0
+    # a lane on the large tree swaps to the small one; a lane on the small tree stays
+    assert O.balance_tree(2, 1.0, 64, 1000, 10, 0.2, 0) == 1
+    assert O.balance_tree(2, 1.0, 64, 1000, 10, 0.2, 1) == 1
+
+
+def test_lane_parallel_rrtc_is_valid_and_thread_independent():
+    """The lane-parallel restatement returns collision-free paths from start to goal, and
+    the same result whatever the number of threads (commits keep lane order)."""
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    env = W.shelf_env(2)
+    m = O.OracleModel(robot, env)
+    _, _, fs = W.planning_workload(2, lambda q: m.check_states(q)[1] == 0, robot=robot, env=env)
+    s0, g0 = W.pick_problem(fs, lambda a, b: bool(m.check_motions(a[None], b[None], 0.01, 1)[0][0]), 2)
+    a = O.rrtc_lanes(m, s0, g0, lanes=16, seed=7, nthreads=1)
+    b = O.rrtc_lanes(m, s0, g0, lanes=16, seed=7, nthreads=4)
+    assert a[0]["solved"] and a[0] == b[0]
+    np.testing.assert_array_equal(a[1], b[1])
+    path = a[1]
+    np.testing.assert_array_equal(path[0], s0)
+    np.testing.assert_array_equal(path[-1], g0)
+    assert m.check_motions(path[:-1], path[1:], 0.01, 1)[0].all()
