@@ -269,6 +269,28 @@ typedef struct gbmp_projection {
 GBMP_API gbmp_status gbmp_project_states(gbmp_robot robot, const gbmp_projection *proj, float *d_q, int64_t n,
                                 float *d_task_cost, float *d_bound_cost, void *stream);
 
+/* Constrained motions, replacing SingleArmSpace::computeConstrainedMotions
+ * (SingleArmSpace.cu:1049-1366), which checkMotions (:636-639, :1466-1477) and
+ * getPathFromWaypoints (:1416-1419, :1479-1564) use when the space holds projectable
+ * constraints.  Motion k walks from d_from[k] towards d_to[k] ([n*L] each): every
+ * iteration moves all joints by `resolution` (<= 0: the robot's) along the unit direction
+ * to the goal, then runs two projection passes of `proj` (its `iterations` is ignored);
+ * the motion stops when the second pass's total error (task error norm + limit violation
+ * norm) exceeds 1e-3, when the state is farther from the goal than the previous one or
+ * moved more than 5 x resolution, or after max_iterations (the reference uses 10000);
+ * each state reached while still approaching is recorded, and coming within
+ * `resolution` of the goal achieves the motion.  d_ok[k] = 1 when the motion was
+ * achieved and every recorded state is collision-free with zero task-space and
+ * joint-limit cost (checkStates); d_cost[k] its length (L2 over all joints of the
+ * recorded states, 0 when not ok); d_num_states[k] the number of recorded states; with
+ * d_states [n * states_cap * L] non-NULL the first states_cap recorded states of each
+ * motion.  Outputs may be NULL.  One launch, asynchronous on `stream`. */
+GBMP_API gbmp_status gbmp_constrained_motions(gbmp_robot robot, gbmp_env env, const gbmp_projection *proj,
+                                              const float *d_from, const float *d_to, int64_t n, float resolution,
+                                              int32_t max_iterations, uint8_t *d_ok, float *d_cost,
+                                              int32_t *d_num_states, float *d_states, int32_t states_cap,
+                                              void *stream);
+
 /* ---- parallel RRT-Connect ----
  * Replaces CPRRTC::RobotSolver (cudampl/CPRRTC/include/RobotSolver.h:84-101,
  * cudampl/CPRRTC/src/RobotSolver.cu:348-473) and pRRTC::solve (pRRTC/src/planning/

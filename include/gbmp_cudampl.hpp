@@ -369,8 +369,16 @@ class SingleArmSpace {
         const int n = states1->getNumOfStates();
         if (n != states2->getNumOfStates()) throw std::runtime_error("Number of states in states1 and states2 are not equal");
         if (n == 0) throw std::runtime_error("No states to check");
-        // the reference switches to checkConstrainedMotions here (SingleArmSpace.cu:636-639)
-        if (projectable_) throw std::runtime_error("checkMotions with a projectable constraint is not supported");
+        // with projectable constraints the motions follow them (checkConstrainedMotions,
+        // SingleArmSpace.cu:636-639, :1466-1477)
+        if (projectable_) {
+            std::vector<uint8_t> h_ok;
+            constrainedMotions(states1->getJointStatesCuda(), states2->getJointStatesCuda(), n, h_ok, motion_costs,
+                               nullptr);
+            motion_feasibility.assign(n, false);
+            for (int i = 0; i < n; ++i) motion_feasibility[i] = h_ok[i] != 0;
+            return true;
+        }
         detail::DevArray ok((size_t)n), len(sizeof(float) * n);
         if (!ok.ok() || !len.ok()) {
             motion_feasibility.assign(n, false);
@@ -430,9 +438,37 @@ class SingleArmSpace {
     // Waypoints to a dense path at the space resolution (SingleArmSpace.cu:1411-1464,
     // interpolateVectors in util.cpp:205-248).
     BaseStatesPtr getPathFromWaypoints(const BaseStatesPtr &waypoints) {
-        // the reference switches to getConstrainedPathFromWaypoints here (SingleArmSpace.cu:1416-1419)
-        if (projectable_)
-            throw std::runtime_error("getPathFromWaypoints with a projectable constraint is not supported");
+        // with projectable constraints (getConstrainedPathFromWaypoints, SingleArmSpace.cu:1416-1419,
+        // :1479-1564): each segment as a constrained motion forwards and backwards (a
+        // constrained motion need not be feasible both ways); the forward motion's states
+        // if it is feasible, else the backward motion's in reverse, else none
+        if (projectable_) {
+            auto w = waypoints->getJointStatesFullHost();
+            if (w.size() < 2) return createStatesFromVectorFull(w);
+            const int m = 2 * (int)(w.size() - 1);
+            std::vector<float> from((size_t)m * L_), to((size_t)m * L_);
+            for (size_t i = 0; i + 1 < w.size(); ++i) {
+                std::copy(w[i].begin(), w[i].end(), from.begin() + (2 * i) * L_);
+                std::copy(w[i + 1].begin(), w[i + 1].end(), to.begin() + (2 * i) * L_);
+                std::copy(w[i + 1].begin(), w[i + 1].end(), from.begin() + (2 * i + 1) * L_);
+                std::copy(w[i].begin(), w[i].end(), to.begin() + (2 * i + 1) * L_);
+            }
+            detail::DevArray d_from(sizeof(float) * from.size()), d_to(sizeof(float) * to.size());
+            if (!d_from.ok() || !d_to.ok()) return nullptr;
+            cudaMemcpy(d_from.p, from.data(), sizeof(float) * from.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(d_to.p, to.data(), sizeof(float) * to.size(), cudaMemcpyHostToDevice);
+            std::vector<uint8_t> ok;
+            std::vector<float> cost;
+            std::vector<std::vector<std::vector<float>>> motions;
+            constrainedMotions(static_cast<float *>(d_from.p), static_cast<float *>(d_to.p), m, ok, cost, &motions);
+            std::vector<std::vector<float>> path;
+            for (int i = 0; i < m; i += 2) {
+                if (ok[i]) path.insert(path.end(), motions[i].begin(), motions[i].end());
+                else if (ok[i + 1]) path.insert(path.end(), motions[i + 1].rbegin(), motions[i + 1].rend());
+            }
+            if (path.empty()) return nullptr;
+            return createStatesFromVectorFull(path);
+        }
         auto w = waypoints->getJointStatesFullHost();
         std::vector<std::vector<float>> out;
         for (size_t i = 0; i + 1 < w.size(); ++i) {
@@ -458,6 +494,41 @@ class SingleArmSpace {
     int numSpheres() const { return S_; }
 
   private:
+    // Constrained motions d_from[k] -> d_to[k] (device, [n * L] each) on the space's
+    // projectable constraints (computeConstrainedMotions, SingleArmSpace.cu:1049-1366, at
+    // most 10000 iterations): feasibility, length and, when `motions` is given, the
+    // recorded states of every feasible motion.
+    void constrainedMotions(const float *d_from, const float *d_to, int n, std::vector<uint8_t> &ok,
+                            std::vector<float> &cost, std::vector<std::vector<std::vector<float>>> *motions) {
+        constexpr int kMaxIterations = 10000;
+        const int cap = motions ? kMaxIterations : 0;
+        detail::DevArray d_ok((size_t)n), d_cost(sizeof(float) * n), d_cnt(sizeof(int32_t) * n),
+            d_states(sizeof(float) * (size_t)n * cap * L_);
+        if (!d_ok.ok() || !d_cost.ok() || !d_cnt.ok() || !d_states.ok())
+            throw std::runtime_error("constrained motion buffers could not be allocated");
+        detail::check(gbmp_constrained_motions(robot_, env_, &proj_, d_from, d_to, n, resolution_, kMaxIterations,
+                                               static_cast<uint8_t *>(d_ok.p), static_cast<float *>(d_cost.p),
+                                               static_cast<int32_t *>(d_cnt.p),
+                                               cap ? static_cast<float *>(d_states.p) : nullptr, cap ? cap : 1,
+                                               nullptr));
+        ok.resize(n);
+        cost.resize(n);
+        std::vector<int32_t> cnt(n);
+        cudaMemcpy(ok.data(), d_ok.p, n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(cost.data(), d_cost.p, sizeof(float) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(cnt.data(), d_cnt.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+        if (!motions) return;
+        motions->assign(n, {});
+        for (int k = 0; k < n; ++k) {
+            if (!ok[k]) continue;
+            const int c = std::min(cnt[k], cap);
+            std::vector<float> flat((size_t)c * L_);
+            cudaMemcpy(flat.data(), static_cast<float *>(d_states.p) + (size_t)k * cap * L_, sizeof(float) * flat.size(),
+                       cudaMemcpyDeviceToHost);
+            for (int j = 0; j < c; ++j) (*motions)[k].emplace_back(flat.begin() + (size_t)j * L_, flat.begin() + (size_t)(j + 1) * L_);
+        }
+    }
+
     void build() {
         gbmp_robot_desc d{};
         d.num_links = L_;

@@ -115,6 +115,7 @@ SIGNATURES = {
     "gbmp_gather_states": [_i32, _vp, _i64, _vp, _i64, _vp, _vp, _vp],
     "gbmp_sample": [_vp, _u64, _u64, _i64, _vp, _vp],
     "gbmp_project_states": [_vp, C.c_void_p, _vp, _i64, _vp, _vp, _vp],
+    "gbmp_constrained_motions": [_vp, _vp, C.c_void_p, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _i32, _vp],
     "gbmp_planner_create": [_vp, _i32, _i32, C.POINTER(_vp)],
     "gbmp_planner_destroy": [_vp],
     "gbmp_rrtc_solve": [_vp, _vp, _vp, _vp, C.POINTER(RrtcSettings), _vp, _i32, C.POINTER(RrtcResult), _vp],

@@ -160,6 +160,29 @@ def project_states(robot: Robot, q, task_link: int = -1, offset=None, reference=
                                           stream_handle(stream)))
 
 
+def constrained_motions(robot: Robot, env: Env, q_from, q_to, task_link: int = -1, offset=None,
+                        reference=(0, 0, 0, 0, 0, 0), tolerance=(0, 0, 0, 0, 0, 0), use_boundary: bool = True,
+                        resolution: float = 0.0, max_iterations: int = 10000, ok=None, cost=None, num_states=None,
+                        states=None, stream=None):
+    """Constrained motions q_from[k] -> q_to[k] ([n, L] each) on the task-space region and
+    the joint limits (gbmp_constrained_motions): ok / cost / num_states [n]; states
+    [n, cap, L] receives the first cap recorded states of each motion."""
+    n = _n(q_from, robot.L)
+    assert q_to.shape == q_from.shape
+    p = _lib.Projection()
+    p.task_link = int(task_link)
+    off = np.eye(4, dtype=np.float32) if offset is None else np.asarray(offset, np.float32)
+    p.offset[:] = [float(v) for v in off.reshape(16)]
+    p.reference[:] = [float(v) for v in reference]
+    p.tolerance[:] = [float(v) for v in tolerance]
+    p.use_boundary = int(bool(use_boundary))
+    p.iterations = 2
+    cap = int(states.shape[1]) if states is not None else 0
+    check(_lib.load().gbmp_constrained_motions(robot.handle, env.handle, C.byref(p), ptr(q_from), ptr(q_to), n,
+                                               float(resolution), int(max_iterations), ptr(ok), ptr(cost),
+                                               ptr(num_states), ptr(states), cap, stream_handle(stream)))
+
+
 def nearest(robot: Robot, tree, queries, out, cand=None, stream=None):
     M = _n(tree, robot.L)
     Q = _n(queries, robot.L)

@@ -1154,3 +1154,119 @@ void or_project(const or_robot *r, const uint8_t *active, const float *lower, co
         if (bound_cost) bound_cost[s] = p->use_boundary ? pr_bound_cost(L, active, lower, upper, qs) : 0.f;
     }
 }
+
+/* ------------------------------------------------------------------------------------
+ * Constrained motions (SingleArmSpace::computeConstrainedMotions,
+ * cudampl/CUDAMPLib/src/spaces/SingleArmSpace.cu:1049-1366, with approachKernel
+ * :855-886, update_with_grad_and_flag :951-975, checkIfCostIsZero :1031-1045,
+ * checkValidOfApproaching :888-949, updateMotionStep :980-993 and checkAchieveGoal
+ * :998-1029).  Motion k walks from `from` towards `to`: every iteration moves all joints
+ * by `res` along the unit direction to the goal, then runs two projection passes (FK,
+ * task-space gradient and the joint-limit pull, added with step 1 to the active
+ * joints; each pass records the total error: the norm of the dead-banded task error
+ * plus the norm of the limit violations, at the state before its update).  The motion
+ * stops approaching when the second pass's error exceeds 1e-3, when the new state is
+ * farther from the goal than the previous one, or when it moved more than 5 res; each
+ * state reached while still approaching is recorded; reaching the goal within `res`
+ * ends it as achieved.  A motion is feasible when it achieved the goal and every
+ * recorded state passes checkStates (collision costs, task-space cost and limit cost
+ * all exactly 0; SingleArmSpace.cu:1295-1340); its cost is the L2 length over all
+ * joints of the recorded states.  states: [n * cap * L] or NULL; count[k] the number of
+ * recorded states (only the first cap are stored).
+ * ---------------------------------------------------------------------------------- */
+static float cm_task_error(const or_robot *r, const or_projection *p, const float *poses)
+{
+    float P[16], v[6], c = 0.f;
+    pr_task_frame(poses, p->task_link, p->offset, P, v);
+    float e[6];
+    e[0] = pr_dead(p->reference[3] - v[3], p->tolerance[3]);
+    e[1] = pr_dead(p->reference[4] - v[4], p->tolerance[4]);
+    e[2] = pr_dead(p->reference[5] - v[5], p->tolerance[5]);
+    e[3] = pr_dead(p->reference[0] - v[0], p->tolerance[0]);
+    e[4] = pr_dead(p->reference[1] - v[1], p->tolerance[1]);
+    e[5] = pr_dead(p->reference[2] - v[2], p->tolerance[2]);
+    (void)r;
+    for (int k = 0; k < 6; ++k) c += e[k] * e[k];
+    return sqrtf(c);
+}
+
+void or_constrained_motions(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs,
+                            const float *thr, const uint8_t *active, const float *lower, const float *upper,
+                            const or_projection *p, const float *from, const float *to, int64_t n, float res,
+                            int32_t max_iters, uint8_t *ok, float *cost, int32_t *count, float *states, int32_t cap,
+                            int32_t nthreads)
+{
+    const int L = r->L;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+    for (int64_t k = 0; k < n; ++k) {
+        const float *goal = to + k * L;
+        float q[64], prev[64], last[64], poses[64 * 16], gt[64], gb[64], C[3 * 257];
+        float *Cb = r->S <= 256 ? C : (float *)malloc(sizeof(float) * 3 * (r->S + 1));
+        memcpy(q, from + k * L, sizeof(float) * L);
+        int approaching = 1, achieved = 0, feasible = 1;
+        int32_t steps = 0;
+        double len = 0.0;
+        for (int32_t it = 0; it < max_iters && approaching; ++it) {
+            memcpy(prev, q, sizeof(float) * L);
+            float norm = 0.f;
+            for (int j = 0; j < L; ++j) { const float d = goal[j] - q[j]; norm += d * d; }
+            norm = sqrtf(norm);
+            if (norm > 1e-6f)
+                for (int j = 0; j < L; ++j) q[j] += (goal[j] - q[j]) / norm * res;
+            float err = 0.f;
+            for (int pass = 0; pass < 2; ++pass) {
+                or_fk_f32(r, q, 1, poses);
+                for (int j = 0; j < L; ++j) gt[j] = gb[j] = 0.f;
+                float et = 0.f, eb = 0.f;
+                if (p->task_link >= 0) {
+                    pr_task_grad(r, active, p, poses, gt);
+                    et = cm_task_error(r, p, poses);
+                }
+                if (p->use_boundary) {
+                    for (int j = 0; j < L; ++j) {
+                        if (!active[j]) continue;
+                        if (q[j] < lower[j]) { gb[j] = lower[j] - q[j]; eb += gb[j] * gb[j]; }
+                        else if (q[j] > upper[j]) { gb[j] = upper[j] - q[j]; eb += gb[j] * gb[j]; }
+                    }
+                    eb = sqrtf(eb);
+                }
+                err = et + eb;
+                for (int j = 0; j < L; ++j)
+                    if (active[j]) q[j] = q[j] + (gt[j] + gb[j]);
+            }
+            if (err > 1e-3f) { approaching = 0; break; }
+            float dpg = 0.f, dcg = 0.f, dpc = 0.f;
+            for (int j = 0; j < L; ++j) {
+                dpg += (prev[j] - goal[j]) * (prev[j] - goal[j]);
+                dcg += (q[j] - goal[j]) * (q[j] - goal[j]);
+                dpc += (prev[j] - q[j]) * (prev[j] - q[j]);
+            }
+            if (sqrtf(dcg) > sqrtf(dpg) || sqrtf(dpc) > res * 5.0f) { approaching = 0; break; }
+            /* a recorded state: checkStates on it */
+            if (states && steps < cap) memcpy(states + ((size_t)k * cap + steps) * L, q, sizeof(float) * L);
+            if (steps > 0) {
+                double s2 = 0.0;
+                for (int j = 0; j < L; ++j) s2 += (double)(q[j] - last[j]) * (q[j] - last[j]);
+                len += sqrt(s2);
+            }
+            memcpy(last, q, sizeof(float) * L);
+            ++steps;
+            if (feasible) {
+                or_fk_f32(r, q, 1, poses);
+                centers_one_f32(r, poses, Cb);
+                if (self_cost(Cb, np, pairs, thr) != 0.f || env_sphere_cost(r, e, Cb) != 0.f ||
+                    env_cuboid_cost(r, e, Cb) != 0.f || env_cylinder_cost(r, e, Cb) != 0.f)
+                    feasible = 0;
+                else if (p->task_link >= 0 && pr_task_cost(p, poses) != 0.f)
+                    feasible = 0;
+                else if (p->use_boundary && pr_bound_cost(L, active, lower, upper, q) != 0.f)
+                    feasible = 0;
+            }
+            if (sqrtf(dcg) < res) { achieved = 1; approaching = 0; }
+        }
+        ok[k] = (uint8_t)(achieved && feasible);
+        cost[k] = ok[k] ? (float)len : 0.f;
+        count[k] = steps;
+        if (Cb != C) free(Cb);
+    }
+}

@@ -133,6 +133,14 @@ void or_project(const or_robot *r, const uint8_t *active, const float *lower, co
                 const or_projection *p, float *q, int64_t n, float *task_cost, float *bound_cost,
                 int32_t nthreads);
 
+/* Constrained motions (SingleArmSpace.cu:1049-1366): ok[n], cost[n], count[n] recorded
+ * states, states [n * cap * L] or NULL. */
+void or_constrained_motions(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs,
+                            const float *thr, const uint8_t *active, const float *lower, const float *upper,
+                            const or_projection *p, const float *from, const float *to, int64_t n, float res,
+                            int32_t max_iters, uint8_t *ok, float *cost, int32_t *count, float *states, int32_t cap,
+                            int32_t nthreads);
+
 #ifdef __cplusplus
 }
 #endif

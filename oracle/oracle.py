@@ -77,6 +77,9 @@ def lib():
         L.or_balance_tree.restype = C.c_int32
         L.or_num_threads.restype = C.c_int32
         L.or_project.argtypes = [vp, _u8p, _f32p, _f32p, vp, _f32p, C.c_int64, vp, vp, C.c_int32]
+        L.or_constrained_motions.argtypes = [vp, vp, C.c_int32, _i32p, _f32p, _u8p, _f32p, _f32p, vp, _f32p, _f32p,
+                                             C.c_int64, C.c_float, C.c_int32, _u8p, _f32p, _i32p, vp, C.c_int32,
+                                             C.c_int32]
         _lib = L
     return _lib
 
@@ -216,6 +219,23 @@ class OracleModel:
         lib().or_project(C.byref(self.r), _c(rb.active, np.uint8), _c(rb.lower, np.float32), _c(rb.upper, np.float32),
                          C.byref(proj), q, n, tc.ctypes.data, bc.ctypes.data, nthreads)
         return q, tc, bc
+
+    def constrained_motions(self, q_from, q_to, proj: Projection, res, max_iters=10000, cap=0, nthreads=0):
+        """Constrained motions (computeConstrainedMotions): ok [n], cost [n], recorded
+        state counts [n] and, with cap > 0, the first cap recorded states [n, cap, L]."""
+        rb = self.robot
+        f = _c(np.asarray(q_from).reshape(-1, self.L), np.float32)
+        t = _c(np.asarray(q_to).reshape(-1, self.L), np.float32)
+        n = f.shape[0]
+        ok = np.zeros(n, np.uint8)
+        cost = np.zeros(n, np.float32)
+        cnt = np.zeros(n, np.int32)
+        st = np.zeros((n, max(cap, 1), self.L), np.float32)
+        lib().or_constrained_motions(C.byref(self.r), C.byref(self.e), self.npairs, self.pairs, self.thr_sq,
+                                     _c(rb.active, np.uint8), _c(rb.lower, np.float32), _c(rb.upper, np.float32),
+                                     C.byref(proj), f, t, n, res, max_iters, ok, cost, cnt,
+                                     st.ctypes.data if cap > 0 else None, cap, nthreads)
+        return ok.astype(bool), cost, cnt, (st if cap > 0 else None)
 
     def check_motions(self, q_from, q_to, res, rule=STEP_L2, early_exit=True, nthreads=0):
         f = _c(np.asarray(q_from).reshape(-1, self.L), np.float32)

@@ -232,6 +232,25 @@ int main(int argc, char **argv) {
         std::vector<float> gf;
         for (auto &row : gtask.getGoalStatesVector()) gf.insert(gf.end(), row.begin(), row.end());
         out.flat("region_goals", gf);
+        // constrained motions between region goals, and a path through three of them
+        // (checkConstrainedMotions / getConstrainedPathFromWaypoints)
+        const auto &gv = gtask.getGoalStatesVector();
+        const size_t nm = std::min<size_t>(16, gv.size() > 1 ? gv.size() - 1 : 0);
+        if (nm > 0) {
+            std::vector<std::vector<float>> a(gv.begin(), gv.begin() + nm), b(gv.begin() + 1, gv.begin() + nm + 1);
+            std::vector<bool> cm_ok;
+            std::vector<float> cm_cost;
+            region->checkMotions(region->createStatesFromVector(a), region->createStatesFromVector(b), cm_ok, cm_cost);
+            std::vector<int> oki(cm_ok.begin(), cm_ok.end());
+            out.flat("region_motion_ok", oki);
+            out.flat("region_motion_cost", cm_cost);
+            std::vector<std::vector<float>> wp(gv.begin(), gv.begin() + std::min<size_t>(3, gv.size()));
+            auto rp = region->getPathFromWaypoints(region->createStatesFromVector(wp));
+            std::vector<float> rf2;
+            if (rp)
+                for (auto &row : rp->getJointStatesHost()) rf2.insert(rf2.end(), row.begin(), row.end());
+            out.flat("region_path", rf2);
+        }
         std::printf("facade ok: %d states, %d edges, path of %zu waypoints, RRG path of %zu states (%s), %zu region "
                     "goals\n", n, m, path.size(), task->getSolution().size(), task->getFailureReason().c_str(),
                     gtask.getGoalStatesVector().size());

@@ -83,6 +83,8 @@ def _read_results(path):
 @pytest.mark.gpu
 def test_facade_matches_oracle(tmp_path):
     import oracle as O
+    import torch
+    from isaac_sim_ros2_humble_gb300 import api
     exe = build_facade_check(tmp_path)
     robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
     env = W.random_env(21, 64, 16, 4, oriented=True)
@@ -151,6 +153,29 @@ def test_facade_matches_oracle(tmp_path):
     assert np.abs(pos - np.asarray(region[1][:3])).max() < 0.05 + 2e-4
     assert np.all(full_g[:, act] >= robot.lower[act] - 1e-6) and np.all(full_g[:, act] <= robot.upper[act] + 1e-6)
     assert np.all(m.clearance(full_g) > -BAND)
+
+    # constrained motions between region goals: the facade's verdicts and lengths are the
+    # C-ABI's (same kernel); the path through three goals stays in the region and the
+    # limits, is collision-free and moves at most 5 x resolution a state within a motion
+    nm = len(got.get("region_motion_ok", []))
+    if nm:
+        full_a, full_b = full_g[:nm], full_g[1:nm + 1]
+        R, E = api.Robot(robot), api.Env(env)
+        region_kw = dict(task_link=region[0], reference=region[1], tolerance=region[2], use_boundary=True)
+        okc = torch.zeros(nm, dtype=torch.uint8, device="cuda")
+        costc = torch.zeros(nm, device="cuda")
+        api.constrained_motions(R, E, torch.from_numpy(full_a.copy()).cuda(), torch.from_numpy(full_b.copy()).cuda(),
+                                resolution=RES, ok=okc, cost=costc, **region_kw)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(got["region_motion_ok"].astype(bool), okc.cpu().numpy().astype(bool))
+        np.testing.assert_array_equal(got["region_motion_cost"].astype(np.float32), costc.cpu().numpy())
+        rp = got["region_path"].astype(np.float32).reshape(-1, robot.dim)
+        if len(rp):
+            full_p = robot.full_from_active(rp)
+            _, tc, bc = m.project(full_p, O.projection(iterations=0, **region_kw))
+            assert (tc == 0).all() and (bc == 0).all()
+            assert (m.check_states(full_p)[1] == 0).all()
+            assert np.linalg.norm(np.diff(full_p, axis=0), axis=1).max() <= 6 * RES * (1 + 1e-5)
 
 
 def _check_path(ms, robot, path, start, goal):
