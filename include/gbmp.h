@@ -111,6 +111,12 @@ GBMP_API gbmp_status gbmp_robot_self_pairs(gbmp_robot robot, int32_t *h_pairs, f
  * of `dim` values) build full vectors from these. */
 GBMP_API gbmp_status gbmp_robot_joints(gbmp_robot robot, uint8_t *h_active, float *h_default, float *h_lower,
                               float *h_upper);
+/* Device-side health of a robot handle: *status = GBMP_ERR_TIMEOUT when a kernel working
+ * for it gave up a bounded device-side wait (its results are then not valid; the kernels
+ * stage tables into shared memory with asynchronous bulk copies and wait for them with a
+ * limit), GBMP_OK otherwise.  Synchronous (reads one word).  No reference counterpart
+ * (the reference exits the process on a CUDA error, util.h:12-19). */
+GBMP_API gbmp_status gbmp_robot_device_status(gbmp_robot robot, int32_t *status);
 /* Select the kernel family used by later calls: 0 table-driven, 1 generated. */
 GBMP_API gbmp_status gbmp_robot_use_codegen(gbmp_robot robot, int32_t enable);
 /* The generated kernels of a robot created with GBMP_ROBOT_CODEGEN (the reference writes
@@ -167,12 +173,18 @@ GBMP_API gbmp_status gbmp_check_states_fk(gbmp_robot robot, gbmp_env env, const 
  * :467-522, feasibility SingleArmSpace.cu:603-626).  Edge k runs from d_from[k] to
  * d_to[k] ([E*L] each).  States are generated on the fly, never materialised.
  * Outputs (device, any may be NULL): d_ok[E] 1 = collision-free; d_first_hit[E] lowest
- * colliding state index or -1; d_length[E] L2 length (the reference's motion cost);
- * d_num_steps[E] interpolated state count.  step_rule GBMP_STEP_L2 is the reference
- * rule; GBMP_STEP_LINF bounds the per-joint step by `resolution` instead.
- * resolution <= 0 uses the robot's resolution.  Stream-synchronising (one 4-byte read).
- * Robots of up to 32 sphere-carrying links are validated by chunks of 8 consecutive
- * states a warp (4 for robots of more than 16 links), others state by state;
+ * colliding state index, -1 for a free edge, -2 for an edge of more than 4,194,304
+ * interpolated states, which is not validated (d_ok 0); d_length[E] L2 length (the
+ * reference's motion cost); d_num_steps[E] interpolated state count (4,194,305 for an edge
+ * that is too long).  step_rule GBMP_STEP_L2 is the reference rule; GBMP_STEP_LINF
+ * bounds the per-joint step by `resolution` instead.  resolution <= 0 uses the robot's
+ * resolution.  Asynchronous: three launches on `stream`, no host synchronisation (the
+ * reference reads step counts back to the host, SingleArmSpace.cu:728-739).  The working
+ * memory belongs to the robot handle: calls with one robot on different streams must be
+ * ordered by the caller.  Each edge is validated by one warp, state order, stopping at its
+ * first colliding state; the edges are taken longest first.  Robots of up to 32
+ * sphere-carrying links are validated by chunks of consecutive states (the first 4
+ * states, then 8 at a time; 4 for robots of more than 16 links), others state by state;
  * gbmp_robot_set_edge_form overrides the form for one robot handle. */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
@@ -192,7 +204,7 @@ GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const floa
 GBMP_API gbmp_status gbmp_robot_set_edge_form(gbmp_robot robot, int32_t form);
 
 /* gbmp_check_edges without any allocation: same arguments, kernels and results (both
- * entry points run one implementation), but its working memory is a fixed 5 MiB device
+ * entry points run one implementation), but its working memory is a fixed 4.5 MiB device
  * array inside the library (one per device) instead of a buffer grown with cudaMalloc.
  * No counterpart in the reference, whose checkMotions allocates and frees its state
  * buffers on every call.
@@ -201,8 +213,8 @@ GBMP_API gbmp_status gbmp_robot_set_edge_form(gbmp_robot robot, int32_t form);
  * device memory is fully reserved up front, or code that runs while memory is exhausted.
  * Limits: n_edges <= 65536 and n_edges * num_links <= 1,048,576; larger calls return
  * GBMP_ERR_CAPACITY with a message and do nothing (use gbmp_check_edges or split them).
- * The scratch's wave counters must start at zero: every call zeroes them on `stream`
- * before its first kernel; all other scratch is written before it is read.
+ * The scratch's counters must start at zero: every call zeroes them on `stream` before
+ * its first kernel; all other scratch is written before it is read.
  * Calls on one device share the scratch: calls whose work overlaps on the device (other
  * streams, other host threads) race and give wrong results; order them on one stream or
  * synchronise between them.  Different devices do not share it.
@@ -210,7 +222,7 @@ GBMP_API gbmp_status gbmp_robot_set_edge_form(gbmp_robot robot, int32_t form);
  * address with that device current; a caller that captures streams makes that first
  * call before it begins a capture.  The address belongs to the device's context and is
  * kept for the life of the process: do not call this entry point on a device after
- * cudaDeviceReset of that device.  Stream-synchronising like gbmp_check_edges. */
+ * cudaDeviceReset of that device.  Asynchronous like gbmp_check_edges. */
 GBMP_API gbmp_status gbmp_check_edges_noalloc(gbmp_robot robot, gbmp_env env, const float *d_from,
                                      const float *d_to, int64_t n_edges, float resolution,
                                      int32_t step_rule, uint8_t *d_ok, int32_t *d_first_hit,

@@ -99,6 +99,7 @@ SIGNATURES = {
     "gbmp_robot_self_pairs": [_vp, _vp, _vp, _i32],
     "gbmp_robot_joints": [_vp, _vp, _vp, _vp, _vp],
     "gbmp_robot_use_codegen": [_vp, _i32],
+    "gbmp_robot_device_status": [_vp, _i32p],
     "gbmp_robot_codegen_info": [_vp, C.c_char_p, _i64, C.POINTER(_i64), C.POINTER(_u64), C.POINTER(_i32),
                                 C.POINTER(C.c_double)],
     "gbmp_env_create": [_i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, C.POINTER(_vp)],

@@ -502,7 +502,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     const int kend = (need == 0u && !overflow) ? 0 : ks;   // nothing near any state: all free
     for (int k = 0; k < kend; ++k) {
         const int s = s0 + k;
-        if (k == 4) {   // once per chunk: stop if another warp found an earlier hit on this edge
+        if (k == 4 && first_hit) {   // once per chunk: stop if another warp found an earlier hit on this edge
             int known = 0;
             if (lane == 0) known = *(volatile const int *)first_hit;
             known = __shfl_sync(kFull, known, 0);
@@ -528,42 +528,54 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     return found;
 }
 
-// One wave of edge validation by chunks: states [b0, b1) of every live edge, K per task,
-// chunk-major order so that lower chunks of an edge are examined first.
+// Edge validation by chunks: a warp takes the next edge of `order` (a shared counter; the
+// edges come longest first, so the last edges taken are the shortest and the warps end
+// together), walks its states in chunks -- the first 4 states, then K at a time -- and
+// stops at the first colliding state.  One warp per edge, so no state past the edge's
+// first hit is placed in a later chunk.  Writes the edge's outputs (ok, first hit; -2 for
+// an edge too long to validate).
+constexpr int kFirstChunk = 4;
+
 template <int SPL, int K, bool CNT>
 __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
     k_edge_chunk(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
-                 const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
-                 const int *__restrict__ live, const int *__restrict__ live_count, int b0, int b1) {
+                 const int *__restrict__ nsteps, const float *__restrict__ dir, const int *__restrict__ order,
+                 long long n_edges, int *__restrict__ next, unsigned char *__restrict__ ok_out,
+                 int *__restrict__ first_hit_out) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
-    stage_tables(R, E, t, nwords);
+    if (!stage_tables(R, E, t, nwords)) return;
     const int warp = threadIdx.x / kWarp;
     WarpScratch w;
     ChunkScratch cs;
     carve_chunk(smem + smem_tables_bytes(R, nwords), R, K, warp, cs, w);
-    __syncthreads();
     const int lane = threadIdx.x & 31;
-    const long long count = *live_count;
-    const int nch = (b1 - b0 + K - 1) / K;
-    const long long tasks = count * (long long)nch;
-    const long long nw = (long long)gridDim.x * kChunkWarps;
-    for (long long task = blockIdx.x * (long long)kChunkWarps + warp; task < tasks; task += nw) {
-        const int c = (int)(task / count);
-        const int e = live[task % count];
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(next, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= n_edges) break;
+        const int e = order[i];
         const int n = nsteps[e];
-        const int s0 = b0 + c * K;
-        if (s0 >= n) continue;
-        const int s1 = min(min(s0 + K, b1), n);
-        int known = 0;
-        if (lane == 0) known = *(volatile int *)(first_hit + e);
-        known = __shfl_sync(kFull, known, 0);
-        if (known < s0) continue;
-        const long long off = (long long)e * R.L;
-        const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, s0, s1, n,
-                                              first_hit + e);
-        if (h >= 0 && lane == 0) atomicMin(first_hit + e, h);
+        int hit = -1;
+        if (n > kMaxEdgeStates) {
+            hit = -2;   // too long to validate
+        } else {
+            const long long off = (long long)e * R.L;
+            for (int s0 = 0; s0 < n;) {
+                const int s1 = min(s0 + (s0 == 0 ? kFirstChunk : K), n);
+                const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, s0,
+                                                           s1, n, nullptr);
+                __syncwarp();
+                if (h >= 0) { hit = h; break; }
+                s0 = s1;
+            }
+        }
+        if (lane == 0) {
+            if (ok_out) ok_out[e] = hit == -1;
+            if (first_hit_out) first_hit_out[e] = hit;
+        }
         __syncwarp();
     }
 }
@@ -623,14 +635,17 @@ gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, 
 
 gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int grid, size_t smem, cudaStream_t s,
                               const float *from, const float *to, const int *nsteps, const float *dir,
-                              int *first_hit, const int *live, const int *live_count, int b0, int b1) {
+                              const int *order, long long n_edges, int *next, unsigned char *ok, int *first_hit) {
+    // the grid is the resident blocks, at most one warp per edge
+    const long long need = (n_edges + kChunkWarps - 1) / kChunkWarps;
+    if (need < grid) grid = (int)need;
     GBMP_CHUNK_SWITCH(R.spl, K, {
         if (R.work)
-            k_edge_chunk<SPL, KK, true><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir,
-                                                                                first_hit, live, live_count, b0, b1);
+            k_edge_chunk<SPL, KK, true><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir, order,
+                                                                                n_edges, next, ok, first_hit);
         else
-            k_edge_chunk<SPL, KK, false><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir,
-                                                                                 first_hit, live, live_count, b0, b1);
+            k_edge_chunk<SPL, KK, false><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir, order,
+                                                                                 n_edges, next, ok, first_hit);
     });
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;

@@ -234,10 +234,9 @@ std::string codegen_source(const gbmp_robot_s *r) {
     // Edge set-up (KernelGenerator.h:408-465 step + direction), k_edge_setup with L fixed.
     s.line("extern \"C\" __global__ void __launch_bounds__(256) gbmp_gen_edge_setup(");
     s.line("    const float *__restrict__ from, const float *__restrict__ to, long long E, float res, int rule,");
-    s.line("    int *__restrict__ nsteps, float *__restrict__ dir, int *__restrict__ first_hit, int *__restrict__ live,");
-    s.line("    int *__restrict__ ctr, float *__restrict__ length_out, int *__restrict__ nsteps_out) {");
+    s.line("    int *__restrict__ nsteps, float *__restrict__ dir, int *__restrict__ hist,");
+    s.line("    float *__restrict__ length_out, int *__restrict__ nsteps_out) {");
     s.line("  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;");
-    s.line("  if (k == 0) ctr[1] = (int)E;");
     s.line("  if (k >= E) return;");
     s.line("  const float *f = from + k * GBMP_L, *t = to + k * GBMP_L;");
     s.line("  float d2 = 0.f, dinf = 0.f;");
@@ -249,14 +248,14 @@ std::string codegen_source(const gbmp_robot_s *r) {
     s.line("  }");
     s.line("  const float len = __fsqrt_rn(d2);");
     s.line("  const float metric = rule == %d ? dinf : len;", GBMP_STEP_LINF);
-    s.line("  const int n = (int)__fdiv_rn(metric, res) + 1;");
+    s.line("  const float ratio = __fdiv_rn(metric, res);");
+    s.line("  const int n = ratio < %d.0f ? (int)ratio + 1 : %d;", kMaxEdgeStates, kMaxEdgeStates + 1);
     s.line("  const float fn = (float)n;");
     s.line("#pragma unroll");
     s.line("  for (int j = 0; j < GBMP_L; ++j) dir[k * GBMP_L + j] = __fdiv_rn(__fadd_rn(t[j], -f[j]), fn);");
     s.line("  nsteps[k] = n;");
-    s.line("  first_hit[k] = %d;", INT_MAX);
-    s.line("  live[k] = (int)k;");
-    s.line("  atomicMax(ctr, n);");
+    s.line("  const int b = n >> 4;");
+    s.line("  atomicAdd(hist + (%d - (b < %d ? b : %d)), 1);", kEdgeBuckets - 1, kEdgeBuckets - 1, kEdgeBuckets - 1);
     s.line("  if (length_out) length_out[k] = len;");
     s.line("  if (nsteps_out) nsteps_out[k] = n;");
     s.line("}");
@@ -397,13 +396,13 @@ gbmp_status codegen_fk(const gbmp_robot_s *r, const float *q, long long n, float
 }
 
 gbmp_status codegen_edge_setup(const gbmp_robot_s *r, const float *from, const float *to, long long E, float res,
-                               int rule, int *nsteps, float *dir, int *first_hit, int *live, int *ctr,
-                               float *length_out, int *nsteps_out, cudaStream_t s) {
+                               int rule, int *nsteps, float *dir, int *hist, float *length_out, int *nsteps_out,
+                               cudaStream_t s) {
     const int tb = 256;
     const unsigned blocks = (unsigned)((E + tb - 1) / tb);
-    void *args[] = {(void *)&from,  (void *)&to,        (void *)&E,    (void *)&res,
-                    (void *)&rule,  (void *)&nsteps,    (void *)&dir,  (void *)&first_hit,
-                    (void *)&live,  (void *)&ctr,       (void *)&length_out, (void *)&nsteps_out};
+    void *args[] = {(void *)&from,  (void *)&to,   (void *)&E,    (void *)&res,
+                    (void *)&rule,  (void *)&nsteps, (void *)&dir, (void *)&hist,
+                    (void *)&length_out, (void *)&nsteps_out};
     ProfScope ps(GBMP_PROF_OTHER, s);
     GBMP_CUDA(cudaLaunchKernel((const void *)r->cg->edge_setup, dim3(blocks), dim3(tb), args, 0, s));
     return GBMP_OK;

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     extern __shared__ __align__(16) unsigned char smem[];
     DevEnv E{0, 0, 0, nullptr};
     SmemTables t = carve_tables(smem, R, 0);
-    stage_tables(R, E, t, 0);
+    if (!stage_tables(R, E, t, 0)) return;
     WarpScratch w = carve_warp(smem + smem_tables_bytes(R, 0), R, threadIdx.x / kWarp);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
-    stage_tables(R, E, t, nwords);
+    if (!stage_tables(R, E, t, nwords)) return;
     WarpScratch w = carve_warp(smem + smem_tables_bytes(R, nwords), R, threadIdx.x / kWarp);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -137,13 +137,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     }
 }
 
-// Edge set-up: step count, direction, L2 length (KernelGenerator.h:433-465); one thread per edge.
+// Edge set-up: step count, direction, L2 length (KernelGenerator.h:433-465); one thread per
+// edge.  Also counts the edges per length bucket (hist, longest bucket first) for the
+// longest-first processing order.  An edge of more than kMaxEdgeStates states gets
+// kMaxEdgeStates + 1 and is not validated.
 __global__ void k_edge_setup(const float *__restrict__ from, const float *__restrict__ to, long long E, int L,
                              float res, int rule, int *__restrict__ nsteps, float *__restrict__ dir,
-                             int *__restrict__ first_hit, int *__restrict__ live, int *__restrict__ ctr,
-                             float *__restrict__ length_out, int *__restrict__ nsteps_out) {
+                             int *__restrict__ hist, float *__restrict__ length_out, int *__restrict__ nsteps_out) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (k == 0) ctr[1] = (int)E;
     if (k >= E) return;
     const float *f = from + k * L, *t = to + k * L;
     float d2 = 0.f, dinf = 0.f;
@@ -157,88 +158,76 @@ __global__ void k_edge_setup(const float *__restrict__ from, const float *__rest
     // rule (pRRTC's granularity G = res): n = G + 1 states at k / G, dir = (to - from) / G
     const bool count = rule == GBMP_STEP_COUNT;
     const float metric = rule == GBMP_STEP_LINF ? dinf : len;
-    const int n = count ? (int)res + 1 : (int)__fdiv_rn(metric, res) + 1;
+    const float ratio = count ? res : __fdiv_rn(metric, res);
+    const int n = ratio < (float)kMaxEdgeStates ? (int)ratio + 1 : kMaxEdgeStates + 1;
     const float fn = count ? (float)(n - 1) : (float)n;
     for (int j = 0; j < L; ++j) dir[k * L + j] = __fdiv_rn(__fadd_rn(t[j], -f[j]), fn);
     nsteps[k] = n;
-    first_hit[k] = INT_MAX;
-    live[k] = (int)k;
-    atomicMax(ctr, n);
+    atomicAdd(hist + edge_bucket(n), 1);
     if (length_out) length_out[k] = len;
     if (nsteps_out) nsteps_out[k] = n;
 }
 
-// One wave of edge validation: states [b0, b1) of every live edge, one warp per state,
-// state-major order so that lower states of an edge are examined first and later ones
-// can skip once a hit is known.
+// Processing order of the edges, longest bucket first: order[slot] = edge, the slots of a
+// bucket following the counts of the longer buckets (hist) in arrival order (cursor).
+__global__ void k_edge_order(const int *__restrict__ nsteps, long long E, const int *__restrict__ hist,
+                             int *__restrict__ cursor, int *__restrict__ order) {
+    __shared__ int base[kEdgeBuckets];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < kEdgeBuckets; ++b) { base[b] = acc; acc += hist[b]; }
+    }
+    __syncthreads();
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < E; k += (long long)gridDim.x * blockDim.x) {
+        const int b = edge_bucket(nsteps[k]);
+        order[base[b] + atomicAdd(cursor + b, 1)] = (int)k;
+    }
+}
+
+// Edge validation state by state (robots with more than 32 sphere groups, and the
+// per-state form of the others): a warp takes the next edge of `order` (a shared
+// counter), walks its states in order and stops at the first colliding state.
 template <int SPL, bool CULL>
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, CULL ? 3 : 1)
-    k_edge_wave(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
-                const int *__restrict__ nsteps, const float *__restrict__ dir, int *__restrict__ first_hit,
-                const int *__restrict__ live, const int *__restrict__ live_count, int b0, int b1) {
+    k_edge_states(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
+                  const int *__restrict__ nsteps, const float *__restrict__ dir, const int *__restrict__ order,
+                  long long n_edges, int *__restrict__ next, unsigned char *__restrict__ ok_out,
+                  int *__restrict__ first_hit_out) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
-    stage_tables(R, E, t, nwords);
+    if (!stage_tables(R, E, t, nwords)) return;
     WarpScratch w = carve_warp(smem + smem_tables_bytes(R, nwords), R, threadIdx.x / kWarp);
-    __syncthreads();
     const int lane = threadIdx.x & 31;
-    const long long count = *live_count;
-    const long long tasks = count * (long long)(b1 - b0);
-    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
-    for (long long task = blockIdx.x * (long long)kWarpsPerBlock + threadIdx.x / kWarp; task < tasks;
-         task += nw) {
-        const int s = b0 + (int)(task / count);
-        const int e = live[task % count];
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(next, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= n_edges) break;
+        const int e = order[i];
         const int n = nsteps[e];
-        if (s >= n) continue;
-        // skip once a lower state of this edge is known to collide; the read is
-        // broadcast from lane 0 so that the whole warp takes the same branch
-        int known = 0;
-        if (lane == 0) known = *(volatile int *)(first_hit + e);
-        known = __shfl_sync(kFull, known, 0);
-        if (known < s) continue;
-        for (int j = lane; j < R.L; j += kWarp)
-            w.q[j] = (s == n - 1) ? to[(long long)e * R.L + j]
-                                  : __fmaf_rn(dir[(long long)e * R.L + j], (float)s, from[(long long)e * R.L + j]);
-        __syncwarp();
-        warp_fk(t, R.L, w, lane);
-        const bool hit = CULL ? warp_collide_culled<SPL>(t, R, E, w, lane)
-                              : warp_collide<SPL, false>(t, R, E, w, lane, nullptr);
-        if (hit && lane == 0) atomicMin(first_hit + e, s);
-        __syncwarp();
-    }
-}
-
-// Keep edges that have no hit yet and still have states at or beyond b1.
-__global__ void k_edge_compact(const int *__restrict__ live_in, const int *__restrict__ count_in,
-                               const int *__restrict__ first_hit, const int *__restrict__ nsteps, int b1,
-                               int *__restrict__ live_out, int *__restrict__ count_out) {
-    const int count = *count_in;
-    const int lane = threadIdx.x & 31;
-    for (long long base = blockIdx.x * (long long)blockDim.x; base < count; base += (long long)gridDim.x * blockDim.x) {
-        const long long i = base + threadIdx.x;
-        bool keep = false;
-        int e = 0;
-        if (i < count) {
-            e = live_in[i];
-            keep = first_hit[e] == INT_MAX && nsteps[e] > b1;
+        int hit = -1;
+        if (n > kMaxEdgeStates) {
+            hit = -2;   // too long to validate
+        } else {
+            const long long off = (long long)e * R.L;
+            for (int s = 0; s < n; ++s) {
+                for (int j = lane; j < R.L; j += kWarp)
+                    w.q[j] = (s == n - 1) ? to[off + j] : __fmaf_rn(dir[off + j], (float)s, from[off + j]);
+                __syncwarp();
+                warp_fk(t, R.L, w, lane);
+                const bool h = CULL ? warp_collide_culled<SPL>(t, R, E, w, lane)
+                                    : warp_collide<SPL, false>(t, R, E, w, lane, nullptr);
+                __syncwarp();
+                if (h) { hit = s; break; }
+            }
         }
-        const unsigned m = __ballot_sync(kFull, keep);
-        int slot = 0;
-        if (lane == 0 && m) slot = atomicAdd(count_out, __popc(m));
-        slot = __shfl_sync(kFull, slot, 0);
-        if (keep) live_out[slot + __popc(m & ((1u << lane) - 1u))] = e;
+        if (lane == 0) {
+            if (ok_out) ok_out[e] = hit == -1;
+            if (first_hit_out) first_hit_out[e] = hit;
+        }
+        __syncwarp();
     }
-}
-
-__global__ void k_edge_finish(long long E, const int *__restrict__ fh, unsigned char *__restrict__ ok,
-                              int *__restrict__ first_hit_out) {
-    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (k >= E) return;
-    const int h = fh[k];
-    if (ok) ok[k] = h == INT_MAX;
-    if (first_hit_out) first_hit_out[k] = h == INT_MAX ? -1 : h;
 }
 
 // ---------------------------------------------------------------------------------
@@ -270,25 +259,6 @@ static int current_device_sms(int *dev) {
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d) != cudaSuccess) return 0;
     *dev = d;
     return sms;
-}
-
-// Wave boundaries of edge validation: 4, 8, 16, 32 states, then 64 per wave.  Small
-// first waves retire the many edges that collide near their start before longer
-// edges are expanded further.
-static int wave_end(int b) {
-    if (b < 4) return 4;
-    if (b < 12) return 12;
-    if (b < 28) return 28;
-    if (b < 60) return 60;
-    return b + 64;
-}
-
-constexpr int kMaxWaves = 4096;
-
-static int max_edge_states() {
-    int b = 0;
-    for (int w = 0; w < kMaxWaves; ++w) b = wave_end(b);
-    return b;
 }
 
 // Host-side dispatch on spheres per lane (each instantiation gets its own register
@@ -413,7 +383,7 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     std::vector<unsigned char> blob;
     auto put = [&](const void *src, size_t bytes) {
         size_t off = align16(blob.size());
-        blob.resize(off + align16(bytes ? bytes : 1), 0);
+        blob.resize(off + align16(bytes), 0);
         if (bytes) memcpy(blob.data() + off, src, bytes);
         return off;
     };
@@ -478,14 +448,6 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
         lpair.back() = q + 1;
     }
     const int NPL = (int)lpair.size() / 4;
-    size_t o_jl = put(jl.data(), jl.size() * 4), o_axn = put(axn.data(), axn.size() * 4);
-    size_t o_axr = put(axr.data(), axr.size() * 4), o_sph = put(sph.data(), 4 * 4 * (size_t)S);
-    size_t o_type = put(r->type.data(), 4 * L), o_par = put(r->parent.data(), 4 * L);
-    size_t o_sl = put(r->slink.data(), 4 * (size_t)S);
-    size_t o_pairs = put(packed.data(), 4 * (size_t)r->P), o_thr = put(thr_sorted.data(), 4 * (size_t)r->P);
-    size_t o_lo = put(r->lower.data(), 4 * L), o_up = put(r->upper.data(), 4 * L);
-    size_t o_def = put(r->defv.data(), 4 * L), o_act = put(r->active.data(), L);
-    size_t o_grp = put(grp.data(), 4 * 4 * (size_t)G), o_glink = put(glink.data(), 4 * (size_t)G);
     std::vector<int> gso(G + 1, 0), gsl(S ? S : 1, 0);   // spheres of each group, index order
     for (int k = 0; k < S; ++k) gso[sgrp[k] + 1]++;
     for (int g = 0; g < G; ++g) gso[g + 1] += gso[g];
@@ -493,8 +455,22 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
         std::vector<int> fill(gso.begin(), gso.end() - 1);
         for (int k = 0; k < S; ++k) gsl[fill[sgrp[k]]++] = k;
     }
+    // The tables the kernels stage in shared memory come first, segment for segment in
+    // the order and 16-byte alignment of carve_tables, so that one bulk copy of
+    // smem_tables_bytes(R, 0) bytes stages them; the tables read from global memory follow.
+    size_t o_jl = put(jl.data(), jl.size() * 4), o_axn = put(axn.data(), axn.size() * 4);
+    size_t o_axr = put(axr.data(), axr.size() * 4), o_sph = put(sph.data(), 4 * 4 * (size_t)S);
+    size_t o_type = put(r->type.data(), 4 * L), o_par = put(r->parent.data(), 4 * L);
+    size_t o_sl = put(r->slink.data(), 4 * (size_t)S);
+    size_t o_grp = put(grp.data(), 4 * 4 * (size_t)G), o_glink = put(glink.data(), 4 * (size_t)G);
     size_t o_sgrp = put(sgrp.data(), 4 * (size_t)S), o_lpair = put(lpair.data(), 4 * lpair.size());
     size_t o_gso = put(gso.data(), 4 * (size_t)(G + 1)), o_gsl = put(gsl.data(), 4 * (size_t)S);
+    const size_t staged_bytes = align16(blob.size());
+    size_t o_pairs = put(packed.data(), 4 * (size_t)r->P), o_thr = put(thr_sorted.data(), 4 * (size_t)r->P);
+    size_t o_lo = put(r->lower.data(), 4 * L), o_up = put(r->upper.data(), 4 * L);
+    size_t o_def = put(r->defv.data(), 4 * L), o_act = put(r->active.data(), L);
+    const unsigned zero = 0;
+    size_t o_fault = put(&zero, sizeof zero);
 
     int dev = 0;
     r->num_sms = current_device_sms(&dev);
@@ -529,6 +505,15 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     D.grp = (const float *)(b + o_grp); D.glink = (const int *)(b + o_glink);
     D.sgrp = (const int *)(b + o_sgrp); D.lpair = (const int4 *)(b + o_lpair);
     D.gso = (const int *)(b + o_gso); D.gsl = (const int *)(b + o_gsl);
+    D.stage = b;
+    D.stage_bytes = (unsigned)staged_bytes;
+    D.fault = (unsigned *)(b + o_fault);
+    if (staged_bytes != smem_tables_bytes(D, 0)) {   // the layouts must agree byte for byte
+        set_error("internal: staged table block of %zu bytes, shared-memory layout of %zu", staged_bytes,
+                  smem_tables_bytes(D, 0));
+        gbmp_robot_destroy(r);
+        return GBMP_ERR_CUDA;
+    }
     if (flags & GBMP_ROBOT_CODEGEN) {
         gbmp_status st = codegen_build(r);
         if (st) {
@@ -576,6 +561,14 @@ gbmp_status gbmp_robot_joints(gbmp_robot r, uint8_t *h_active, float *h_default,
     if (h_default) memcpy(h_default, r->defv.data(), sizeof(float) * L);
     if (h_lower) memcpy(h_lower, r->lower.data(), sizeof(float) * L);
     if (h_upper) memcpy(h_upper, r->upper.data(), sizeof(float) * L);
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_robot_device_status(gbmp_robot r, int32_t *status) {
+    GBMP_CHECK_ARG(r && status, "robot/status is NULL");
+    unsigned f = 0;
+    GBMP_CUDA(cudaMemcpy(&f, r->dev.fault, sizeof f, cudaMemcpyDeviceToHost));
+    *status = f ? GBMP_ERR_TIMEOUT : GBMP_OK;
     return GBMP_OK;
 }
 
@@ -816,18 +809,24 @@ gbmp_status gbmp_robot_set_edge_form(gbmp_robot r, int32_t form) {
 // Both entry points run the same kernels; they differ only in where the working memory
 // comes from: gbmp_check_edges grows a buffer owned by the robot handle, and
 // gbmp_check_edges_noalloc uses one fixed array that the library holds on each device.
+// Three launches, no host round trip:
+//   k_edge_setup   step count, direction and length per edge, length histogram;
+//   k_edge_order   the edges in longest-first order (counting sort by buckets);
+//   validation     a warp takes the next edge of that order (shared counter), walks its
+//                  states in order (chunks of consecutive states, or state by state) and
+//                  stops at the first colliding state; it writes the edge's outputs.
 // Working memory of E edges of L links:
-//   nsteps[E], first_hit[E], liveA[E]   int    written by the set-up kernel
-//   liveB[E]                            int    written by k_edge_compact
-//   dir[E*L]                            float  written by the set-up kernel
-//   ctr[kMaxWaves + 2]                  int    MUST START AT ZERO (ctr[0] longest edge,
-//                                              ctr[1 + w] live edges entering wave w):
-//                                              zeroed on the stream by every call
+//   nsteps[E], order[E]   int
+//   dir[E*L]              float
+//   ctr[kEdgeCtrInts]     int    MUST START AT ZERO (hist[64], cursor[64], next):
+//                                zeroed on the stream by every call
 // ---------------------------------------------------------------------------------
 namespace gbmp {
 
+constexpr int kEdgeCtrInts = 2 * kEdgeBuckets + 32;
+
 struct EdgeScratch {
-    int *nsteps, *fh, *liveA, *liveB;
+    int *nsteps, *order;
     float *dir;
     int *ctr;
 };
@@ -848,34 +847,28 @@ static gbmp_status edge_args(gbmp_robot r, gbmp_env env, long long E, float *res
 static gbmp_status edge_validate(gbmp_robot r, gbmp_env env, const float *d_from, const float *d_to, long long E,
                                  float res, int rule, uint8_t *d_ok, int32_t *d_first_hit, float *d_length,
                                  int32_t *d_num_steps, cudaStream_t s, const EdgeScratch &sc) {
-    int *nsteps = sc.nsteps, *fh = sc.fh, *liveA = sc.liveA, *liveB = sc.liveB, *ctr = sc.ctr;
+    int *nsteps = sc.nsteps, *order = sc.order, *ctr = sc.ctr;
+    int *hist = ctr, *cursor = ctr + kEdgeBuckets, *next = ctr + 2 * kEdgeBuckets;
     float *dir = sc.dir;
     const int L = r->L;
-    GBMP_CUDA(cudaMemsetAsync(ctr, 0, (kMaxWaves + 2) * sizeof(int), s));
+    GBMP_CUDA(cudaMemsetAsync(ctr, 0, kEdgeCtrInts * sizeof(int), s));
     const int tb = 256;
     const unsigned blocks = (unsigned)((E + tb - 1) / tb);
     gbmp_status st = GBMP_OK;
     if (r->use_cg && rule != GBMP_STEP_COUNT) {   // the generated set-up knows the checkMotions rules
-        st = codegen_edge_setup(r, d_from, d_to, E, res, rule, nsteps, dir, fh, liveA, ctr, d_length, d_num_steps, s);
+        st = codegen_edge_setup(r, d_from, d_to, E, res, rule, nsteps, dir, hist, d_length, d_num_steps, s);
         if (st) return st;
     } else {
         ProfScope ps(GBMP_PROF_OTHER, s);
-        k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, fh, liveA, ctr, d_length,
-                                          d_num_steps);
+        k_edge_setup<<<blocks, tb, 0, s>>>(d_from, d_to, E, L, res, rule, nsteps, dir, hist, d_length, d_num_steps);
     }
     GBMP_CUDA(cudaGetLastError());
-    int n_max = 0;
-    GBMP_CUDA(cudaMemcpyAsync(&n_max, ctr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GBMP_CUDA(cudaStreamSynchronize(s));
     {
-        int b = 0, waves = 0;
-        while (b < n_max && waves <= kMaxWaves) { b = wave_end(b); ++waves; }
-        if (waves > kMaxWaves) {
-            set_error("an edge has %d interpolated states; at most %d are supported per call", n_max,
-                      max_edge_states());
-            return GBMP_ERR_CAPACITY;
-        }
+        ProfScope ps(GBMP_PROF_OTHER, s);
+        k_edge_order<<<(unsigned)std::min<long long>(blocks, 4LL * r->num_sms), tb, 0, s>>>(nsteps, E, hist, cursor,
+                                                                                            order);
     }
+    GBMP_CUDA(cudaGetLastError());
 
     const DevEnv Ev = env->dev();
     DevRobot D = r->dev;
@@ -894,47 +887,29 @@ static gbmp_status edge_validate(gbmp_robot r, gbmp_env env, const float *d_from
     }
     if (!K) {
         GBMP_SPL_SWITCH(r->dev.spl, {
-            st = cull ? persistent_grid(k_edge_wave<SPL, true>, smem, r->num_sms, &grid)
-                      : persistent_grid(k_edge_wave<SPL, false>, smem, r->num_sms, &grid);
+            st = cull ? persistent_grid(k_edge_states<SPL, true>, smem, r->num_sms, &grid)
+                      : persistent_grid(k_edge_states<SPL, false>, smem, r->num_sms, &grid);
         });
     }
     if (st) return st;
-    int b0 = 0, wave = 0;
-    int *live_in = liveA, *live_out = liveB;
-    while (b0 < n_max) {
-        const int b1 = wave_end(b0);
-        int *cnt_in = ctr + 1 + wave, *cnt_out = ctr + 2 + wave;
-        {
-            ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
-            if (K) {
-                st = edge_chunk_launch(D, Ev, K, grid, smem, s, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0,
-                                       b1);
-                if (st) return st;
-            } else {
-                GBMP_SPL_SWITCH(r->dev.spl, {
-                    if (cull)
-                        k_edge_wave<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                            D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
-                    else
-                        k_edge_wave<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
-                            D, Ev, d_from, d_to, nsteps, dir, fh, live_in, cnt_in, b0, b1);
-                });
-            }
-        }
-        GBMP_CUDA(cudaGetLastError());
-        if (b1 < n_max) {
-            ProfScope ps(GBMP_PROF_OTHER, s);
-            k_edge_compact<<<(unsigned)std::min<long long>(blocks, 4LL * r->num_sms), tb, 0, s>>>(
-                live_in, cnt_in, fh, nsteps, b1, live_out, cnt_out);
-            GBMP_CUDA(cudaGetLastError());
-        }
-        std::swap(live_in, live_out);
-        b0 = b1;
-        ++wave;
-    }
+    const long long need = (E + kWarpsPerBlock - 1) / kWarpsPerBlock;   // one warp per edge at most
+    if (need < grid) grid = (int)need;
     {
-        ProfScope ps(GBMP_PROF_OTHER, s);
-        k_edge_finish<<<blocks, tb, 0, s>>>(E, fh, d_ok, d_first_hit);
+        ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
+        if (K) {
+            st = edge_chunk_launch(D, Ev, K, grid, smem, s, d_from, d_to, nsteps, dir, order, E, next, d_ok,
+                                   d_first_hit);
+            if (st) return st;
+        } else {
+            GBMP_SPL_SWITCH(r->dev.spl, {
+                if (cull)
+                    k_edge_states<SPL, true><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                        D, Ev, d_from, d_to, nsteps, dir, order, E, next, d_ok, d_first_hit);
+                else
+                    k_edge_states<SPL, false><<<grid, kWarpsPerBlock * kWarp, smem, s>>>(
+                        D, Ev, d_from, d_to, nsteps, dir, order, E, next, d_ok, d_first_hit);
+            });
+        }
     }
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
@@ -945,20 +920,18 @@ static gbmp_status edge_validate(gbmp_robot r, gbmp_env env, const float *d_from
 // laid out as EdgeScratch for up to kNoAllocMaxEdges edges and kNoAllocMaxDirFloats
 // edges x links:
 //   [0, 4 Ei)            nsteps[E]
-//   [4 Ei, 8 Ei)         first_hit[E]
-//   [8 Ei, 12 Ei)        liveA[E]
-//   [12 Ei, 16 Ei)       liveB[E]
-//   [16 Ei, +4 D)        dir[E*L]
-//   [.., +4 (W+2))       ctr[W+2]   zeroed on the stream at the start of every call
-// with Ei = kNoAllocMaxEdges, D = kNoAllocMaxDirFloats, W = kMaxWaves.  Every call on a
+//   [4 Ei, 8 Ei)         order[E]
+//   [8 Ei, +4 D)         dir[E*L]
+//   [.., +4 C)           ctr[C]     zeroed on the stream at the start of every call
+// with Ei = kNoAllocMaxEdges, D = kNoAllocMaxDirFloats, C = kEdgeCtrInts.  Every call on a
 // device shares the array, so calls that overlap on the device race.
 // ---------------------------------------------------------------------------------
 constexpr long long kNoAllocMaxEdges = 65536;
 constexpr long long kNoAllocMaxDirFloats = 1LL << 20;   // n_edges * links
 constexpr size_t kNoAllocEdgeInts = sizeof(int) * kNoAllocMaxEdges;
-constexpr size_t kNoAllocDirOffset = 4 * kNoAllocEdgeInts;
+constexpr size_t kNoAllocDirOffset = 2 * kNoAllocEdgeInts;
 constexpr size_t kNoAllocCtrOffset = kNoAllocDirOffset + sizeof(float) * kNoAllocMaxDirFloats;
-constexpr size_t kNoAllocBytes = (kNoAllocCtrOffset + sizeof(int) * (kMaxWaves + 2) + 255) & ~size_t(255);
+constexpr size_t kNoAllocBytes = (kNoAllocCtrOffset + sizeof(int) * kEdgeCtrInts + 255) & ~size_t(255);
 static_assert(kNoAllocDirOffset % 256 == 0 && kNoAllocCtrOffset % 256 == 0, "scratch regions stay aligned");
 
 static __device__ __align__(256) unsigned char g_edge_scratch[kNoAllocBytes];
@@ -1004,14 +977,16 @@ gbmp_status gbmp_check_edges(gbmp_robot r, gbmp_env env, const float *d_from, co
     if (E == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
     cudaStream_t s = (cudaStream_t)stream;
+    // the working memory is the handle's: calls with the same robot are ordered on the host
+    // (the lock is held while the launches are queued, not while they run; calls on
+    // different streams with the same robot must be ordered by the caller)
     std::lock_guard<std::mutex> lock(r->scratch_mu);
     const size_t eb = align16(sizeof(int) * (size_t)E);
     const size_t db = align16(sizeof(float) * (size_t)E * r->L);
-    st = r->scratch.reserve(4 * eb + db + (kMaxWaves + 2) * sizeof(int));
+    st = r->scratch.reserve(2 * eb + db + kEdgeCtrInts * sizeof(int));
     if (st) return st;
     auto *base = static_cast<unsigned char *>(r->scratch.ptr);
-    EdgeScratch sc{(int *)base, (int *)(base + eb), (int *)(base + 2 * eb), (int *)(base + 3 * eb),
-                   (float *)(base + 4 * eb), (int *)(base + 4 * eb + db)};
+    EdgeScratch sc{(int *)base, (int *)(base + eb), (float *)(base + 2 * eb), (int *)(base + 2 * eb + db)};
     return edge_validate(r, env, d_from, d_to, E, res, rule, d_ok, d_first_hit, d_length, d_num_steps, s, sc);
 }
 
@@ -1031,8 +1006,7 @@ gbmp_status gbmp_check_edges_noalloc(gbmp_robot r, gbmp_env env, const float *d_
     if (st) return st;
     if (E == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_from && d_to, "from/to is NULL");
-    EdgeScratch sc{(int *)base, (int *)(base + kNoAllocEdgeInts), (int *)(base + 2 * kNoAllocEdgeInts),
-                   (int *)(base + 3 * kNoAllocEdgeInts), (float *)(base + kNoAllocDirOffset),
+    EdgeScratch sc{(int *)base, (int *)(base + kNoAllocEdgeInts), (float *)(base + kNoAllocDirOffset),
                    (int *)(base + kNoAllocCtrOffset)};
     return edge_validate(r, env, d_from, d_to, E, res, rule, d_ok, d_first_hit, d_length, d_num_steps,
                          (cudaStream_t)stream, sc);

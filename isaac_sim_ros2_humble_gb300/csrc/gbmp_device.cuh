@@ -64,6 +64,13 @@ struct DevRobot {
     // work[1] += states evaluated.  base_flops = per-state FK + sphere + group transforms.
     unsigned long long *work;
     long long base_flops;
+    // The staged tables (jl .. gsl above) as one block laid out exactly as carve_tables
+    // lays them out in shared memory: `stage_bytes` bytes at `stage` (16-byte aligned), so
+    // that one bulk copy stages them.  `fault`: device word a kernel sets (bit 0) when a
+    // bounded device-side wait gave up.
+    const void *stage;
+    unsigned stage_bytes;
+    unsigned *fault;
 };
 
 // Flop weights of the executed tests (multiply/add/compare = 1, FMA = 2).
@@ -72,6 +79,16 @@ constexpr int kFlCuboid = 33;     // 3x4 transform + clamp + squared distance + 
 constexpr int kFlCylinder = 34;   // 3x4 transform + finite-cylinder distance + compare
 constexpr int kFlSelf = 9;        // 3 sub, 1 mul + 2 FMA, compare
 constexpr int kFlGroupPair = 11;  // group-sphere overlap test
+
+// Edge validation: edges of more than kMaxEdgeStates interpolated states are not
+// validated (reported with first hit -2); edges are processed longest first by buckets of
+// 16 states (bucket 0 the longest).
+constexpr int kMaxEdgeStates = 1 << 22;
+constexpr int kEdgeBuckets = 64;
+__host__ __device__ inline int edge_bucket(int n) {
+    const int b = n >> 4;
+    return kEdgeBuckets - 1 - (b < kEdgeBuckets - 1 ? b : kEdgeBuckets - 1);
+}
 
 constexpr int kMaxGroups = 32;
 constexpr float kBroadMargin = 1e-3f;    // metres added to every group bounding radius
@@ -173,25 +190,67 @@ __device__ inline WarpScratch carve_warp(unsigned char *base, const DevRobot &R,
     return w;
 }
 
-// Block-cooperative copy of the robot tables and environment into shared memory.
-__device__ inline void stage_tables(const DevRobot &R, const DevEnv &E, const SmemTables &t, int nwords) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = tid; i < 12 * R.L; i += nt) t.jl[i] = R.jl[i];
-    for (int i = tid; i < 4 * R.L; i += nt) { t.axn[i] = R.axn[i]; t.axr[i] = R.axr[i]; }
-    for (int i = tid; i < R.S; i += nt) {
-        t.sph[i] = reinterpret_cast<const float4 *>(R.sph)[i];
-        t.slink[i] = R.slink[i];
-        t.sgrp[i] = R.sgrp[i];
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Polls of a staging wait before it gives up (each poll sleeps ~0.1 us after the first
+// few): far beyond the microseconds a copy of at most 227 KB takes.
+constexpr int kStageWaitPolls = 1 << 24;
+
+// Stages the robot tables and the environment into shared memory with two bulk
+// asynchronous copies (TMA, cp.async.bulk: the robot's staged block and the environment
+// words, both 16-byte aligned with sizes that are multiples of 16) completing on one
+// mbarrier.  All threads of the block call it; it begins and ends with a block barrier,
+// so a block may stage again later (the batched planner does, per problem).  Every
+// thread waits on the mbarrier (bounded); if the copies have not completed within the
+// limit the robot's fault word is set and false is returned on every thread, and the
+// caller must not use the tables.
+__device__ inline bool stage_tables(const DevRobot &R, const DevEnv &E, const SmemTables &t, int nwords) {
+    __shared__ __align__(8) unsigned long long s_mbar;
+    __shared__ int s_fail;
+    const unsigned bar = smem_u32(&s_mbar);
+    const unsigned bytes_r = R.stage_bytes, bytes_e = 16u * (unsigned)nwords;
+    __syncthreads();   // no thread still reads tables this block staged before
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // order earlier generic-proxy accesses of this shared memory before the copies
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        unsigned long long state;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                     : "=l"(state)
+                     : "r"(bar), "r"(bytes_r + bytes_e)
+                     : "memory");
+        (void)state;
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(t.jl)),
+                     "l"(R.stage), "r"(bytes_r), "r"(bar)
+                     : "memory");
+        if (bytes_e)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                             smem_u32(t.env)),
+                         "l"(E.words), "r"(bytes_e), "r"(bar)
+                         : "memory");
     }
-    for (int i = tid; i < R.L; i += nt) { t.type[i] = R.type[i]; t.parent[i] = R.parent[i]; }
-    for (int i = tid; i < R.G; i += nt) {
-        t.grp[i] = reinterpret_cast<const float4 *>(R.grp)[i];
-        t.glink[i] = R.glink[i];
+    __syncthreads();   // the mbarrier is initialised before anyone polls it
+    unsigned done = 0;
+    for (int it = 0; it < kStageWaitPolls; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+        if (done) break;
+        if (it > 8) __nanosleep(100);
     }
-    for (int i = tid; i < R.NPL; i += nt) t.lpair[i] = R.lpair[i];
-    for (int i = tid; i <= R.G; i += nt) t.gso[i] = R.gso[i];
-    for (int i = tid; i < R.S; i += nt) t.gsl[i] = R.gsl[i];
-    for (int i = tid; i < nwords; i += nt) t.env[i] = E.words[i];
+    if (!done) s_fail = 1;
+    __syncthreads();
+    const bool ok = s_fail == 0;
+    if (threadIdx.x == 0) {
+        if (ok) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+        else if (R.fault) atomicOr(R.fault, 1u);
+    }
+    return ok;
 }
 
 // ---------------------------------------------------------------------------------

@@ -134,8 +134,8 @@ void codegen_free(Codegen *cg);
 gbmp_status codegen_fk(const gbmp_robot_s *r, const float *q, long long n, float *poses, float *centers,
                        cudaStream_t s);
 gbmp_status codegen_edge_setup(const gbmp_robot_s *r, const float *from, const float *to, long long E, float res,
-                               int rule, int *nsteps, float *dir, int *first_hit, int *live, int *ctr,
-                               float *length_out, int *nsteps_out, cudaStream_t s);
+                               int rule, int *nsteps, float *dir, int *hist, float *length_out, int *nsteps_out,
+                               cudaStream_t s);
 // Edge validation by chunks of consecutive states (gbmp_chunk.cu).  K = states per
 // chunk for this robot (0: use the per-state kernels); `form` is the robot handle's
 // edge_form (0 automatic, 1 per state, 4 or 8 states per chunk).
@@ -143,7 +143,7 @@ int edge_chunk_states(const DevRobot &R, int form);
 gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid);
 gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int grid, size_t smem, cudaStream_t s,
                               const float *from, const float *to, const int *nsteps, const float *dir,
-                              int *first_hit, const int *live, const int *live_count, int b0, int b1);
+                              const int *order, long long n_edges, int *next, unsigned char *ok, int *first_hit);
 }  // namespace gbmp
 
 struct gbmp_env_s {

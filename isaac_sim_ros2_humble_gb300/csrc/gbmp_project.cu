@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     extern __shared__ __align__(16) unsigned char smem[];
     DevEnv E0{0, 0, 0, nullptr};
     SmemTables t = carve_tables(smem, R, 0);
-    stage_tables(R, E0, t, 0);
+    if (!stage_tables(R, E0, t, 0)) return;
     const int warp = threadIdx.x / kWarp, lane = threadIdx.x & 31;
     unsigned char *wbase = smem + smem_tables_bytes(R, 0);
     WarpScratch w = carve_warp(wbase, R, warp);
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
-    stage_tables(R, E, t, nwords);
+    if (!stage_tables(R, E, t, nwords)) return;
     const int warp = threadIdx.x / kWarp, lane = threadIdx.x & 31;
     unsigned char *wbase = smem + smem_tables_bytes(R, nwords);
     WarpScratch w = carve_warp(wbase, R, warp);

@@ -243,7 +243,7 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwords = env_words(E.ns, E.nb, E.nc);
     SmemTables t = carve_tables(smem, R, nwords);
-    stage_tables(R, E, t, nwords);
+    if (!stage_tables(R, E, t, nwords)) return;
     unsigned char *p = smem + smem_tables_bytes(R, nwords);
     WarpScratch w = carve_warp(p, R, threadIdx.x / kWarp);
     p += smem_warp_bytes(R) * kRrtcWarps;

@@ -354,3 +354,33 @@ def test_edge_forms_agree_on_every_edge_of_the_benchmark_call():
             np.testing.assert_array_equal(a, b)
     with pytest.raises(_lib.GbmpError):
         R.set_edge_form(3)
+
+
+def test_device_status_is_clean_after_every_kernel_family(plain, edge):
+    """Every kernel stages its tables with bulk asynchronous copies and a bounded wait;
+    none of the launches above gave up that wait (gbmp_robot_device_status)."""
+    import ctypes as C
+    lib = _lib.load()
+    for R in (plain[4], edge[5]):
+        st = C.c_int32(-1)
+        _lib.check(lib.gbmp_robot_device_status(R.handle, C.byref(st)))
+        assert st.value == _lib.OK
+
+
+def test_edges_too_long_to_validate_are_reported_not_checked(edge):
+    """An edge of more than 4,194,304 interpolated states is not validated: first hit -2,
+    not free, its state count reported; the other edges of the call are validated as
+    usual."""
+    robot, env, qf, qt, m, R, E = edge
+    j = int(np.nonzero(robot.active)[0][-1])
+    res = float((robot.upper[j] - robot.lower[j]) / 5.0e6)
+    f = qf[:3].copy()
+    t = f.copy()
+    t[0, j] = f[0, j] + 20.5 * res          # 21 states
+    f[2, j], t[2, j] = robot.lower[j], robot.upper[j]   # a joint across its range: 5e6 states
+    ok, fh, ln, ns = _run_edges(R, E, f, t, res, 1)
+    assert fh[2] == -2 and not ok[2] and ns[2] == 4194305
+    o_ok, o_fh, o_ns, _ = m.check_motions(f[:2], t[:2], res, 1, early_exit=True)
+    np.testing.assert_array_equal(ns[:2], o_ns)
+    np.testing.assert_array_equal(fh[:2], o_fh)
+    assert ns[1] == 1
