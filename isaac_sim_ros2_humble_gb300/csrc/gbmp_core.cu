@@ -33,7 +33,13 @@ gbmp_status ensure_smem_optin(const void *fn) {
     int dev = 0;
     GBMP_CUDA(cudaGetDevice(&dev));
     if (g_smem_optin.contains(dev, fn)) return GBMP_OK;
-    GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    // the dynamic limit is what the device allows a block minus the kernel's static shared
+    // memory (the staging mbarrier and flags)
+    cudaFuncAttributes fa;
+    GBMP_CUDA(cudaFuncGetAttributes(&fa, fn));
+    int optin = 0;
+    GBMP_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
     GBMP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
     g_smem_optin.insert(dev, fn);
     return GBMP_OK;

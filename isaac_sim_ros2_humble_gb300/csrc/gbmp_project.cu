@@ -405,7 +405,8 @@ extern "C" gbmp_status gbmp_project_states(gbmp_robot r, const gbmp_projection *
         p.tolerance[k] = proj->tolerance[k];
     }
     const size_t smem = smem_tables_bytes(r->dev, 0) + (smem_warp_bytes(r->dev) + proj_warp_bytes(r->dev)) * kWarpsPerBlock;
-    GBMP_CUDA(cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    gbmp_status so = ensure_smem_optin((const void *)k_project);
+    if (so) return so;
     int per_sm = 0;
     GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project, kWarpsPerBlock * kWarp, smem));
     if (per_sm < 1) {

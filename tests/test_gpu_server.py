@@ -118,3 +118,65 @@ def test_wait_timeout_keeps_ticket(resident):
     assert info is not None and info["status"] == 0
     assert first is None or first["status"] == 0
     srv.close()
+
+
+def test_plans_alone_and_in_the_mix_agree_statistically():
+    """Plan requests are solved by parallel lanes, so a result is not reproducible to the
+    bit; the same 30 shelf problems served one at a time and served inside a stream of
+    check requests must agree statistically: success counts within a two-proportion
+    |z| < 3, path lengths with a two-sided Mann-Whitney p > 0.01 and a median per-problem
+    ratio within [0.85, 1.15].  Every solved path starts and ends at its problem's start
+    and goal."""
+    scipy_stats = pytest.importorskip("scipy.stats")
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7", resolution=0.01)
+    shelves = [W.shelf_env(k) for k in range(3)]
+    R = api.Robot(robot)
+    E = [api.Env(e) for e in shelves]
+    probs = []
+    for seed in range(30):
+        m = O.OracleModel(robot, shelves[seed % 3])
+        _, _, fs = W.planning_workload(seed, lambda q, m=m: m.check_states(q)[1] == 0, robot=robot,
+                                       env=shelves[seed % 3])
+        s0, g0 = W.pick_problem(fs, lambda a, b, m=m: bool(m.check_motions(a[None], b[None], 0.01, 1)[0][0]),
+                                seed)
+        probs.append((seed % 3, s0, g0, 100 + seed))
+
+    def serve(mix):
+        srv = api.Server(num_streams=4, hbm_budget_bytes=1 << 30, max_batch_states=1 << 20, plan_workers=1,
+                         plan_batch=8, plan_lanes=64, planner_max_nodes=65536, plan_path_cap=4096)
+        srv.add_robot(R)
+        for e in E:
+            srv.add_env(e)
+        srv.start()
+        rng = np.random.default_rng(9)
+        out, keep = [], []
+        for k, s0, g0, seed in probs:
+            path = np.zeros((4096, robot.num_links), np.float32)
+            t = srv.submit_plan(0, k, s0, g0, seed, path)
+            if mix:   # check traffic around every plan
+                for _ in range(10):
+                    q = robot.sample_full(rng, int(rng.integers(1, 20000)))
+                    v = np.zeros(q.shape[0], np.uint8)
+                    keep.append((q, v, srv.submit_check(0, int(rng.integers(3)), q, v)))
+            info = srv.wait(t, 60.0)
+            assert info is not None
+            if info["solved"]:
+                np.testing.assert_array_equal(path[0], s0)
+                np.testing.assert_array_equal(path[info["path_len"] - 1], g0)
+            out.append((bool(info["solved"]), float(info["cost"])))
+        for q, v, t in keep:
+            assert srv.wait(t, 60.0)["status"] == 0
+        srv.close()
+        return out
+
+    a, b = serve(False), serve(True)
+    sa, sb = np.array([s for s, _ in a]), np.array([s for s, _ in b])
+    p = (sa.sum() + sb.sum()) / (2 * len(sa))
+    z = 0.0 if p in (0.0, 1.0) else (sa.mean() - sb.mean()) / np.sqrt(p * (1 - p) * 2 / len(sa))
+    assert abs(z) < 3.0
+    ca = np.array([c for s, c in a if s])
+    cb = np.array([c for s, c in b if s])
+    assert scipy_stats.mannwhitneyu(ca, cb, alternative="two-sided").pvalue > 0.01
+    both = sa & sb
+    ratio = np.median(np.array([c for _, c in a])[both] / np.array([c for _, c in b])[both])
+    assert 0.85 <= ratio <= 1.15, ratio
