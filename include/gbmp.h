@@ -328,14 +328,17 @@ typedef struct gbmp_rrtc_settings {
     float dd_alpha;
     float dd_radius;
     float dd_min_radius;
-    /* pRRTC's tree balancing (pRRTC/src/planning/pRRTC.cu:348-371, pRRTC_settings.hh:10-11),
-     * the tree each lane grows per iteration: GBMP_BALANCE_DEFAULT (0) and GBMP_BALANCE_SIZE
-     * pRRTC strategy 1: lanes split in proportion to the other tree's share while the
-     * trees differ by less than 1.5 x lanes nodes, else every lane grows tree 0 when its
-     * share of the nodes is below tree_ratio and tree 1 otherwise; GBMP_BALANCE_SWAP
-     * strategy 2: a lane keeps its tree and swaps while the size difference relative to
-     * its tree is below tree_ratio; GBMP_BALANCE_NONE (pRRTC's 0): half the lanes per tree.
-     * tree_ratio <= 0 takes pRRTC's default for the strategy (0.5, or 1.0 for strategy 2). */
+    /* Tree balancing, the tree each lane grows per iteration (pRRTC/src/planning/
+     * pRRTC.cu:348-371, pRRTC_settings.hh:10-11).  GBMP_BALANCE_DEFAULT (0): lanes split in
+     * proportion to the other tree's share of the nodes, at every size.  GBMP_BALANCE_SIZE:
+     * pRRTC strategy 1, the same while the trees differ by less than 1.5 x lanes nodes,
+     * else every lane grows tree 0 when its share is below tree_ratio and tree 1 otherwise
+     * (so a tree trapped in a pocket of free space takes every lane and an unsolvable
+     * problem runs to its iteration cap or deadline rather than its node cap).
+     * GBMP_BALANCE_SWAP: pRRTC strategy 2, a lane keeps its tree and swaps while the size
+     * difference relative to its tree is below tree_ratio.  GBMP_BALANCE_NONE (pRRTC's
+     * 0): half the lanes per tree.  tree_ratio <= 0 takes pRRTC's default for the
+     * strategy (0.5, or 1.0 for strategy 2). */
     int32_t balance;
     float tree_ratio;
 } gbmp_rrtc_settings;

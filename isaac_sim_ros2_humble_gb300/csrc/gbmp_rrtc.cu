@@ -154,11 +154,11 @@ static bool plan_step(const gbmp_rrtc_settings *s, float robot_res, float *res) 
     return *res > 0.f;
 }
 
-// Balance strategy of a solve in the device encoding (0 none, 1 size, 2 swap) and its
+// Balance strategy of a solve in the device encoding (0 none, 1 size, 2 swap, 3 proportional) and its
 // tree ratio; false on an unknown strategy or a non-finite ratio.
 static bool plan_balance(const gbmp_rrtc_settings *s, int *balance, float *ratio) {
     switch (s->balance) {
-    case GBMP_BALANCE_DEFAULT:
+    case GBMP_BALANCE_DEFAULT: *balance = 3; break;
     case GBMP_BALANCE_SIZE: *balance = 1; break;
     case GBMP_BALANCE_SWAP: *balance = 2; break;
     case GBMP_BALANCE_NONE: *balance = 0; break;

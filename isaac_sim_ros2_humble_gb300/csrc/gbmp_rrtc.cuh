@@ -35,7 +35,7 @@ struct RrtcParams {
     const unsigned long long *deadline_ptr;   // read from device memory when non-null
     int dd = 0;                       // dynamic domain on (needs RrtcDev::radii)
     float dd_alpha = 0.f, dd_radius = 0.f, dd_min = 0.f;
-    int balance = 1;                  // pRRTC balance strategy: 0 none, 1 size, 2 swap
+    int balance = 3;                  // 0 none, 1 pRRTC size, 2 pRRTC swap, 3 proportional
     float tree_ratio = 0.5f;
 };
 
@@ -48,13 +48,17 @@ __host__ __device__ inline float lane_hash(int lane) {
 
 // Tree a lane grows (pRRTC.cu:348-371).  n0, n1: tree sizes; cur: the lane's tree in its
 // previous iteration, -1 at its first (half the lanes per tree, pRRTC's iteration 1).
-// Strategy 1 splits the lanes in proportion to the other tree's share while the trees
-// differ by less than 1.5 x lanes nodes, else grows tree 0 while its share is below
-// tree_ratio; strategy 2 swaps a lane's tree while the size difference relative to it
-// is below tree_ratio.
+// Strategy 3 (the default) splits the lanes in proportion to the other tree's share at
+// every size; strategy 1 (pRRTC's) does so while the trees differ by less than 1.5 x
+// lanes nodes, else grows tree 0 while its share is below tree_ratio; strategy 2 swaps a
+// lane's tree while the size difference relative to it is below tree_ratio.  (Under
+// strategy 1 every lane grows the smaller tree once they differ: a tree trapped in a
+// pocket of free space then takes all lanes, the other tree stops growing, and an
+// unsolvable problem runs to its iteration cap or deadline instead of its node cap.)
 __host__ __device__ inline int balance_tree(int balance, float tree_ratio, int lanes, int n0, int n1, float h,
                                             int cur) {
     if (cur < 0 || balance == 0) return h < 0.5f ? 0 : 1;
+    if (balance == 3) return h < 1.f - (float)n0 / (float)(n0 + n1 > 1 ? n0 + n1 : 1) ? 0 : 1;
     if (balance == 2) {
         const int nt = cur == 0 ? n0 : n1, no = cur == 0 ? n1 : n0;
         const float ratio = (float)abs(nt - no) / (float)(nt > 1 ? nt : 1);

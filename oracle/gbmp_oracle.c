@@ -818,12 +818,14 @@ static float lane_hash(int32_t lane)
 /* Tree grown by a lane (pRRTC.cu:348-371).  balance: 0 none (half the lanes each), 1
  * proportional while the trees are within 1.5 x lanes nodes of each other and the
  * smaller one (by tree_ratio) otherwise, 2 VAMP (swap trees while the size difference
- * relative to the grown tree is below tree_ratio).  cur: the lane's tree in its previous
- * round, -1 in its first. */
+ * relative to the grown tree is below tree_ratio), 3 proportional at every size (the
+ * device planner's default).  cur: the lane's tree in its previous round, -1 in its
+ * first. */
 int32_t or_balance_tree(int32_t balance, float tree_ratio, int32_t lanes, int32_t n0, int32_t n1, float h,
                         int32_t cur)
 {
     if (cur < 0 || balance == 0) return h < 0.5f ? 0 : 1;
+    if (balance == 3) return h < 1.f - (float)n0 / (float)(n0 + n1 > 1 ? n0 + n1 : 1) ? 0 : 1;
     if (balance == 2) {
         int32_t nt = cur == 0 ? n0 : n1, no = cur == 0 ? n1 : n0;
         float ratio = (float)abs(nt - no) / (float)(nt > 1 ? nt : 1);

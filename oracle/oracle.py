@@ -267,7 +267,7 @@ def rrtc(model, start, goal, range_=0.1, res=0.01, rule=STEP_LINF, seed=0, max_n
             "tree_sizes": sizes.tolist()}, path[: pl.value].copy()
 
 
-def rrtc_lanes(model, start, goal, lanes=64, range_=0.1, res=0.01, rule=STEP_LINF, seed=0, balance=1,
+def rrtc_lanes(model, start, goal, lanes=64, range_=0.1, res=0.01, rule=STEP_LINF, seed=0, balance=3,
                tree_ratio=0.5, max_nodes=200000, max_iters=20000, path_cap=65536, nthreads=0):
     """Lane-parallel RRT-Connect in synchronous rounds: the device planner's per-lane rule
     (same Philox streams, balance rule, step rules), `lanes` lanes per round."""

@@ -16,7 +16,7 @@ per-lane rule, Philox streams, balance rule and step rule, lanes in synchronous 
 Every device path is also re-validated by the oracle's edge checker (up to the 1e-4 m
 clearance band, as every verdict test here).  The same bar
 compares batched solves (one persistent launch, lanes migrating between problems) with
-single solves, and pRRTC's balance strategy 2 on the device with the oracle.
+single solves, and pRRTC's balance strategies 1 and 2 on the device with the oracle.
 """
 import numpy as np
 import pytest
@@ -123,7 +123,7 @@ def _device_single(shelf, balance=_lib.BALANCE_DEFAULT, problems=None):
     return out
 
 
-def _oracle_lanes(shelf, balance=1, problems=None):
+def _oracle_lanes(shelf, balance=3, problems=None):
     robot, R, models, envs, probs = shelf
     out = []
     for seed, sc, s0, g0 in (problems or probs):
@@ -141,7 +141,14 @@ def single(shelf):
 
 def test_device_planner_matches_the_lane_parallel_oracle(shelf, single):
     ora = _oracle_lanes(shelf)
-    _compare("device vs oracle (balance 1)", single, ora)
+    _compare("device vs oracle (proportional balance)", single, ora)
+
+
+def test_balance_strategy_one_matches_the_oracle(shelf):
+    half = shelf[4][N_PROBLEMS // 2:]
+    dev = _device_single(shelf, balance=_lib.BALANCE_SIZE, problems=half)
+    ora = _oracle_lanes(shelf, balance=1, problems=half)
+    _compare("device vs oracle (balance 1)", dev, ora)
 
 
 def test_batched_solves_match_single_solves(shelf, single):

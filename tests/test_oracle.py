@@ -241,6 +241,9 @@ def test_balance_rule_follows_prrtc():
     # strategy 2: swap while |nt - no| / nt < tree_ratio
     assert O.balance_tree(2, 1.0, 64, 100, 90, 0.2, 0) == 1
     assert O.balance_tree(2, 0.05, 64, 100, 90, 0.2, 0) == 0
+    # proportional at every size (the device default)
+    assert O.balance_tree(3, 0.5, 64, 100, 900, 0.89, 1) == 0
+    assert O.balance_tree(3, 0.5, 64, 100, 900, 0.91, 0) == 1
     # a lane on the large tree swaps to the small one; a lane on the small tree stays
     assert O.balance_tree(2, 1.0, 64, 1000, 10, 0.2, 0) == 1
     assert O.balance_tree(2, 1.0, 64, 1000, 10, 0.2, 1) == 1
