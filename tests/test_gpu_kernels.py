@@ -384,3 +384,31 @@ def test_edges_too_long_to_validate_are_reported_not_checked(edge):
     np.testing.assert_array_equal(ns[:2], o_ns)
     np.testing.assert_array_equal(fh[:2], o_fh)
     assert ns[1] == 1
+
+
+def test_slab_contact_just_outside_the_band_is_a_collision():
+    """A 7-DOF configuration whose sphere reaches 1.03e-4 m into a shelf slab (outside the
+    1e-4 m band): the state check, the cost check and a two-state edge ending there all
+    report the collision."""
+    robot = W.serial_arm(1, dof=7, n_spheres=59, name="arm7")
+    env = W.shelf_env(0)
+    q = np.array([[0., -0.55056757, -0.4444837, -0.50623834, 1.2990656, -0.17087601, -1.0629332, 0.05316496]],
+                 np.float32)
+    m = O.OracleModel(robot, env)
+    assert m.clearance(q)[0] < -1e-4
+    R, E = api.Robot(robot), api.Env(env)
+    v = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E, dev(q), verdict=v)
+    costs = torch.zeros((4, 1), device="cuda")
+    vc = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E, dev(q), verdict=vc, costs=costs, mode=1)
+    torch.cuda.synchronize()
+    oc, _ = m.check_states(q)
+    np.testing.assert_allclose(costs.cpu().numpy(), oc, rtol=1e-3, atol=2e-6)
+    assert int(vc.item()) == 1
+    assert int(v.item()) == 1, "verdict-mode check misses a 0.1 mm slab contact"
+    prev = np.array([[0., -0.5432064, -0.43647614, -0.49676698, 1.2924869, -0.1640834, -1.0549506, 0.05819874]],
+                    np.float32)
+    ok, fh, _, ns = _run_edges(R, E, prev, q, 0.01, 1)
+    o_ok, o_fh, o_ns, _ = m.check_motions(prev, q, 0.01, 1)
+    assert ns[0] == o_ns[0] and fh[0] == o_fh[0] and not ok[0]

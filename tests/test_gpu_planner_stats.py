@@ -118,6 +118,13 @@ def _device_single(shelf, balance=_lib.BALANCE_DEFAULT, problems=None):
         r, path = planner.solve(envs[sc], s0, g0, lanes=LANES, max_iters=MAX_ITERS, range_=RANGE, resolution=RES,
                                 rule=RULE, seed=seed, time_limit_s=30.0, balance=balance)
         if r["solved"]:
+            # the device's own state check agrees that every waypoint is free (a planner
+            # that appended an unchecked node would fail here, whatever the rounding)
+            v = torch.zeros(len(path), dtype=torch.uint8, device="cuda")
+            api.check_states(R, envs[sc], torch.from_numpy(np.ascontiguousarray(path)).cuda(), verdict=v)
+            torch.cuda.synchronize()
+            bad = np.nonzero(v.cpu().numpy())[0]
+            assert len(bad) == 0, (seed, bad.tolist(), path[bad].tolist())
             _valid(models[sc][1], path, s0, g0)
         out.append((bool(r["solved"]), float(r["cost"])))
     return out
