@@ -426,6 +426,15 @@ typedef struct gbmp_server_config {
     float plan_resolution;
     int32_t step_rule;
     double plan_time_limit_s;
+    /* Blocks of one plan launch.  Plan launches are persistent: their blocks hold their
+     * SMs until the problems end, and check launches (on higher-priority streams) cannot
+     * preempt them, so a plan launch that fills every SM delays every check behind it.
+     * Capping the plan blocks leaves room on each SM for check blocks, at the price of plan
+     * throughput: on one GB300 at 2000 req/s of the 70 % check / 30 % plan stream, a cap of
+     * 3 blocks per SM over two plan workers (228 blocks each) cut the median latency from
+     * 392 to 164 ms and the check p99 from 1.30 to 0.75 s, but served 1198 instead of 1498
+     * req/s.  0: no cap (the planning kernel fits 5 blocks per SM). */
+    int32_t plan_max_blocks;
 } gbmp_server_config;
 
 typedef struct gbmp_request_info {

@@ -65,7 +65,7 @@ class ServerConfig(C.Structure):
                 ("plan_workers", C.c_int32), ("plan_batch", C.c_int32), ("plan_lanes", C.c_int32),
                 ("planner_max_nodes", C.c_int32), ("plan_path_cap", C.c_int32), ("plan_max_iters", C.c_int32),
                 ("plan_range", C.c_float), ("plan_resolution", C.c_float), ("step_rule", C.c_int32),
-                ("plan_time_limit_s", C.c_double)]
+                ("plan_time_limit_s", C.c_double), ("plan_max_blocks", C.c_int32)]
 
 
 class RequestInfo(C.Structure):

@@ -322,10 +322,11 @@ class Server:
     def __init__(self, num_streams: int = 4, hbm_budget_bytes: int = 1 << 30, max_batch_states: int = 1 << 20,
                  plan_workers: int = 1, plan_batch: int = 64, plan_lanes: int = 8, planner_max_nodes: int = 32768,
                  plan_path_cap: int = 4096, plan_max_iters: int = 100000, plan_range: float = 0.1,
-                 plan_resolution: float = 0.01, step_rule: int = _lib.STEP_LINF, plan_time_limit_s: float = 10.0):
+                 plan_resolution: float = 0.01, step_rule: int = _lib.STEP_LINF, plan_time_limit_s: float = 10.0,
+                 plan_max_blocks: int = 0):
         cfg = _lib.ServerConfig(num_streams, hbm_budget_bytes, max_batch_states, plan_workers, plan_batch, plan_lanes,
                                 planner_max_nodes, plan_path_cap, plan_max_iters, plan_range, plan_resolution,
-                                step_rule, plan_time_limit_s)
+                                step_rule, plan_time_limit_s, int(plan_max_blocks))
         h = C.c_void_p()
         check(_lib.load().gbmp_server_create(C.byref(cfg), C.byref(h)))
         self.handle = h

@@ -284,8 +284,20 @@ __device__ __forceinline__ void rot33(const float *n4, float s, float c, float *
 
 // Joint-local transform of link i (one lane): revolute P * R(axis, q), prismatic
 // P * T(axis q), fixed P, in the product order of mul_elem.  Unsupported types get
-// the identity and are flagged so that the chain gives them an identity pose.
-__device__ __forceinline__ void joint_local(const SmemTables &t, int i, float q, float *M) {
+// the identity and are flagged so that the chain gives them an identity pose.  Computed
+// in registers (joint_local_regs) and stored as three float4 rows: the 12-word stride
+// between the lanes' transforms then spreads a quarter-warp's stores over all 32 banks
+// (scalar stores at that stride hit 8 banks, 4-way conflicts).  `Mout` is 16-byte aligned.
+__device__ __forceinline__ void joint_local_regs(const SmemTables &t, int i, float q, float *M);
+__device__ __forceinline__ void joint_local(const SmemTables &t, int i, float q, float *Mout) {
+    float M[12];
+    joint_local_regs(t, i, q, M);
+    float4 *o = reinterpret_cast<float4 *>(Mout);
+    o[0] = make_float4(M[0], M[1], M[2], M[3]);
+    o[1] = make_float4(M[4], M[5], M[6], M[7]);
+    o[2] = make_float4(M[8], M[9], M[10], M[11]);
+}
+__device__ __forceinline__ void joint_local_regs(const SmemTables &t, int i, float q, float *M) {
     const float *P = t.jl + 12 * i;
     const int ty = t.type[i];
     if (ty == 1) {

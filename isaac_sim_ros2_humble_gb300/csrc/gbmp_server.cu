@@ -21,6 +21,7 @@
 //  * Every request records submit, start and finish times; the server keeps latency
 //    percentiles.
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <cmath>
 #include <chrono>
@@ -87,6 +88,7 @@ struct gbmp_server_s {
     int64_t cap_states = 0;                 // states per slot
     int max_L = 0;
     int device = 0;
+    int num_sms = 152;
 
     std::mutex mu;
     std::condition_variable cv_sched, cv_done, cv_plan, cv_complete;
@@ -299,8 +301,10 @@ void plan_loop(gbmp_server_s *s, int worker) {
         set.time_limit_s = s->cfg.plan_time_limit_s;
         std::vector<char> done(n, 0);
         // small batches get more lanes per problem (up to 1024 blocks per launch), large
-        // ones at least plan_lanes
-        const int lpp = std::max(s->cfg.plan_lanes, std::min(1024, 1024 / n));
+        // ones at least plan_lanes; with plan_max_blocks the launch's blocks stay within it so
+        // that check batches find room on every SM (persistent plan blocks hold their SMs)
+        const int cap = s->cfg.plan_max_blocks > 0 ? s->cfg.plan_max_blocks : INT_MAX;
+        const int lpp = std::max(1, std::min(std::max(s->cfg.plan_lanes, std::min(1024, 1024 / n)), cap / n));
         gbmp_status ps = cs != GBMP_OK ? cs : gbmp::batch_begin(bp, n, probs.data(), &set, lpp, 0, st);
         // hand out results as problems end
         auto deliver = [&](int i, int flag) {
@@ -393,9 +397,11 @@ gbmp_status gbmp_server_create(const gbmp_server_config *cfg, gbmp_server *out) 
                                               cfg->plan_lanes >= 1 && cfg->plan_path_cap >= 2 &&
                                               cfg->plan_range > 0.f && cfg->plan_max_iters >= 1),
                    "bad planner configuration");
+    GBMP_CHECK_ARG(cfg->plan_max_blocks >= 0, "plan_max_blocks < 0");
     auto *s = new gbmp_server_s();
     s->cfg = *cfg;
     cudaGetDevice(&s->device);
+    cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device);
     int lo_prio = 0, hi_prio = 0;
     cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     for (int i = 0; i < cfg->num_streams; ++i) {
