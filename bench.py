@@ -69,11 +69,11 @@ def parse():
     ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
     ap.add_argument("--edges", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="all", choices=["all", "edges", "plain", "plan", "batch", "serve"],
+    ap.add_argument("--workload", default="all", choices=["all", "edges", "plain", "fk", "plan", "batch", "serve"],
                     help="all: the headline edge line with every secondary workload; otherwise one workload's "
                          "own line")
     ap.add_argument("--plan-seeds", type=int, default=100)
-    ap.add_argument("--lanes", default="1024,2048,4096")
+    ap.add_argument("--lanes", default="1024,2048,4096,8192")
     ap.add_argument("--rates", default="200,1000,2000", help="serve: Poisson arrival rates (req/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
@@ -368,6 +368,70 @@ def gpu_problem_set(n_seeds, R, robot, api, W, torch):
         start, goal = W.pick_problem(free, edge_free, seed)
         problems.append((seed, sc, start, goal))
     return envs, problems
+
+
+def bench_fk(args, flush):
+    """Forward kinematics alone (the reference's generated FK kernel): 1,048,576 states of
+    the 8-DOF benchmark arm, 4x4 link poses and sphere centres written out.  Timed twice
+    on the same inputs: the table-driven kernel (tables staged in shared memory) and the
+    kernel generated for this robot at run time (NVRTC, every
+    constant a literal, one thread per state).  Both write the same bytes; the bound is
+    HBM.  The table-driven kernel takes chunks of 10 consecutive states per warp (the
+    chunk FK of edge validation) and writes each chunk's poses as one contiguous block."""
+    import torch
+    from isaac_sim_ros2_humble_gb300 import _lib, api, workloads as W
+    robot, _, _, _ = W.edge_workload(n_edges=16)
+    n = 1 << 20
+    q = torch.from_numpy(robot.sample_full(np.random.default_rng(7), n)).cuda()
+    L, S = robot.num_links, robot.num_spheres
+    poses = torch.empty((n, L, 16), device="cuda")
+    centers = torch.empty((n, S, 3), device="cuda")
+    nbytes = n * (4 * L + 64 * L + 12 * S)
+    peak = _hbm_peak()
+    out = {}
+    for name, cg in (("table", False), ("generated", True)):
+        R = api.Robot(robot, codegen=cg)
+        info = R.codegen_info() if cg else None
+        for _ in range(max(3, args.warmup)):
+            api.fk(R, q, poses, centers)
+        torch.cuda.synchronize()
+        ms = []
+        clk = ClockSampler(torch.cuda.current_device()).start()
+        clk.mark_begin()
+        for i in range(max(10, min(args.steps, 50))):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            api.fk(R, q, poses, centers)
+            b.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        clk.mark_end()
+        t = float(np.median(ms))
+        out[name] = {"ms": t, "states_per_s": n / (t / 1e3), "hbm_gbs": nbytes / (t / 1e3) / 1e9,
+                     "frac_of_measured_hbm": nbytes / (t / 1e3) / 1e9 / peak if peak else None,
+                     "clocks": clk.stop()}
+        if info:
+            out[name]["nvrtc_ms"] = info.get("compile_ms")
+            out[name]["cache"] = info.get("cache")
+        torch.cuda.synchronize()
+    best = min(out, key=lambda k: out[k]["ms"])
+    return {"metric": "FK states/s", "value": out["table"]["states_per_s"], "unit": "states/s",
+            "higher_is_better": True, "ms_per_step": out["table"]["ms"],
+            "config": {"workload": "fk_8dof_110spheres_1M_states", "states": n, "links": L, "spheres": S,
+                       "bytes_per_state": nbytes // n, "l2_flush": "384 MB buffer written between steps",
+                       "faster": best, "per_kernel": out},
+            "roofline": {"bound": "hbm", "achieved": out["table"]["hbm_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": out["table"]["frac_of_measured_hbm"],
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
+            "clocks": out["table"]["clocks"]}
+
+
+def _hbm_peak():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except Exception:
+        return 6800.0   # the recipe's fallback figure
 
 
 def bench_plan(args, flush):
@@ -715,10 +779,11 @@ def main():
     dev = torch.device("cuda", torch.cuda.current_device())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    if args.workload in ("plain", "plan", "batch", "serve"):
+    if args.workload in ("plain", "fk", "plan", "batch", "serve"):
         if rank != 0:
             return 0
         fn = {"plain": lambda: bench_plain(args, flush, _lib.measure_fp32_peak(1.0)),
+              "fk": lambda: bench_fk(args, flush),
               "plan": lambda: bench_plan(args, flush), "batch": lambda: bench_batch(args, flush),
               "serve": lambda: bench_serve(args)}[args.workload]
         print(json.dumps(_standalone_line(fn(), args)), flush=True)
@@ -854,6 +919,7 @@ def main():
         if args.workload == "all" and ws == 1:
             sec = {}
             for name, fn in (("plain_fk_collision", lambda: bench_plain(args, flush, fp32_peak)),
+                             ("fk", lambda: bench_fk(args, flush)),
                              ("plan", lambda: bench_plan(args, flush)),
                              ("uneven_batch", lambda: bench_batch(args, flush)),
                              ("serving", lambda: bench_serve(args))):

@@ -184,7 +184,7 @@ GBMP_API gbmp_status gbmp_check_states_fk(gbmp_robot robot, gbmp_env env, const 
  * ordered by the caller.  Each edge is validated by one warp, state order, stopping at its
  * first colliding state; the edges are taken longest first.  Robots of up to 32
  * sphere-carrying links are validated by chunks of consecutive states (the first 4
- * states, then 8 at a time; 4 for robots of more than 16 links), others state by state;
+ * states, then 10 at a time; 4 for robots of more than 16 links), others state by state;
  * gbmp_robot_set_edge_form overrides the form for one robot handle. */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
@@ -198,7 +198,7 @@ GBMP_API gbmp_status gbmp_check_edges(gbmp_robot robot, gbmp_env env, const floa
                              int32_t *d_first_hit, float *d_length, int32_t *d_num_steps, void *stream);
 
 /* Tuning and test control of the edge-validation form of one robot handle: 0 automatic
- * (the default), 1 state by state, 4 or 8 consecutive states per chunk (chunks need a
+ * (the default), 1 state by state, 4 or 10 consecutive states per chunk (chunks need a
  * robot of at most 32 sphere-carrying links; others stay state by state).  Results do
  * not depend on the form.  No counterpart in the reference. */
 GBMP_API gbmp_status gbmp_robot_set_edge_form(gbmp_robot robot, int32_t form);

@@ -59,7 +59,7 @@ class Robot:
         return pairs[: 2 * self.P].reshape(-1, 2), thr[: self.P]
 
     def set_edge_form(self, form: int):
-        """Edge-validation form of this handle: 0 automatic, 1 state by state, 4 or 8
+        """Edge-validation form of this handle: 0 automatic, 1 state by state, 4 or 10
         states per chunk (tuning and tests; results do not depend on it)."""
         check(_lib.load().gbmp_robot_set_edge_form(self.handle, int(form)))
 

@@ -80,21 +80,17 @@ __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K
     w.cmask = reinterpret_cast<unsigned *>(p + off);
 }
 
-// FK of the chunk's ks states (state s = s0 + k from f towards t by d, the last state of
-// the edge exactly t), all chains advancing together: first the ks x (L - 1) joint-local
-// transforms of links 1.. spread over the lanes link-major (the lanes of one pass mostly
-// share a joint type, so the type branches diverge little; link 0 is the identity and
-// needs none), then the chains, one pose row a lane (below).  The arithmetic is
-// warp_fk's (joint_local, mul_elem), so poses are bit-identical.
-template <int K>
-__device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const float *__restrict__ f,
-                                     const float *__restrict__ to, const float *__restrict__ d, int s0, int n,
-                                     float *locK, float *lpK, int lane) {
+// FK of a chunk's ks states, all chains advancing together: first the ks x (L - 1)
+// joint-local transforms of links 1.. spread over the lanes link-major (the lanes of one
+// pass mostly share a joint type, so the type branches diverge little; link 0 is the
+// identity and needs none), then the chains, one pose row a lane (below).  qv(k, i) is
+// joint i of state k.  The arithmetic is warp_fk's (joint_local, mul_elem), so poses are
+// bit-identical.
+template <int K, typename QV>
+__device__ inline void warp_fk_chunk_q(const SmemTables &t, int L, int ks, QV qv, float *locK, float *lpK, int lane) {
     for (int idx = lane; idx < ks * (L - 1); idx += kWarp) {
         const int i = 1 + idx / ks, k = idx - (i - 1) * ks;
-        const int s = s0 + k;
-        const float qv = (s == n - 1) ? to[i] : __fmaf_rn(d[i], (float)s, f[i]);
-        joint_local(t, i, qv, locK + 12 * (k * L + i));
+        joint_local(t, i, qv(k, i), locK + 12 * (k * L + i));
     }
     __syncwarp();
     // Composition: lane 3 k + r (k < ks) owns row r of state k's poses and walks the
@@ -127,6 +123,21 @@ __device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const f
         }
     }
     __syncwarp();
+}
+
+// FK of the chunk's ks states of one edge (state s = s0 + k from f towards t by d, the
+// last state of the edge exactly t).
+template <int K>
+__device__ inline void warp_fk_chunk(const SmemTables &t, int L, int ks, const float *__restrict__ f,
+                                     const float *__restrict__ to, const float *__restrict__ d, int s0, int n,
+                                     float *locK, float *lpK, int lane) {
+    warp_fk_chunk_q<K>(
+        t, L, ks,
+        [&](int k, int i) {
+            const int s = s0 + k;
+            return (s == n - 1) ? to[i] : __fmaf_rn(d[i], (float)s, f[i]);
+        },
+        locK, lpK, lane);
 }
 
 // Append this lane's obstacle (when mask != 0) to the candidate list; returns the new
@@ -582,8 +593,8 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
 
 #define GBMP_CHUNK_SWITCH(spl, K, ...)                                                       \
     do {                                                                                     \
-        if ((K) == 8) {                                                                      \
-            constexpr int KK = 8;                                                            \
+        if ((K) == 10) {                                                                     \
+            constexpr int KK = 10;                                                            \
             switch (spl) {                                                                   \
             case 1: { constexpr int SPL = 1; __VA_ARGS__; } break;                           \
             case 2: { constexpr int SPL = 2; __VA_ARGS__; } break;                           \
@@ -609,10 +620,13 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
         }                                                                                    \
     } while (0)
 
+// States per chunk: 10 (three pose-row lanes per state fill 30 of 32 lanes in the chunk
+// FK; measured 8.22 ms against 8.43 for 8 on the 65,536-edge benchmark call), 4 for
+// robots of more than 16 links, whose pose block per state is larger.
 int edge_chunk_states(const DevRobot &R, int form) {
     if (!R.cull || form == 1) return 0;
-    if (form == 4 || form == 8) return form;
-    return R.L <= 16 ? 8 : 4;
+    if (form == 4 || form == 10) return form;
+    return R.L <= 16 ? 10 : 4;
 }
 
 gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid) {
@@ -647,6 +661,90 @@ gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int gri
             k_edge_chunk<SPL, KK, false><<<grid, kChunkWarps * kWarp, smem, s>>>(R, E, from, to, nsteps, dir, order,
                                                                                  n_edges, next, ok, first_hit);
     });
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// FK alone (gbmp_fk): chunks of kFkChunk consecutive states per warp, the chunk FK above,
+// then the chunk's link poses and sphere centres written out.  The poses of consecutive
+// states are consecutive in memory, so a chunk's poses are one block that the warp writes
+// as 16-byte words, 512 contiguous bytes per store (float4 rows from shared memory, the
+// constant last row 0 0 0 1 built in registers); the sphere centres of the chunk are
+// likewise one block, written lane by lane in order.
+// ---------------------------------------------------------------------------------
+constexpr int kFkChunk = 10;
+
+__host__ __device__ inline size_t smem_fk_chunk_warp(const DevRobot &R) {
+    return 2 * align16(sizeof(float) * 12 * R.L * kFkChunk);
+}
+
+__global__ void __launch_bounds__(kChunkWarps *kWarp)
+    k_fk_chunk(DevRobot R, const float *__restrict__ q, long long n, float *__restrict__ poses,
+               float *__restrict__ centers, int vec) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const DevEnv E{0, 0, 0, nullptr};
+    SmemTables t = carve_tables(smem, R, 0);
+    if (!stage_tables(R, E, t, 0)) return;
+    const int warp = threadIdx.x / kWarp, lane = threadIdx.x & 31;
+    unsigned char *wbase = smem + smem_tables_bytes(R, 0) + smem_fk_chunk_warp(R) * warp;
+    float *lpK = reinterpret_cast<float *>(wbase);
+    float *locK = reinterpret_cast<float *>(wbase + align16(sizeof(float) * 12 * R.L * kFkChunk));
+    const int L = R.L, S = R.S;
+    const long long nchunks = (n + kFkChunk - 1) / kFkChunk;
+    const long long nw = (long long)gridDim.x * kChunkWarps;
+    for (long long c = blockIdx.x * (long long)kChunkWarps + warp; c < nchunks; c += nw) {
+        const long long s0 = c * kFkChunk;
+        const int ks = (int)min((long long)kFkChunk, n - s0);
+        const float *qc = q + s0 * L;
+        warp_fk_chunk_q<kFkChunk>(t, L, ks, [&](int k, int i) { return qc[k * L + i]; }, locK, lpK, lane);
+        if (poses) {
+            if (vec) {
+                float4 *P4 = reinterpret_cast<float4 *>(poses + s0 * L * 16);
+                const float4 *rows = reinterpret_cast<const float4 *>(lpK);
+                for (int f = lane; f < ks * L * 4; f += kWarp) {
+                    const int r = f & 3, kl = f >> 2;   // kl = k * L + link
+                    P4[f] = r < 3 ? rows[3 * kl + r] : make_float4(0.f, 0.f, 0.f, 1.f);
+                }
+            } else {
+                float *P = poses + s0 * L * 16;
+                for (int e = lane; e < ks * L * 16; e += kWarp) {
+                    const int kl = e >> 4, k = e & 15;
+                    P[e] = k < 12 ? lpK[12 * kl + k] : (k == 15 ? 1.f : 0.f);
+                }
+            }
+        }
+        if (centers) {
+            float *Cc = centers + s0 * S * 3;
+            for (int p = lane; p < ks * S; p += kWarp) {
+                const int k = p / S, j = p - k * S;
+                const float4 sp = t.sph[j];
+                const float3 c3 = xform_point_a16(lpK + 12 * (k * L + t.slink[j]), sp.x, sp.y, sp.z);
+                Cc[3 * p] = c3.x;
+                Cc[3 * p + 1] = c3.y;
+                Cc[3 * p + 2] = c3.z;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+gbmp_status fk_chunk_launch(const DevRobot &R, int num_sms, const float *q, long long n, float *poses,
+                            float *centers, cudaStream_t s) {
+    const size_t smem = smem_tables_bytes(R, 0) + smem_fk_chunk_warp(R) * kChunkWarps;
+    gbmp_status st = ensure_smem_optin((const void *)k_fk_chunk);
+    if (st) return st;
+    int per_sm = 0;
+    GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fk_chunk, kChunkWarps * kWarp, smem));
+    if (per_sm < 1) {
+        set_error("FK kernel does not fit on an SM (%zu bytes of shared memory)", smem);
+        return GBMP_ERR_CAPACITY;
+    }
+    long long grid = (long long)per_sm * num_sms;
+    const long long need = ((n + kFkChunk - 1) / kFkChunk + kChunkWarps - 1) / kChunkWarps;
+    if (need < grid) grid = need;
+    const int vec = (reinterpret_cast<uintptr_t>(poses) & 15u) == 0;
+    k_fk_chunk<<<(int)grid, kChunkWarps * kWarp, smem, s>>>(R, q, n, poses, centers, vec);
     GBMP_CUDA(cudaGetLastError());
     return GBMP_OK;
 }

@@ -749,6 +749,10 @@ gbmp_status gbmp_fk(gbmp_robot r, const float *d_q, int64_t n, float *d_poses, f
     if (n == 0) return GBMP_OK;
     GBMP_CHECK_ARG(d_q, "q is NULL");
     if (r->use_cg) return codegen_fk(r, d_q, n, d_poses, d_centers, (cudaStream_t)stream);
+    if (r->dev.L <= 16) {
+        ProfScope ps(GBMP_PROF_FK, (cudaStream_t)stream);
+        return fk_chunk_launch(r->dev, r->num_sms, d_q, n, d_poses, d_centers, (cudaStream_t)stream);
+    }
     const size_t smem = smem_tables_bytes(r->dev, 0) + smem_warp_bytes(r->dev) * kWarpsPerBlock;
     int grid = 0;
     gbmp_status st = persistent_grid(k_fk, smem, r->num_sms, &grid);
@@ -805,7 +809,7 @@ gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int6
 
 gbmp_status gbmp_robot_set_edge_form(gbmp_robot r, int32_t form) {
     GBMP_CHECK_ARG(r, "robot is NULL");
-    GBMP_CHECK_ARG(form == 0 || form == 1 || form == 4 || form == 8, "edge form %d is not 0, 1, 4 or 8", form);
+    GBMP_CHECK_ARG(form == 0 || form == 1 || form == 4 || form == 10, "edge form %d is not 0, 1, 4 or 10", form);
     r->edge_form = form;
     return GBMP_OK;
 }

@@ -119,7 +119,7 @@ struct gbmp_robot_s {
     // device tables (one allocation)
     void *d_block = nullptr;
     gbmp::DevRobot dev{};
-    // edge validation form: 0 automatic, 1 state by state, 4 or 8 states per chunk
+    // edge validation form: 0 automatic, 1 state by state, 4 or 10 states per chunk
     int edge_form = 0;
     // edge-check scratch
     std::mutex scratch_mu;
@@ -138,8 +138,11 @@ gbmp_status codegen_edge_setup(const gbmp_robot_s *r, const float *from, const f
                                cudaStream_t s);
 // Edge validation by chunks of consecutive states (gbmp_chunk.cu).  K = states per
 // chunk for this robot (0: use the per-state kernels); `form` is the robot handle's
-// edge_form (0 automatic, 1 per state, 4 or 8 states per chunk).
+// edge_form (0 automatic, 1 per state, 4 or 10 states per chunk).
 int edge_chunk_states(const DevRobot &R, int form);
+// FK alone of n states by chunks of consecutive states (robots of at most 16 links).
+gbmp_status fk_chunk_launch(const DevRobot &R, int num_sms, const float *q, long long n, float *poses,
+                            float *centers, cudaStream_t s);
 gbmp_status edge_chunk_prepare(const DevRobot &R, const DevEnv &E, int num_sms, int K, size_t *smem, int *grid);
 gbmp_status edge_chunk_launch(const DevRobot &R, const DevEnv &E, int K, int grid, size_t smem, cudaStream_t s,
                               const float *from, const float *to, const int *nsteps, const float *dir,

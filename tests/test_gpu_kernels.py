@@ -50,6 +50,33 @@ def test_fk_poses_and_centers(plain, edge):
         assert np.abs(poses.cpu().numpy() - m.fk(q)).max() < 2e-6
 
 
+def test_fk_sizes_and_unaligned_outputs(edge):
+    """gbmp_fk by chunks of consecutive states: partial last chunks, a single state, one
+    output alone, and pose / centre buffers that are not 16-byte aligned (written word by
+    word) all give the poses and centres of one full aligned call, bit for bit."""
+    robot, q = edge[0], edge[2]
+    R = edge[5]
+    L, S = robot.num_links, robot.num_spheres
+    n0 = q.shape[0]
+    p_ref = torch.zeros((n0, L, 16), device="cuda")
+    c_ref = torch.zeros((n0, S, 3), device="cuda")
+    api.fk(R, dev(q), p_ref, c_ref)
+    for n in (1, 9, 10, 11, 257):
+        flat_p = torch.full((n * L * 16 + 1,), float("nan"), device="cuda")
+        flat_c = torch.full((n * S * 3 + 1,), float("nan"), device="cuda")
+        poses, cen = flat_p[1:].view(n, L, 16), flat_c[1:].view(n, S, 3)   # 4-byte offset
+        assert poses.data_ptr() % 16 != 0
+        api.fk(R, dev(q[:n]), poses, cen)
+        only_p = torch.zeros((n, L, 16), device="cuda")
+        api.fk(R, dev(q[:n]), only_p, None)
+        only_c = torch.zeros((n, S, 3), device="cuda")
+        api.fk(R, dev(q[:n]), None, only_c)
+        torch.cuda.synchronize()
+        assert torch.equal(poses, p_ref[:n]) and torch.equal(cen, c_ref[:n])
+        assert torch.equal(only_p, p_ref[:n]) and torch.equal(only_c, c_ref[:n])
+        assert torch.isnan(flat_p[0]) and torch.isnan(flat_c[0])
+
+
 def test_fk_branching_tree():
     """Parent map that is not a chain, fixed and prismatic joints, un-normalised axes."""
     robot = W.tree_robot(3)
@@ -339,21 +366,48 @@ def test_check_edges_full_size_sampled_parity():
 
 
 def test_edge_forms_agree_on_every_edge_of_the_benchmark_call():
-    """All 65,536 edges of the benchmark call validated state by state (k_edge_wave) and by
-    chunks of 4 and 8 states (k_edge_chunk): identical verdicts, first hits, state counts
-    and lengths on every edge (the chunk form's narrow tests are the per-state tests)."""
+    """All 65,536 edges of the benchmark call validated state by state (k_edge_states) and
+    by chunks of 4 and 10 states (k_edge_chunk): identical verdicts, first hits, state
+    counts and lengths on every edge (the chunk form's narrow tests are the per-state
+    tests)."""
     robot, env, qf, qt = W.edge_workload()
     R, E = api.Robot(robot), api.Env(env)
     out = {}
-    for form in (1, 4, 8):
+    for form in (1, 4, 10):
         R.set_edge_form(form)
         out[form] = _run_edges(R, E, qf, qt, 0.01, 1)
     R.set_edge_form(0)
-    for form in (4, 8):
+    for form in (4, 10):
         for a, b in zip(out[form], out[1]):
             np.testing.assert_array_equal(a, b)
-    with pytest.raises(_lib.GbmpError):
-        R.set_edge_form(3)
+    for bad in (3, 8):
+        with pytest.raises(_lib.GbmpError):
+            R.set_edge_form(bad)
+
+
+@pytest.mark.parametrize("dof,n_spheres", [(4, 100), (3, 120), (6, 70)])
+def test_edge_forms_agree_for_large_sphere_groups(dof, n_spheres):
+    """Self-pair tests of the chunk form for links of 16 or fewer spheres (two group pairs
+    at a time, half a warp each), 17-32 spheres (a pair on the whole warp) and more than
+    32 (the pair list): the same first hits as the per-state form on every edge, and the
+    oracle's outside the clearance band."""
+    robot = W.serial_arm(30 + dof, dof=dof, n_spheres=n_spheres, offset_range=(0.1, 0.3),
+                         radius_range=(0.02, 0.05))
+    env = W.random_env(31, 40, 12, 4, oriented=True)
+    R, E = api.Robot(robot), api.Env(env)
+    rng = np.random.default_rng(dof)
+    qf, qt = robot.sample_full(rng, 1024), robot.sample_full(rng, 1024)
+    out = {}
+    for form in (1, 10):
+        R.set_edge_form(form)
+        out[form] = _run_edges(R, E, qf, qt, 0.02, 1)
+    R.set_edge_form(0)
+    for a, b in zip(out[10], out[1]):
+        np.testing.assert_array_equal(a, b)
+    ok, fh, ln, ns = out[10]
+    assert 0 < ok.sum() < len(ok)
+    m = O.OracleModel(robot, env)
+    _edge_parity(m, qf[:192], qt[:192], 0.02, 1, ok[:192], fh[:192], ln[:192], ns[:192])
 
 
 def test_device_status_is_clean_after_every_kernel_family(plain, edge):
