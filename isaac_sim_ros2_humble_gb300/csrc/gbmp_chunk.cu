@@ -285,7 +285,9 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             const int4 lpr = t.lpair[pairs_overflow ? k : cs.pl[k]];
             const float4 a = w.gb[lpr.x], b = w.gb[lpr.y];
             const float rr = a.w + b.w;
-            on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
+            // (with pairs_overflow every enabled pair is walked; a group outside `need`
+            // has no sphere placed this state, and its pairs cannot touch in this chunk)
+            on = ((need >> lpr.x) & (need >> lpr.y) & 1u) && sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
             ga = lpr.x;
             gb = lpr.y;
             p0 = lpr.z;
