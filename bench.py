@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--impl", default="gbmp", choices=["gbmp", "reference"])
     ap.add_argument("--edges", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="all", choices=["all", "edges", "plain", "fk", "plan", "batch", "serve"],
+    ap.add_argument("--workload", default="all", choices=["all", "edges", "plain", "fk", "checkbatch", "plan", "batch", "serve"],
                     help="all: the headline edge line with every secondary workload; otherwise one workload's "
                          "own line")
     ap.add_argument("--plan-seeds", type=int, default=100)
@@ -434,6 +434,68 @@ def _hbm_peak():
         return 6800.0   # the recipe's fallback figure
 
 
+def bench_check_batch(args, flush):
+    """Uneven checking instances: 256 state-check requests over 4 robots (6-9 DOF, 40-115
+    spheres) and 16 scenes (50-500 obstacles), sizes log-uniform in 1..65,536 states (the
+    serving mix's check requests).  One batched launch (gbmp_check_batch_run: a
+    descriptor per request, blocks staging their own request's tables) against the plain
+    path, one gbmp_check_states launch per request back to back on the same stream.  Both
+    are device-timed with CUDA events around the whole set; outputs are compared."""
+    import torch
+    from isaac_sim_ros2_humble_gb300 import api, workloads as W
+    robots = [W.serial_arm(80 + i, dof=6 + i, n_spheres=40 + 25 * i, prismatic_torso=i >= 2, resolution=0.01)
+              for i in range(4)]
+    envs = [W.random_env(90 + k, *(lambda O: (O - round(O * 80 / 336), round(O * 64 / 336), round(O * 16 / 336)))
+                         (50 + 30 * k), oriented=True) for k in range(16)]
+    R = [api.Robot(r) for r in robots]
+    E = [api.Env(e) for e in envs]
+    g = np.random.default_rng(17)
+    reqs, total = [], 0
+    for _ in range(256):
+        i, k = int(g.integers(4)), int(g.integers(16))
+        n = int(min(65536, np.exp(g.uniform(0, np.log(65536)))))
+        q = torch.from_numpy(robots[i].sample_full(g, n)).cuda()
+        reqs.append(dict(robot=R[i], env=E[k], q=q, verdict=torch.zeros(n, dtype=torch.uint8, device="cuda")))
+        total += n
+    plain_v = [torch.zeros_like(r["verdict"]) for r in reqs]
+    cb = api.CheckBatch(max_requests=len(reqs))
+
+    def batched():
+        cb.run(reqs)
+
+    def plain():
+        for r, v in zip(reqs, plain_v):
+            api.check_states(r["robot"], r["env"], r["q"], verdict=v)
+
+    out = {}
+    clk = ClockSampler(torch.cuda.current_device()).start()
+    clk.mark_begin()
+    for name, fn in (("batched", batched), ("plain", plain)):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for i in range(max(5, min(args.steps, 20))):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        out[name] = float(np.median(ms))
+    clk.mark_end()
+    same = all(torch.equal(r["verdict"], v) for r, v in zip(reqs, plain_v))
+    cb.close()
+    return {"metric": "uneven check batch throughput", "value": total / (out["batched"] / 1e3), "unit": "states/s",
+            "higher_is_better": True, "ms_per_step": out["batched"], "speedup_vs_plain": out["plain"] / out["batched"],
+            "config": {"workload": "check_batch_4robots_16scenes_256_requests", "requests": len(reqs),
+                       "states": total, "plain_ms": out["plain"], "verdicts_identical": bool(same),
+                       "l2_flush": "384 MB buffer written between steps",
+                       "timing": "CUDA events around the whole set of requests"},
+            "clocks": clk.stop()}
+
+
 def bench_plan(args, flush):
     """Single-problem parallel RRT-Connect: time to first solution over seeded shelf
     problems (7-DOF arm, 5 slabs + 40 boxes), for several lane counts."""
@@ -535,14 +597,16 @@ def bench_batch(args, flush):
         problems.append((R, E, s0, g0, 1000 + i))
     kw = dict(range_=PLAN_RANGE, resolution=PLAN_RES, rule=RULE, time_limit_s=10.0)
     bp = api.BatchPlanner(max_problems=n, max_nodes=32768, max_links=16, path_cap=4096)
-    # lanes per problem chosen on the batch itself (replays of the captured graph)
-    tune = {}
-    for lpp in (4, 8, 16, 32):
-        bp.solve(problems, lanes_per_problem=lpp, use_graph=True, **kw)
-        t0 = time.perf_counter()
-        out = bp.solve(problems, lanes_per_problem=lpp, use_graph=True, **kw)
-        tune[lpp] = ((time.perf_counter() - t0) * 1e3, sum(r["solved"] for r, _ in out))
-    best = min(tune, key=lambda k: tune[k][0])
+    # lanes per problem chosen by the library's launch-shape autotuner on the batch itself
+    # (gbmp_rrtc_solve_batch_auto: each candidate twice, then the fastest is kept)
+    api.BatchPlanner.autotune_reset()
+    tune_calls, tune, best = 0, {}, -1
+    while tune_calls < 20:
+        bp.solve(problems, lanes_per_problem="auto", use_graph=True, **kw)
+        tune_calls += 1
+        tune, best = api.BatchPlanner.autotune_record(problems, use_graph=True, **kw)
+        if best is not None and best >= 0:
+            break
     steps = max(3, min(args.steps, 5))
     clk = ClockSampler(torch.cuda.current_device()).start()
     times, solved = [], []
@@ -552,7 +616,7 @@ def bench_batch(args, flush):
         if rep == max(args.warmup, 1):
             clk.mark_begin()
         t0 = time.perf_counter()
-        out = bp.solve(problems, lanes_per_problem=best, use_graph=True, **kw)
+        out = bp.solve(problems, lanes_per_problem="auto", use_graph=True, **kw)
         if rep >= max(args.warmup, 1):
             times.append((time.perf_counter() - t0) * 1e3)
             solved.append(sum(r["solved"] for r, _ in out))
@@ -607,7 +671,8 @@ def bench_batch(args, flush):
             "higher_is_better": True, "ms_per_step": batch_ms, "steps": steps,
             "speedup_vs_plain": plain_ms / batch_ms,
             "config": {"workload": "uneven_batch_256_rrtc", "problems": n, "lanes_per_problem": best,
-                       "autotune_ms": {str(k): v[0] for k, v in tune.items()},
+                       "autotune_ms": {str(k): v for k, v in tune.items()}, "autotune_calls": tune_calls,
+                       "autotuner": "gbmp_rrtc_solve_batch_auto (in libgbmp, keyed by the batch shape)",
                        "solved_batched": int(np.median(solved)), "graph": True,
                        "plain_sequential_ms": plain_ms, "plain_lanes": plain_best,
                        "plain_solved": plain[plain_best][1],
@@ -779,11 +844,12 @@ def main():
     dev = torch.device("cuda", torch.cuda.current_device())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    if args.workload in ("plain", "fk", "plan", "batch", "serve"):
+    if args.workload in ("plain", "fk", "checkbatch", "plan", "batch", "serve"):
         if rank != 0:
             return 0
         fn = {"plain": lambda: bench_plain(args, flush, _lib.measure_fp32_peak(1.0)),
               "fk": lambda: bench_fk(args, flush),
+              "checkbatch": lambda: bench_check_batch(args, flush),
               "plan": lambda: bench_plan(args, flush), "batch": lambda: bench_batch(args, flush),
               "serve": lambda: bench_serve(args)}[args.workload]
         print(json.dumps(_standalone_line(fn(), args)), flush=True)
@@ -920,6 +986,7 @@ def main():
             sec = {}
             for name, fn in (("plain_fk_collision", lambda: bench_plain(args, flush, fp32_peak)),
                              ("fk", lambda: bench_fk(args, flush)),
+                             ("check_batch", lambda: bench_check_batch(args, flush)),
                              ("plan", lambda: bench_plan(args, flush)),
                              ("uneven_batch", lambda: bench_batch(args, flush)),
                              ("serving", lambda: bench_serve(args))):

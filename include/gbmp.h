@@ -168,6 +168,32 @@ GBMP_API gbmp_status gbmp_check_states_fk(gbmp_robot robot, gbmp_env env, const 
                                           int32_t mode, uint8_t *d_verdict, float *d_costs, float *d_total,
                                           float *d_poses, float *d_centers, void *stream);
 
+/* State checks of many (robot, scene) requests in one launch (no reference counterpart:
+ * the reference checks one space's states per checkStates call, SingleArmSpace.cu:
+ * 1572-1602).  Each request names its robot, scene, states and outputs (the arguments of
+ * gbmp_check_states_fk); its outputs are bit-identical to that call's.  The handle owns a
+ * pinned and a device descriptor table of max_requests entries, so a run allocates
+ * nothing; a run waits (on the host) until the previous run's descriptors have been
+ * uploaded, so one handle serves one stream at a time (use one handle per stream).  All
+ * robots must live on the device the handle was created on.  Requests with n = 0 are
+ * skipped. */
+typedef struct gbmp_check_batch_s *gbmp_check_batch;
+typedef struct gbmp_check_request {
+    gbmp_robot robot;
+    gbmp_env env;
+    const float *d_q;         /* [n x L] */
+    int64_t n;
+    uint8_t *d_verdict;       /* [n] or NULL */
+    float *d_costs;           /* [4 x n] (GBMP_CHECK_COST) or NULL */
+    float *d_total;           /* [n] (GBMP_CHECK_COST) or NULL */
+    float *d_poses;           /* [n x L x 16] or NULL */
+    float *d_centers;         /* [n x S x 3] or NULL */
+} gbmp_check_request;
+GBMP_API gbmp_status gbmp_check_batch_create(int32_t max_requests, gbmp_check_batch *out);
+GBMP_API gbmp_status gbmp_check_batch_run(gbmp_check_batch batch, const gbmp_check_request *requests,
+                                          int32_t n_requests, int32_t mode, void *stream);
+GBMP_API gbmp_status gbmp_check_batch_destroy(gbmp_check_batch batch);
+
 /* Edge validation, replacing SingleArmSpace::checkMotions / checkUnconstrainedMotions
  * (SingleArmSpace.cu:628-848; step rule KernelGenerator.h:408-465, interpolation
  * :467-522, feasibility SingleArmSpace.cu:603-626).  Edge k runs from d_from[k] to
@@ -401,12 +427,37 @@ GBMP_API gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner planner, int32_t n
                                            const gbmp_rrtc_settings *settings, int32_t lanes_per_problem,
                                            int32_t use_graph, gbmp_rrtc_result *results, float *h_paths,
                                            void *stream);
+/* gbmp_rrtc_solve_batch with the lanes per problem chosen by the library's launch-shape
+ * autotuner (no reference counterpart).  Decisions are keyed by the batch's shape: device,
+ * problem count, use_graph, the multiset of per-problem (links, sphere count bucket,
+ * obstacle count bucket) and the settings that change a lane's work (max_iters, range,
+ * resolution, step rule, dynamic domain, balance).  Each new key tries the candidates 4,
+ * 8, 16, 32 and 64 lanes per problem (those within the block limit) twice each on the
+ * caller's own solves, timed on the host around the synchronous solve, then keeps the
+ * candidate with the least time for every later solve of the key.  Results are those of
+ * gbmp_rrtc_solve_batch with that lane count; *lanes_used (NULL allowed) returns it.
+ * The decisions are kept in the process (all planners share them). */
+GBMP_API gbmp_status gbmp_rrtc_solve_batch_auto(gbmp_batch_planner planner, int32_t n,
+                                                const gbmp_rrtc_problem *problems,
+                                                const gbmp_rrtc_settings *settings, int32_t use_graph,
+                                                gbmp_rrtc_result *results, float *h_paths, int32_t *lanes_used,
+                                                void *stream);
+/* The autotuner's record for the shape of (problems, settings, use_graph): *count
+ * candidates (0: shape not seen), their lanes and least times in ms (-1: not tried yet;
+ * first `capacity` entries written, NULL allowed) and *chosen, the decided lanes per
+ * problem or -1 while still exploring. */
+GBMP_API gbmp_status gbmp_batch_autotune_lookup(int32_t n, const gbmp_rrtc_problem *problems,
+                                                const gbmp_rrtc_settings *settings, int32_t use_graph,
+                                                int32_t *lanes, double *ms, int32_t capacity, int32_t *count,
+                                                int32_t *chosen);
+/* Forgets every autotuner decision of the process. */
+GBMP_API gbmp_status gbmp_batch_autotune_reset(void);
 
 /* ---- continuous-batching request server ----
  * No counterpart in the reference (its callers run one request at a time).  Robots and
  * environments are registered once and stay resident; FK+collision requests are
- * batched as they arrive (grouped by robot and environment, one launch per group,
- * batches overlapping on `num_streams` streams) and admitted while the in-flight
+ * batched as they arrive (grouped by robot and environment, all groups of a batch in one
+ * gbmp_check_batch_run launch, batches overlapping on `num_streams` streams) and admitted while the in-flight
  * device bytes stay within hbm_budget_bytes; plan requests are solved in batched,
  * graph-captured launches by `plan_workers` threads with device-resident trees.
  * Host buffers passed to submit must stay valid until gbmp_server_wait returns. */

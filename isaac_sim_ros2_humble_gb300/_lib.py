@@ -28,6 +28,12 @@ class Projection(C.Structure):
                 ("tolerance", C.c_float * 6), ("use_boundary", C.c_int32), ("iterations", C.c_int32)]
 
 
+class CheckRequest(C.Structure):
+    _fields_ = [("robot", C.c_void_p), ("env", C.c_void_p), ("d_q", C.c_void_p), ("n", C.c_int64),
+                ("d_verdict", C.c_void_p), ("d_costs", C.c_void_p), ("d_total", C.c_void_p),
+                ("d_poses", C.c_void_p), ("d_centers", C.c_void_p)]
+
+
 class GbmpError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"gbmp status {status} ({STATUS.get(status, '?')}): {message}")
@@ -108,6 +114,9 @@ SIGNATURES = {
     "gbmp_fk": [_vp, _vp, _i64, _vp, _vp, _vp],
     "gbmp_check_states": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp],
     "gbmp_check_states_fk": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gbmp_check_batch_create": [_i32, C.POINTER(_vp)],
+    "gbmp_check_batch_run": [_vp, C.POINTER(CheckRequest), _i32, _i32, _vp],
+    "gbmp_check_batch_destroy": [_vp],
     "gbmp_robot_set_edge_form": [_vp, _i32],
     "gbmp_check_edges": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
     "gbmp_check_edges_noalloc": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
@@ -126,6 +135,11 @@ SIGNATURES = {
     "gbmp_batch_planner_destroy": [_vp],
     "gbmp_rrtc_solve_batch": [_vp, _i32, C.POINTER(RrtcProblem), C.POINTER(RrtcSettings), _i32, _i32,
                               C.POINTER(RrtcResult), _vp, _vp],
+    "gbmp_rrtc_solve_batch_auto": [_vp, _i32, C.POINTER(RrtcProblem), C.POINTER(RrtcSettings), _i32,
+                                   C.POINTER(RrtcResult), _vp, _i32p, _vp],
+    "gbmp_batch_autotune_lookup": [_i32, C.POINTER(RrtcProblem), C.POINTER(RrtcSettings), _i32, _i32p,
+                                   C.POINTER(C.c_double), _i32, _i32p, _i32p],
+    "gbmp_batch_autotune_reset": [],
     "gbmp_server_create": [C.POINTER(ServerConfig), C.POINTER(_vp)],
     "gbmp_server_add_robot": [_vp, _vp, _i32p],
     "gbmp_server_add_env": [_vp, _vp, _i32p],

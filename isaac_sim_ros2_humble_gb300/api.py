@@ -132,6 +132,41 @@ def check_states(robot: Robot, env: Env, q, verdict=None, costs=None, total=None
                                                ptr(total), ptr(poses), ptr(centers), stream_handle(stream)))
 
 
+class CheckBatch:
+    """State checks of many (robot, scene) requests in one launch (gbmp_check_batch_*).
+    run() takes a list of dicts with keys robot, env, q and optionally verdict, costs,
+    total, poses, centers (CUDA tensors, as check_states takes them).  One handle serves
+    one stream at a time."""
+
+    def __init__(self, max_requests: int = 1024):
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.gbmp_check_batch_create(int(max_requests), C.byref(h)))
+        self.handle = h
+        self.max_requests = int(max_requests)
+
+    def run(self, requests, mode=_lib.CHECK_VERDICT, stream=None):
+        arr = (_lib.CheckRequest * max(1, len(requests)))()
+        for i, r in enumerate(requests):
+            robot = r["robot"]
+            n = _n(r["q"], robot.L)
+            arr[i] = _lib.CheckRequest(robot.handle, r["env"].handle, ptr(r["q"]), n, ptr(r.get("verdict")),
+                                       ptr(r.get("costs")), ptr(r.get("total")), ptr(r.get("poses")),
+                                       ptr(r.get("centers")))
+        check(_lib.load().gbmp_check_batch_run(self.handle, arr, len(requests), int(mode), stream_handle(stream)))
+
+    def close(self):
+        if self.handle:
+            _lib.load().gbmp_check_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def check_edges(robot: Robot, env: Env, q_from, q_to, resolution: float = 0.0, rule: int = _lib.STEP_L2,
                 ok=None, first_hit=None, length=None, num_steps=None, stream=None):
     n = _n(q_from, robot.L)
@@ -283,12 +318,9 @@ class BatchPlanner:
         except Exception:
             pass
 
-    def solve(self, problems, lanes_per_problem: int = 8, use_graph: bool = True, max_iters: int = 100000,
-              range_: float = 0.1, resolution: float = 0.0, rule: int = _lib.STEP_L2, time_limit_s: float = 10.0,
-              stream=None, dynamic_domain: bool = False, dd_alpha: float = 1e-4, dd_radius: float = 4.0,
-              dd_min_radius: float = 1.0, balance: int = _lib.BALANCE_DEFAULT, tree_ratio: float = 0.0):
-        """problems: list of (Robot, Env, start[L], goal[L], seed).  Returns a list of
-        (result dict, path [path_len, L])."""
+    @staticmethod
+    def _inputs(problems, max_iters, range_, resolution, rule, time_limit_s, dynamic_domain, dd_alpha, dd_radius,
+                dd_min_radius, balance, tree_ratio):
         n = len(problems)
         arr = (_lib.RrtcProblem * n)()
         keep = []
@@ -299,11 +331,31 @@ class BatchPlanner:
         st = _lib.RrtcSettings(0, int(max_iters), float(range_), float(resolution), int(rule), 0, float(time_limit_s),
                                int(bool(dynamic_domain)), float(dd_alpha), float(dd_radius), float(dd_min_radius),
                                int(balance), float(tree_ratio))
+        return arr, st, keep
+
+    def solve(self, problems, lanes_per_problem=8, use_graph: bool = True, max_iters: int = 100000,
+              range_: float = 0.1, resolution: float = 0.0, rule: int = _lib.STEP_L2, time_limit_s: float = 10.0,
+              stream=None, dynamic_domain: bool = False, dd_alpha: float = 1e-4, dd_radius: float = 4.0,
+              dd_min_radius: float = 1.0, balance: int = _lib.BALANCE_DEFAULT, tree_ratio: float = 0.0):
+        """problems: list of (Robot, Env, start[L], goal[L], seed).  Returns a list of
+        (result dict, path [path_len, L]).  lanes_per_problem="auto" lets the library's
+        launch-shape autotuner choose (gbmp_rrtc_solve_batch_auto); the lanes it used are
+        then in self.last_lanes."""
+        n = len(problems)
+        arr, st, keep = self._inputs(problems, max_iters, range_, resolution, rule, time_limit_s, dynamic_domain,
+                                     dd_alpha, dd_radius, dd_min_radius, balance, tree_ratio)
         res = (_lib.RrtcResult * n)()
         paths = self._paths[:n]
-        check(_lib.load().gbmp_rrtc_solve_batch(self.handle, n, arr, C.byref(st), int(lanes_per_problem),
-                                                int(bool(use_graph)), res, paths.ctypes.data,
-                                                stream_handle(stream)))
+        if lanes_per_problem == "auto":
+            used = C.c_int32()
+            check(_lib.load().gbmp_rrtc_solve_batch_auto(self.handle, n, arr, C.byref(st), int(bool(use_graph)), res,
+                                                         paths.ctypes.data, C.byref(used), stream_handle(stream)))
+            self.last_lanes = used.value
+        else:
+            check(_lib.load().gbmp_rrtc_solve_batch(self.handle, n, arr, C.byref(st), int(lanes_per_problem),
+                                                    int(bool(use_graph)), res, paths.ctypes.data,
+                                                    stream_handle(stream)))
+            self.last_lanes = int(lanes_per_problem)
         out = []
         flat = self._paths.reshape(self.max_problems, -1)
         for i in range(n):
@@ -312,6 +364,27 @@ class BatchPlanner:
             p = flat[i, : r["path_len"] * L].reshape(-1, L).copy() if r["solved"] else np.zeros((0, L), np.float32)
             out.append((r, p))
         return out
+
+    @classmethod
+    def autotune_record(cls, problems, use_graph: bool = True, max_iters: int = 100000, range_: float = 0.1,
+                        resolution: float = 0.0, rule: int = _lib.STEP_L2, time_limit_s: float = 10.0,
+                        dynamic_domain: bool = False, dd_alpha: float = 1e-4, dd_radius: float = 4.0,
+                        dd_min_radius: float = 1.0, balance: int = _lib.BALANCE_DEFAULT, tree_ratio: float = 0.0):
+        """The autotuner's record for this batch shape: {lanes: least ms (-1 untried)} and
+        the chosen lanes (-1 while exploring, None if the shape was never solved)."""
+        arr, st, keep = cls._inputs(problems, max_iters, range_, resolution, rule, time_limit_s, dynamic_domain,
+                                    dd_alpha, dd_radius, dd_min_radius, balance, tree_ratio)
+        lanes, ms = (C.c_int32 * 16)(), (C.c_double * 16)()
+        cnt, chosen = C.c_int32(), C.c_int32()
+        check(_lib.load().gbmp_batch_autotune_lookup(len(problems), arr, C.byref(st), int(bool(use_graph)), lanes, ms,
+                                                     16, C.byref(cnt), C.byref(chosen)))
+        if cnt.value == 0:
+            return {}, None
+        return {lanes[i]: ms[i] for i in range(min(cnt.value, 16))}, chosen.value
+
+    @staticmethod
+    def autotune_reset():
+        check(_lib.load().gbmp_batch_autotune_reset())
 
 
 class Server:

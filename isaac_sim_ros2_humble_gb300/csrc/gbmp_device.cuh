@@ -751,4 +751,55 @@ __device__ inline bool warp_collide_dispatch(const SmemTables &t, const DevRobot
     }
 }
 
+// Link poses [L*16] (row-major 4x4, last row 0 0 0 1) and sphere centres [S*3] of the
+// state whose FK is in w.lp, written to HBM by the warp.
+__device__ inline void store_fk(const SmemTables &t, const DevRobot &R, const WarpScratch &w, long long s,
+                                float *__restrict__ poses, float *__restrict__ centers, int lane) {
+    if (poses) {
+        float *P = poses + s * R.L * 16;
+        for (int e = lane; e < R.L * 16; e += kWarp) {
+            const int li = e >> 4, k = e & 15;
+            P[e] = k < 12 ? w.lp[12 * li + k] : (k == 15 ? 1.f : 0.f);
+        }
+    }
+    if (centers) {
+        float *C = centers + s * R.S * 3;
+        for (int k = lane; k < R.S; k += kWarp) {
+            const float4 sp = t.sph[k];
+            const float3 p = xform_point(w.lp + 12 * t.slink[k], sp.x, sp.y, sp.z);
+            C[3 * k] = p.x; C[3 * k + 1] = p.y; C[3 * k + 2] = p.z;
+        }
+    }
+}
+
+// One state of a collision check, one warp: FK of state s of q, its poses / centres when
+// asked for, the collision test, and the outputs (verdict; in cost mode the four
+// constraint costs [4][n] and their total).  k_check_states and the batched check run
+// this routine, so their outputs are bit-identical.
+template <bool COST, int SPL>
+__device__ inline void check_state(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
+                                   const float *__restrict__ q, long long s, long long n,
+                                   unsigned char *__restrict__ verdict, float *__restrict__ costs,
+                                   float *__restrict__ total, float *__restrict__ poses, float *__restrict__ centers,
+                                   int lane) {
+    for (int j = lane; j < R.L; j += kWarp) w.q[j] = q[s * R.L + j];
+    __syncwarp();
+    warp_fk(t, R.L, w, lane);
+    if (poses || centers) store_fk(t, R, w, s, poses, centers, lane);
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    const bool hit = (!COST && R.cull) ? warp_collide_culled<SPL>(t, R, E, w, lane)
+                                       : warp_collide<SPL, COST>(t, R, E, w, lane, c);
+    if (lane == 0) {
+        if (COST) {
+            const float tot = ((c[0] + c[1]) + c[2]) + c[3];
+            if (costs) { costs[s] = c[0]; costs[n + s] = c[1]; costs[2 * n + s] = c[2]; costs[3 * n + s] = c[3]; }
+            if (total) total[s] = tot;
+            if (verdict) verdict[s] = tot != 0.f;
+        } else if (verdict) {
+            verdict[s] = hit;
+        }
+    }
+    __syncwarp();
+}
+
 }  // namespace gbmp

@@ -21,10 +21,12 @@
 // lane iteration cap, the node cap and a %globaltimer deadline end the launch with a
 // status the host reads.
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstring>
 
+#include "gbmp_autotune.h"
 #include "gbmp_rrtc.cuh"
 
 namespace gbmp {
@@ -516,6 +518,99 @@ gbmp_status gbmp_rrtc_solve_batch(gbmp_batch_planner b, int32_t n, const gbmp_rr
     gbmp_status st = gbmp::batch_begin(b, n, problems, s, lanes_per_problem, use_graph, (cudaStream_t)stream);
     if (st) return st;
     return gbmp::batch_end(b, problems, results, h_paths, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace gbmp {
+
+// Lanes-per-problem candidates of the autotuned batched solve, each timed twice.
+static LaneTuner &lane_tuner() {
+    static LaneTuner t({4, 8, 16, 32, 64}, 2);
+    return t;
+}
+
+// Signature of a batched solve's shape: device, problem count, graph use, the multiset of
+// per-problem (links, sphere bucket, obstacle bucket), and the settings that change the
+// work of a lane.
+static gbmp_status batch_shape_key(int n, const gbmp_rrtc_problem *problems, const gbmp_rrtc_settings *s,
+                                   int use_graph, uint64_t *key) {
+    GBMP_CHECK_ARG(problems && s && n >= 1, "NULL argument or n < 1");
+    int dev = 0;
+    GBMP_CUDA(cudaGetDevice(&dev));
+    ShapeKey k;
+    k.add((uint64_t)dev);
+    k.add((uint64_t)n);
+    k.add((uint64_t)(use_graph != 0));
+    std::vector<uint64_t> shapes((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        GBMP_CHECK_ARG(problems[i].robot && problems[i].env, "problem %d: robot/env is NULL", i);
+        const gbmp_env e = problems[i].env;
+        shapes[(size_t)i] = ((uint64_t)problems[i].robot->L << 48) | (shape_bucket(problems[i].robot->S) << 24) |
+                            shape_bucket((int64_t)e->ns + e->nb + e->nc);
+    }
+    std::sort(shapes.begin(), shapes.end());
+    for (uint64_t v : shapes) k.add(v);
+    uint32_t fr = 0, fs = 0;
+    memcpy(&fr, &s->range, 4);
+    memcpy(&fs, &s->resolution, 4);
+    k.add((uint64_t)s->max_iters);
+    k.add(((uint64_t)fr << 32) | fs);
+    k.add((uint64_t)(uint32_t)s->step_rule);
+    k.add((uint64_t)(uint32_t)s->dynamic_domain);
+    k.add((uint64_t)(uint32_t)s->balance);
+    *key = k.hash;
+    return GBMP_OK;
+}
+
+}  // namespace gbmp
+
+extern "C" {
+
+gbmp_status gbmp_rrtc_solve_batch_auto(gbmp_batch_planner b, int32_t n, const gbmp_rrtc_problem *problems,
+                                       const gbmp_rrtc_settings *s, int32_t use_graph, gbmp_rrtc_result *results,
+                                       float *h_paths, int32_t *lanes_used, void *stream) {
+    GBMP_CHECK_ARG(b && problems && s && results, "NULL argument");
+    GBMP_CHECK_ARG(n >= 1 && n <= b->max_problems, "n %d outside [1, %d]", n, b->max_problems);
+    uint64_t key = 0;
+    gbmp_status st = gbmp::batch_shape_key(n, problems, s, use_graph, &key);
+    if (st) return st;
+    const int max_lanes = (int)std::min<long long>(4096, (1LL << 30) / n);
+    bool trial = false;
+    const int lpp = gbmp::lane_tuner().choose(key, max_lanes, &trial);
+    const auto t0 = std::chrono::steady_clock::now();
+    st = gbmp_rrtc_solve_batch(b, n, problems, s, lpp, use_graph, results, h_paths, stream);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (st == GBMP_OK && trial) gbmp::lane_tuner().report(key, lpp, ms);
+    if (lanes_used) *lanes_used = lpp;
+    return st;
+}
+
+gbmp_status gbmp_batch_autotune_lookup(int32_t n, const gbmp_rrtc_problem *problems, const gbmp_rrtc_settings *s,
+                                       int32_t use_graph, int32_t *lanes, double *ms, int32_t capacity,
+                                       int32_t *count, int32_t *chosen) {
+    GBMP_CHECK_ARG(count && chosen, "NULL argument");
+    uint64_t key = 0;
+    gbmp_status st = gbmp::batch_shape_key(n, problems, s, use_graph, &key);
+    if (st) return st;
+    std::vector<int> cand;
+    std::vector<double> t;
+    int best = -1;
+    *count = 0;
+    *chosen = -1;
+    if (!gbmp::lane_tuner().lookup(key, &cand, &t, &best)) return GBMP_OK;
+    *count = (int32_t)cand.size();
+    *chosen = best;
+    for (int i = 0; i < (int)cand.size() && i < capacity; ++i) {
+        if (lanes) lanes[i] = cand[(size_t)i];
+        if (ms) ms[i] = t[(size_t)i];
+    }
+    return GBMP_OK;
+}
+
+gbmp_status gbmp_batch_autotune_reset(void) {
+    gbmp::lane_tuner().reset();
+    return GBMP_OK;
 }
 
 }  // extern "C"

@@ -68,6 +68,7 @@ struct Slot {
     cudaEvent_t done = nullptr;
     float *d_q = nullptr, *h_q = nullptr;   // [cap_states * max_L]
     uint8_t *d_v = nullptr, *h_v = nullptr; // [cap_states]
+    gbmp_check_batch cb = nullptr;          // one launch for all (robot, scene) groups
 };
 
 struct Batch {
@@ -161,7 +162,8 @@ void scheduler_loop(gbmp_server_s *s) {
         b.bytes = bytes;
         const auto now = Clock::now();
         for (auto &r : take) r->t_start = now;
-        // group by (robot, env): requests of a group become adjacent, one launch per group
+        // group by (robot, env): requests of a group become adjacent, one task per group,
+        // all groups in one batched launch
         std::stable_sort(b.reqs.begin(), b.reqs.end(), [](const std::shared_ptr<Request> &a,
                                                           const std::shared_ptr<Request> &c) {
             return a->robot != c->robot ? a->robot < c->robot : a->env < c->env;
@@ -176,7 +178,8 @@ void scheduler_loop(gbmp_server_s *s) {
         if (cudaMemcpyAsync(sl.d_q, sl.h_q, sizeof(float) * qfloats, cudaMemcpyHostToDevice, sl.stream) != cudaSuccess)
             st = GBMP_ERR_CUDA;
         size_t qoff = 0, voff = 0;
-        for (size_t i = 0; i < b.reqs.size() && st == GBMP_OK;) {
+        std::vector<gbmp_check_request> tasks;
+        for (size_t i = 0; i < b.reqs.size();) {
             const size_t q0 = qoff, v0 = voff;
             int64_t n = 0;
             size_t j = i;
@@ -186,10 +189,17 @@ void scheduler_loop(gbmp_server_s *s) {
                 voff += (size_t)b.reqs[j]->n;
                 ++j;
             }
-            st = gbmp_check_states(s->robots[b.reqs[i]->robot], s->envs[b.reqs[i]->env], sl.d_q + q0, n,
-                                   GBMP_CHECK_VERDICT, sl.d_v + v0, nullptr, nullptr, sl.stream);
+            gbmp_check_request t{};
+            t.robot = s->robots[b.reqs[i]->robot];
+            t.env = s->envs[b.reqs[i]->env];
+            t.d_q = sl.d_q + q0;
+            t.n = n;
+            t.d_verdict = sl.d_v + v0;
+            tasks.push_back(t);
             i = j;
         }
+        if (st == GBMP_OK)
+            st = gbmp_check_batch_run(sl.cb, tasks.data(), (int32_t)tasks.size(), GBMP_CHECK_VERDICT, sl.stream);
         if (st == GBMP_OK &&
             (cudaMemcpyAsync(sl.h_v, sl.d_v, vbytes, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess ||
              cudaEventRecord(sl.done, sl.stream) != cudaSuccess))
@@ -448,6 +458,10 @@ gbmp_status gbmp_server_start(gbmp_server s) {
     s->cap_states = std::min<int64_t>(s->cfg.max_batch_states,
                                       s->cfg.hbm_budget_bytes / ((int64_t)s->streams.size() * per_state));
     GBMP_CHECK_ARG(s->cap_states >= 1, "hbm_budget_bytes too small for one state per stream");
+    // a batch holds at most one task per (robot, scene) group
+    const int64_t groups64 = (int64_t)s->robots.size() * (int64_t)s->envs.size();
+    GBMP_CHECK_ARG(groups64 <= (1 << 20), "%lld (robot, scene) groups, at most 2^20", (long long)groups64);
+    const int32_t groups = (int32_t)groups64;
     for (size_t i = 0; i < s->streams.size(); ++i) {
         Slot sl;
         sl.stream = s->streams[i];
@@ -455,11 +469,14 @@ gbmp_status gbmp_server_start(gbmp_server s) {
         cudaError_t ce = cudaMalloc(&sl.d_q, qb + align16((size_t)s->cap_states));
         if (ce == cudaSuccess) ce = cudaMallocHost(&sl.h_q, qb + align16((size_t)s->cap_states));
         if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-        if (ce != cudaSuccess) {
+        gbmp_status bs = GBMP_OK;
+        if (ce == cudaSuccess) bs = gbmp_check_batch_create(groups, &sl.cb);
+        if (ce != cudaSuccess || bs != GBMP_OK) {
             if (sl.d_q) cudaFree(sl.d_q);
             if (sl.h_q) cudaFreeHost(sl.h_q);
-            set_error("server slot allocation failed: %s", cudaGetErrorString(ce));
-            return ce == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
+            if (sl.done) cudaEventDestroy(sl.done);
+            if (ce != cudaSuccess) set_error("server slot allocation failed: %s", cudaGetErrorString(ce));
+            return ce == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : (ce != cudaSuccess ? GBMP_ERR_CUDA : bs);
         }
         sl.d_v = reinterpret_cast<uint8_t *>(sl.d_q) + qb;
         sl.h_v = reinterpret_cast<uint8_t *>(sl.h_q) + qb;
@@ -582,6 +599,7 @@ gbmp_status gbmp_server_destroy(gbmp_server s) {
     for (auto &sl : s->slots) {
         cudaEventSynchronize(sl.done);
         cudaEventDestroy(sl.done);
+        gbmp_check_batch_destroy(sl.cb);
         cudaFree(sl.d_q);
         cudaFreeHost(sl.h_q);
     }

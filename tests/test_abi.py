@@ -113,7 +113,8 @@ def test_struct_layouts_match_ctypes(tmp_path):
     pairs = {"gbmp_robot_desc": _lib.RobotDesc, "gbmp_limits": _lib.Limits, "gbmp_projection": _lib.Projection,
              "gbmp_rrtc_settings": _lib.RrtcSettings, "gbmp_rrtc_result": _lib.RrtcResult,
              "gbmp_rrtc_problem": _lib.RrtcProblem, "gbmp_server_config": _lib.ServerConfig,
-             "gbmp_request_info": _lib.RequestInfo, "gbmp_server_metrics": _lib.ServerMetrics}
+             "gbmp_request_info": _lib.RequestInfo, "gbmp_server_metrics": _lib.ServerMetrics,
+             "gbmp_check_request": _lib.CheckRequest}
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "gbmp.h"', "int main(void) {"]
     for cname, cls in pairs.items():
         lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
@@ -144,3 +145,17 @@ def test_kernel_setup_is_recorded_per_device(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "devset ok" in out.stdout
+
+
+def test_batch_autotuner_policy_with_a_fake_timer(tmp_path):
+    """The batched planner's launch-shape tuner (csrc/gbmp_autotune.h), driven by a fake
+    timer: each allowed candidate tried twice in order, the least time of each kept, the
+    fastest chosen and kept per shape key, keys independent, lane limits respected, and
+    concurrent callers agreeing on one decision."""
+    exe = tmp_path / "autotune_check"
+    src = os.path.join(ROOT, "tests", "cpp", "autotune_check.cpp")
+    inc = os.path.join(ROOT, "isaac_sim_ros2_humble_gb300", "csrc")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-pthread", "-I", inc, src, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "autotune ok" in out.stdout

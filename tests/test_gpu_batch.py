@@ -67,3 +67,34 @@ def test_batch_matches_alone(batch):
         assert r1["solved"] == r["solved"]
         if r1["solved"]:
             _valid(m, p1, s, g)
+
+
+def test_autotuned_batch_explores_then_keeps_the_fastest(batch):
+    """gbmp_rrtc_solve_batch_auto: a new batch shape tries 4, 8, 16, 32 and 64 lanes per
+    problem twice each, in that order, on the caller's own solves, then keeps the one with
+    the least time; every solve along the way returns valid paths; another shape (fewer
+    problems) gets a decision of its own."""
+    models, probs, oracles = batch
+    api.BatchPlanner.autotune_reset()
+    bp = api.BatchPlanner(max_problems=32, max_nodes=32768, max_links=16, path_cap=4096)
+    kw = dict(use_graph=True, range_=0.1, resolution=RES, rule=RULE, time_limit_s=10.0)
+    assert api.BatchPlanner.autotune_record(probs, **kw) == ({}, None)
+    used = []
+    for call in range(12):
+        out = bp.solve(probs, lanes_per_problem="auto", **kw)
+        used.append(bp.last_lanes)
+        assert sum(r["solved"] for r, _ in out) >= 0.9 * len(probs)
+        for (r, path), (R, E, s, g, seed), m in zip(out, probs, oracles):
+            if r["solved"]:
+                _valid(m, path, s, g)
+    assert used[:10] == [4, 4, 8, 8, 16, 16, 32, 32, 64, 64]
+    times, chosen = api.BatchPlanner.autotune_record(probs, **kw)
+    assert sorted(times) == [4, 8, 16, 32, 64] and all(t > 0 for t in times.values())
+    assert chosen == min(times, key=lambda k: times[k])
+    assert used[10:] == [chosen, chosen]
+    sub = probs[:8]
+    assert api.BatchPlanner.autotune_record(sub, **kw) == ({}, None)
+    bp.solve(sub, lanes_per_problem="auto", **kw)
+    assert bp.last_lanes == 4
+    api.BatchPlanner.autotune_reset()
+    assert api.BatchPlanner.autotune_record(probs, **kw) == ({}, None)
