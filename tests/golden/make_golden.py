@@ -123,6 +123,61 @@ def main():
     g.update(proj_offset=off, proj_target=target, proj_tolerance=tol, proj_q=qp, proj_q1=p1[0], proj_task_cost=p1[1],
              proj_bound_cost=p1[2], limit_q=ql, limit_q1=pl[0], limit_bound_cost=pl[2])
 
+    # wider coverage from a second seed (the arrays above stay as they were):
+    # per-constraint costs of 128 more states, and the first colliding state of 40 short
+    # edges (reference step rule, interpolation, generated FK, sphere transform and cost
+    # kernels; an edge is feasible when every state's total cost is 0, and its first hit
+    # is the first state with a positive total).  The reference's kernels run here one
+    # thread at a time, about 0.1 s per state, so the edges are kept short (joint moves
+    # of at most 0.6, about 25 states each)
+    rng2 = np.random.default_rng(2025)
+
+    def ref_costs(qs):
+        k2 = len(qs)
+        fk = np.zeros((k2, L, 16), np.float32)
+        gen.ref_fk(np.ascontiguousarray(qs, np.float32), k2, fk)
+        c2 = np.zeros((k2, S, 3), np.float32)
+        mgr.ref_sphere_centers(k2, L, S, i32(robot.sphere_link), f32(robot.sphere_pos), fk.reshape(-1).copy(), c2)
+        out = np.zeros((4, k2), np.float32)
+        cc = np.ascontiguousarray(c2.reshape(-1))
+        cst.ref_cost_self(cc, i32(robot.sphere_link), r, np.ascontiguousarray(robot.enables, np.uint8).reshape(-1),
+                          S, L, k2, out[0])
+        cst.ref_cost_sphere(cc, r, S, k2, f32(env.sphere_pos), f32(env.sphere_r), ns, out[1])
+        cst.ref_cost_cuboid(cc, r, S, k2, f32(env.box_pos), f32(env.box_rot), f32(env.box_min), f32(env.box_max), nb,
+                            out[2])
+        cst.ref_cost_cylinder(cc, r, S, k2, f32(env.cyl_pos), f32(env.cyl_rot), f32(env.cyl_radius),
+                              f32(env.cyl_height), nc, out[3])
+        return out
+
+    q2 = robot.sample_full(rng2, 128)
+    g.update(state2_q=q2, state2_costs=ref_costs(q2))
+    # edges from collision-free starts (picked with the oracle, which only selects inputs
+    # here) so that first hits fall inside the edges, not at their first state
+    import oracle as O
+    om = O.OracleModel(robot, env)
+    cand = robot.sample_full(rng2, 400)
+    ne2 = 40
+    ef = cand[om.check_states(cand)[1] == 0][:ne2]
+    assert len(ef) == ne2
+    et = np.clip(ef + rng2.uniform(-0.6, 0.6, ef.shape).astype(np.float32) * robot.active,
+                 robot.lower, robot.upper).astype(np.float32)
+    res2 = np.float32(0.05)
+    st2 = np.zeros(ne2, np.int32)
+    d2 = np.zeros((ne2, L), np.float32)
+    dist2 = np.zeros(ne2, np.float32)
+    gen.ref_step(ef.copy(), et.copy(), ne2, res2, st2, d2, dist2)
+    start2 = np.concatenate([[0], np.cumsum(st2)[:-1]]).astype(np.int32)
+    states2 = np.zeros((int(st2.sum()), L), np.float32)
+    gen.ref_interp(np.ascontiguousarray(ef), np.ascontiguousarray(et), ne2, start2, st2.copy(), np.ascontiguousarray(d2),
+                   states2)
+    tot2 = ref_costs(states2).sum(axis=0)
+    fh2 = np.full(ne2, -1, np.int32)
+    for e in range(ne2):
+        hits = np.nonzero(tot2[start2[e]:start2[e] + st2[e]] > 0)[0]
+        if len(hits):
+            fh2[e] = hits[0]
+    g.update(edge2_from=ef, edge2_to=et, edge2_res=res2, edge2_steps=st2, edge2_first_hit=fh2)
+
     np.savez_compressed(OUT, **g)
     print(OUT, os.path.getsize(OUT), "bytes")
 

@@ -84,3 +84,31 @@ def test_projection():
     stable = np.abs(m.project(qu, O.projection(**kw))[0] - q1).max(axis=1) < 1e-5
     assert stable.mean() > 0.75
     assert np.abs(q1[stable] - G["proj_q1"][stable]).max() < 1e-4
+
+
+def _first_hits_agree(m, qf, qt, res, fh, gfh):
+    """First hits equal, or differing only where a state up to the later one lies inside
+    the clearance band."""
+    for k in np.nonzero(fh != gfh)[0]:
+        st = m.edge_states(qf[k], qt[k], res, O.STEP_L2)
+        upto = max(fh[k], gfh[k]) if min(fh[k], gfh[k]) >= 0 else len(st) - 1
+        assert np.any(np.abs(m.clearance(st[: upto + 1])) <= BAND), (k, fh[k], gfh[k])
+
+
+def test_wider_states_and_edge_first_hits(edge):
+    """128 more states (per-constraint costs) and 40 short edges from collision-free
+    starts whose first colliding state the reference's own step, interpolation, FK and
+    cost kernels give (7 of them collide part-way)."""
+    robot, env, m = edge
+    q2, gc = G["state2_q"], G["state2_costs"]
+    oc, ot = m.check_states(q2)
+    np.testing.assert_allclose(oc, gc, rtol=1e-4, atol=2e-5)
+    differ = (ot > 0) != (gc.sum(axis=0) > 0)
+    assert np.all(np.abs(m.clearance(q2[differ])) <= BAND)
+    ef, et, res = G["edge2_from"], G["edge2_to"], float(G["edge2_res"])
+    ok, fh, ns, _ = m.check_motions(ef, et, res, O.STEP_L2)
+    np.testing.assert_array_equal(ns, G["edge2_steps"])
+    gfh = G["edge2_first_hit"]
+    assert (gfh > 0).sum() >= 5 and (gfh < 0).sum() >= 5
+    _first_hits_agree(m, ef, et, res, fh, gfh)
+    np.testing.assert_array_equal(ok, fh < 0)

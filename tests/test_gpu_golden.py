@@ -1,7 +1,8 @@
 """The GPU kernels against golden vectors of the reference's own kernels
 (tests/golden/reference_outputs.npz, see tests/golden/make_golden.py): FK poses and
 sphere centres, per-constraint collision costs and verdicts, edge step counts and
-lengths, nearest-neighbour indices and steered states of the benchmark robot and scene."""
+lengths, edge first hits, nearest-neighbour indices and steered states of the benchmark
+robot and scene."""
 import os
 
 import numpy as np
@@ -65,3 +66,38 @@ def test_gpu_matches_reference_golden():
     api.steer(R, dev(G["nn_tree"][:64]), to, float(G["steer_max"]))
     torch.cuda.synchronize()
     assert np.abs(to.cpu().numpy() - G["steer_out"]).max() <= 1e-6
+
+
+def test_gpu_edge_first_hits_match_reference_golden():
+    """128 more states in cost mode and 40 short edges whose first colliding state comes
+    from the reference's own kernels: costs within FP32 tolerance, verdicts and first hits
+    equal outside the clearance band, on both edge forms."""
+    robot, env, _, _ = W.edge_workload(n_edges=1)
+    R, E = api.Robot(robot), api.Env(env)
+    m = O.OracleModel(robot, env)
+    q2, gc = G["state2_q"], G["state2_costs"]
+    n = len(q2)
+    costs = torch.zeros((4, n), device="cuda")
+    v = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E, dev(q2), verdict=v, costs=costs, mode=1)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(costs.cpu().numpy(), gc, rtol=2e-4, atol=4e-5)
+    differ = v.cpu().numpy().astype(bool) != (gc.sum(axis=0) > 0)
+    assert np.all(np.abs(m.clearance(q2[differ])) <= BAND)
+    ef, et, res = G["edge2_from"], G["edge2_to"], float(G["edge2_res"])
+    gfh = G["edge2_first_hit"]
+    ne = len(ef)
+    for form in (1, 0):
+        R.set_edge_form(form)
+        ok = torch.zeros(ne, dtype=torch.uint8, device="cuda")
+        fh = torch.zeros(ne, dtype=torch.int32, device="cuda")
+        ns = torch.zeros(ne, dtype=torch.int32, device="cuda")
+        api.check_edges(R, E, dev(ef), dev(et), res, _lib.STEP_L2, ok, fh, None, ns)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(ns.cpu().numpy(), G["edge2_steps"])
+        f = fh.cpu().numpy()
+        for k in np.nonzero(f != gfh)[0]:
+            st = m.edge_states(ef[k], et[k], res, O.STEP_L2)
+            upto = max(f[k], gfh[k]) if min(f[k], gfh[k]) >= 0 else len(st) - 1
+            assert np.any(np.abs(m.clearance(st[: upto + 1])) <= BAND), (form, k, f[k], gfh[k])
+    R.set_edge_form(0)
