@@ -74,6 +74,7 @@ def parse():
                          "own line")
     ap.add_argument("--plan-seeds", type=int, default=100)
     ap.add_argument("--lanes", default="1024,2048,4096,8192")
+    ap.add_argument("--fk-states", type=int, default=1 << 20, help="fk: states per launch")
     ap.add_argument("--rates", default="200,1000,2000", help="serve: Poisson arrival rates (req/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
@@ -381,7 +382,7 @@ def bench_fk(args, flush):
     import torch
     from isaac_sim_ros2_humble_gb300 import _lib, api, workloads as W
     robot, _, _, _ = W.edge_workload(n_edges=16)
-    n = 1 << 20
+    n = args.fk_states
     q = torch.from_numpy(robot.sample_full(np.random.default_rng(7), n)).cuda()
     L, S = robot.num_links, robot.num_spheres
     poses = torch.empty((n, L, 16), device="cuda")
@@ -418,7 +419,7 @@ def bench_fk(args, flush):
     best = min(out, key=lambda k: out[k]["ms"])
     return {"metric": "FK states/s", "value": out["table"]["states_per_s"], "unit": "states/s",
             "higher_is_better": True, "ms_per_step": out["table"]["ms"],
-            "config": {"workload": "fk_8dof_110spheres_1M_states", "states": n, "links": L, "spheres": S,
+            "config": {"workload": f"fk_8dof_110spheres_{n}_states", "states": n, "links": L, "spheres": S,
                        "bytes_per_state": nbytes // n, "l2_flush": "384 MB buffer written between steps",
                        "faster": best, "per_kernel": out},
             "roofline": {"bound": "hbm", "achieved": out["table"]["hbm_gbs"], "peak": peak, "unit": "GB/s",
