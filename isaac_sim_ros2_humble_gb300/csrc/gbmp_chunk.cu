@@ -40,6 +40,7 @@ struct ChunkScratch {
     unsigned *cl;     // candidate obstacle indices
     unsigned *cm;     // their group masks
     int *pl;          // enabled group pairs whose swept spheres overlap (lpair indices)
+    int *nl;          // the spheres of the groups in `need`, in sphere order
 };
 
 // Per-warp shared memory of the chunk kernel: the link poses of the chunk, then one
@@ -50,8 +51,8 @@ struct ChunkScratch {
 // (11 KB without the sharing), which leaves room for larger scenes.
 __host__ __device__ inline size_t smem_chunk_rest(const DevRobot &R) {
     return align16(sizeof(float4) * R.G) + align16(sizeof(float) * R.G) + 2 * align16(sizeof(unsigned) * kChunkCands) +
-           align16(sizeof(int) * kChunkPairs) + align16(sizeof(float4) * R.S) + align16(sizeof(float4) * R.G) +
-           align16(sizeof(float) * R.G) + 2 * align16(sizeof(int) * kWarp);
+           align16(sizeof(int) * kChunkPairs) + align16(sizeof(int) * R.S) + align16(sizeof(float4) * R.S) +
+           align16(sizeof(float4) * R.G) + align16(sizeof(float) * R.G) + 2 * align16(sizeof(int) * kWarp);
 }
 
 __host__ __device__ inline size_t smem_chunk_bytes(const DevRobot &R, int K) {
@@ -70,6 +71,7 @@ __device__ inline void carve_chunk(unsigned char *base, const DevRobot &R, int K
     c.cl = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
     c.cm = reinterpret_cast<unsigned *>(p + off); off += align16(sizeof(unsigned) * kChunkCands);
     c.pl = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * kChunkPairs);
+    c.nl = reinterpret_cast<int *>(p + off); off += align16(sizeof(int) * R.S);
     w.lp = nullptr;
     w.loc = nullptr;
     w.q = nullptr;
@@ -184,21 +186,27 @@ __device__ __forceinline__ float3 xform_point_a16(const float *T, float x, float
 // Exact tests of one state (link poses lp) against the chunk's candidates, then its
 // self-collision pairs.  ns_end / nb_end / nc_end delimit the sphere / cuboid /
 // cylinder candidates; `need` holds the groups any candidate or listed group pair
-// involves (spheres of other groups cannot collide in this chunk and are not placed);
-// npr group pairs are listed in cs.pl unless pairs_overflow.
+// involves (spheres of other groups cannot collide in this chunk and are not placed),
+// and cs.nl lists their nn spheres, packed into the lanes' slots (about 3.4 of the 8
+// groups of the benchmark arm are needed per state, so two slots of four hold them and
+// the slots past the last sphere are skipped); npr group pairs are listed in cs.pl
+// unless pairs_overflow.
 template <int SPL, bool CNT>
 __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                    const ChunkScratch &cs, const float *lp, int ns_end, int nb_end, int nc_end,
-                                   unsigned need, int npr, bool pairs_overflow, int lane, unsigned long long &fl) {
+                                   unsigned need, int npr, bool pairs_overflow, int nn, int lane,
+                                   unsigned long long &fl) {
     constexpr bool count = CNT;   // executed-work accounting compiled in only when asked for
     float cx[SPL], cy[SPL], cz[SPL], cr[SPL], A[SPL];
     unsigned gbit[SPL];
+    const int ms = (nn + kWarp - 1) / kWarp;   // slots holding a sphere on some lane
 #pragma unroll
     for (int m = 0; m < SPL; ++m) {
-        const int k = lane + kWarp * m;
-        const bool place = k < R.S && ((need >> t.sgrp[k]) & 1u);
+        const int idx = lane + kWarp * m;
+        const bool place = idx < nn;
         if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, place)) * 24;
         if (place) {
+            const int k = cs.nl[idx];
             const float4 s = t.sph[k];
             const float3 p = xform_point_a16(lp + 12 * t.slink[k], s.x, s.y, s.z);
             cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
@@ -227,6 +235,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
         const float nb = snb[o];
 #pragma unroll
         for (int m = 0; m < SPL; ++m) {
+            if (m >= ms) break;
             const float v = __fmaf_rn(cx[m], b.x, __fmaf_rn(cy[m], b.y, __fmaf_rn(cz[m], b.z, __fmaf_rn(cr[m], b.w, nb))));
             hit |= (cm & gbit[m]) && v > A[m];
             if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlSphereX;
@@ -241,6 +250,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
         const float4 r0 = bx[5 * o], r1 = bx[5 * o + 1], r2 = bx[5 * o + 2], mn = bx[5 * o + 3], mx = bx[5 * o + 4];
 #pragma unroll
         for (int m = 0; m < SPL; ++m) {
+            if (m >= ms) break;
             if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlCuboid;
             if (cm & gbit[m]) {
                 const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
@@ -260,6 +270,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
         const float4 r0 = cyl[4 * o], r1 = cyl[4 * o + 1], r2 = cyl[4 * o + 2], pr = cyl[4 * o + 3];
 #pragma unroll
         for (int m = 0; m < SPL; ++m) {
+            if (m >= ms) break;
             if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlCylinder;
             if (cm & gbit[m]) {
                 const float3 l = xform_rows(r0, r1, r2, cx[m], cy[m], cz[m]);
@@ -513,6 +524,18 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     // --- D: states in order ---
     int found = -1;
     const int kend = (need == 0u && !overflow) ? 0 : ks;   // nothing near any state: all free
+    // the spheres of the needed groups, packed, so that the per-state slots hold only them
+    int nn = 0;
+    if (kend > 0 && !overflow) {
+        for (int k0 = 0; k0 < R.S; k0 += kWarp) {
+            const int k = k0 + lane;
+            const bool in = k < R.S && ((need >> t.sgrp[k]) & 1u);
+            const unsigned bal = __ballot_sync(kFull, in);
+            if (in) cs.nl[nn + __popc(bal & ((1u << lane) - 1u))] = k;
+            nn += __popc(bal);
+        }
+        __syncwarp();
+    }
     for (int k = 0; k < kend; ++k) {
         const int s = s0 + k;
         if (k == 4 && first_hit) {   // once per chunk: stop if another warp found an earlier hit on this edge
@@ -526,7 +549,8 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
         if (overflow) {
             hit = chunk_fallback<SPL>(t, R, E, w, lp, lane);
         } else {
-            hit = chunk_state<SPL, CNT>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, lane, fl);
+            hit = chunk_state<SPL, CNT>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, nn, lane,
+                                        fl);
         }
         __syncwarp();
         if (hit) {
