@@ -32,13 +32,18 @@ __device__ inline void dd_update(float *radius, bool failed, const RrtcParams &p
 
 // Squared active-joint distance of one node (NW float4 words) from the query held in
 // registers, accumulated joint by joint in index order; inactive joints add exactly 0.
-// `written` clears if any coordinate still holds the NaN sentinel.
+// `written` clears if any coordinate still holds the NaN sentinel.  The words are read
+// through L1 (the blocks on one SM scan the same trees): a node is written once, from
+// the sentinel to its final value, so a line cached before the write can only show the
+// sentinel, and the node is skipped as not yet written, as it is when the scan simply
+// runs before the write (measured: shelf p50 0.82 against 0.86 ms, uneven batch 553-564
+// against 574-579 ms).
 template <int NW>
 __device__ __forceinline__ float node_dist(const float4 *__restrict__ y, const float (&qr)[4 * NW], unsigned am, int L,
                                            bool &written) {
     float4 v4[NW];
 #pragma unroll
-    for (int k = 0; k < NW; ++k) v4[k] = __ldcg(y + k);
+    for (int k = 0; k < NW; ++k) v4[k] = __ldca(y + k);
     float s = 0.f;
 #pragma unroll
     for (int k = 0; k < NW; ++k) {
@@ -136,13 +141,19 @@ __device__ inline int block_nearest(const float *__restrict__ nodes, int size, i
 // Validate the edge a -> b (full joint vectors in shared memory) with the step rule of
 // checkMotions: n = floor(metric / res) + 1 states, dir = (b - a) / n, state k = a +
 // dir * k, the last state is b (for GBMP_STEP_COUNT, pRRTC's granularity G = res:
-// n = G + 1 and dir = (b - a) / G, so the states are at k / G); state 0 (= a, already in
-// the tree) is skipped unless n == 1.  One warp per state.  Returns true if every
-// state is collision-free.
+// n = G + 1 and dir = (b - a) / G, so the states are at k / G).  The states are checked in
+// the direction the edge takes in a returned path, so that a path check (which walks the
+// path from the start root to the goal root) meets exactly the states checked here: the
+// interpolated states of a -> b and b -> a differ, and a thin contact can lie between the
+// states of one direction and on a state of the other.  old_first: a is the node already
+// in the tree (start tree edges), state 0 (= a) is skipped unless n == 1; otherwise
+// (goal tree edges, the new node first) b is the node already in the tree and the last
+// state (= b) is skipped, and with n == 1 the one state checked is a.  One warp per state.
+// Returns true if every state is collision-free.
 template <int SPL, bool CULL>
 __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
-                                const float *a, const float *b, float res, int rule, int *s_flag, float *s_dir,
-                                int *s_n) {
+                                const float *a, const float *b, float res, int rule, bool old_first, int *s_flag,
+                                float *s_dir, int *s_n) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x / kWarp;
     if (threadIdx.x == 0) {
         float d2 = 0.f, dinf = 0.f;
@@ -167,12 +178,14 @@ __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const De
     const float parts = rule == GBMP_STEP_COUNT ? (float)(n - 1) : (float)n;
     for (int j = threadIdx.x; j < R.L; j += blockDim.x) s_dir[j] = __fdiv_rn(__fadd_rn(b[j], -a[j]), parts);
     __syncthreads();
-    for (int k0 = (n == 1 ? 0 : 1); k0 < n; k0 += kRrtcWarps) {
+    const int first = old_first ? (n == 1 ? 0 : 1) : 0;
+    const int last = old_first ? n : (n == 1 ? 1 : n - 1);   // exclusive
+    for (int k0 = first; k0 < last; k0 += kRrtcWarps) {
         const int k = k0 + warp;
         bool hit = false;
-        if (k < n) {
+        if (k < last) {
             for (int j = lane; j < R.L; j += kWarp)
-                w.q[j] = (k == n - 1) ? b[j] : __fmaf_rn(s_dir[j], (float)k, a[j]);
+                w.q[j] = (old_first && k == n - 1) ? b[j] : __fmaf_rn(s_dir[j], (float)k, a[j]);
             __syncwarp();
             warp_fk(t, R.L, w, lane);
             hit = CULL ? warp_collide_culled<SPL>(t, R, E, w, lane)
@@ -319,8 +332,9 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
         for (int j = threadIdx.x; j < L; j += blockDim.x)
             if (act[j] && scale < 1.f) q_s[j] = __fmaf_rn(scale, __fadd_rn(q_s[j], -q_a[j]), q_a[j]);
         __syncthreads();
-        // 5. validate nn -> new
-        if (!block_edge_free<SPL, CULL>(t, R, E, w, q_a, q_s, prm.res, prm.rule, s_misc + 4, s_dir, s_misc + 5)) {
+        // 5. validate nn -> new, in path order (start tree: nn first; goal tree: new first)
+        if (!block_edge_free<SPL, CULL>(t, R, E, w, tr == 0 ? q_a : q_s, tr == 0 ? q_s : q_a, prm.res, prm.rule,
+                                        tr == 0, s_misc + 4, s_dir, s_misc + 5)) {
             if (prm.dd && threadIdx.x == 0) dd_update(P.radii[tr] + nn, true, prm);
             continue;
         }
@@ -358,7 +372,10 @@ __device__ void rrtc_lane(const DevRobot &R, const DevEnv &E, const RrtcDev &P, 
                 q_c[j] = (e == n_ext) ? q_b[j]
                                       : __fmaf_rn(__fdiv_rn(__fadd_rn(q_b[j], -q_s[j]), (float)n_ext), (float)e, q_s[j]);
             __syncthreads();
-            if (!block_edge_free<SPL, CULL>(t, R, E, w, q_a, q_c, prm.res, prm.rule, s_misc + 4, s_dir, s_misc + 5)) {
+            // in path order: the last step joins the goal tree's node to the start tree's
+            // (start tree first), every other step runs away from its tree's root
+            if (!block_edge_free<SPL, CULL>(t, R, E, w, tr == 0 ? q_a : q_c, tr == 0 ? q_c : q_a, prm.res, prm.rule,
+                                            tr == 0, s_misc + 4, s_dir, s_misc + 5)) {
                 connected = false;
                 break;
             }

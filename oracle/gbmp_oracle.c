@@ -670,6 +670,26 @@ static int edge_free(const or_robot *r, const or_env *e, int32_t np, const int32
     return 1;
 }
 
+/* A tree edge old -> new checked in the direction it takes in a returned path (which runs
+ * from the start root to the goal root), so that a path check meets exactly these states:
+ * start tree (tr 0) edges from the old node, state 0 skipped (edge_free); goal tree edges
+ * from the new node towards the old one, the last state (the old node) skipped, and with
+ * one state the new node itself.  Mirrors block_edge_free's old_first rule. */
+static int edge_free_tree(const or_robot *r, const or_env *e, int32_t np, const int32_t *pairs, const float *thr,
+                          const float *old, const float *nw, int tr, float res, int32_t rule, float *P, float *C,
+                          float *dir, float *st)
+{
+    if (tr == 0) return edge_free(r, e, np, pairs, thr, old, nw, res, rule, P, C, dir, st);
+    const int J = r->L;
+    int32_t n = or_edge_steps(nw, old, J, res, rule, dir, NULL);
+    if (n == 1) return !state_collides(r, e, np, pairs, thr, nw, P, C);
+    for (int32_t k = 0; k < n - 1; ++k) {
+        or_edge_state(nw, old, dir, J, n, k, st);
+        if (state_collides(r, e, np, pairs, thr, st, P, C)) return 0;
+    }
+    return 1;
+}
+
 static int32_t tree_nearest(const float *nodes, int32_t size, int32_t J, const uint8_t *active, const float *q)
 {
     float best = INFINITY;
@@ -733,7 +753,7 @@ int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *p
             float sc = range / d;
             for (int j = 0; j < J; ++j) if (active[j]) qs[j] = fmaf(sc, qs[j] - qn[j], qn[j]);
         }
-        if (!edge_free(r, e, np, pairs, thr, qn, qs, res, rule, P, C, dir, st)) continue;
+        if (!edge_free_tree(r, e, np, pairs, thr, qn, qs, tr, res, rule, P, C, dir, st)) continue;
         if (size[tr] >= max_nodes) break;
         int32_t cur = size[tr]++;
         memcpy(nodes[tr] + (int64_t)cur * J, qs, sizeof(float) * J);
@@ -747,7 +767,7 @@ int32_t or_rrtc(const or_robot *r, const or_env *e, int32_t np, const int32_t *p
         int ok = 1;
         for (int32_t k = 1; k <= n_ext && ok; ++k) {
             for (int j = 0; j < J; ++j) qc[j] = (k == n_ext) ? qb[j] : fmaf((qb[j] - qs[j]) / (float)n_ext, (float)k, qs[j]);
-            if (!edge_free(r, e, np, pairs, thr, qa, qc, res, rule, P, C, dir, st)) { ok = 0; break; }
+            if (!edge_free_tree(r, e, np, pairs, thr, qa, qc, tr, res, rule, P, C, dir, st)) { ok = 0; break; }
             if (k < n_ext) {
                 if (size[tr] >= max_nodes) { ok = 0; break; }
                 int32_t nx = size[tr]++;
@@ -903,7 +923,7 @@ int32_t or_rrtc_lanes(const or_robot *r, const or_env *e, int32_t np, const int3
                 float sc = range / d;
                 for (int j = 0; j < J; ++j) if (active[j]) o->qs[j] = fmaf(sc, o->qs[j] - qn[j], qn[j]);
             }
-            o->ext = edge_free(r, e, np, pairs, thr, qn, o->qs, res, rule, P_, C_, dir, st);
+            o->ext = edge_free_tree(r, e, np, pairs, thr, qn, o->qs, tr, res, rule, P_, C_, dir, st);
             if (P_ != P) free(P_);
             if (C_ != C) free(C_);
         }
@@ -937,7 +957,7 @@ int32_t or_rrtc_lanes(const or_robot *r, const or_env *e, int32_t np, const int3
             for (int32_t k = 1; k <= n_ext && ok; ++k) {
                 for (int j = 0; j < J; ++j)
                     qc[j] = (k == n_ext) ? qb[j] : fmaf((qb[j] - o->qs[j]) / (float)n_ext, (float)k, o->qs[j]);
-                if (!edge_free(r, e, np, pairs, thr, qa, qc, res, rule, P_, C_, dir, st)) { ok = 0; break; }
+                if (!edge_free_tree(r, e, np, pairs, thr, qa, qc, o->tr, res, rule, P_, C_, dir, st)) { ok = 0; break; }
                 if (k < n_ext) {
                     if (o->n_chain == o->chain_cap) {
                         o->chain_cap *= 2;
