@@ -146,6 +146,15 @@ GBMP_API gbmp_status gbmp_env_counts(gbmp_env env, int32_t *n_spheres, int32_t *
 GBMP_API gbmp_status gbmp_fk(gbmp_robot robot, const float *d_q, int64_t n, float *d_poses,
                     float *d_centers, void *stream);
 
+/* Space Jacobian of every link, replacing SingleArmStates::calculateSpaceJacobian
+ * (SingleArmStates.cu:223-338, :793-817): d_jac [n*L*L*6], state s, link i, joint j at
+ * ((s * L + i) * L + j) * 6: for a revolute joint j <= i (j > 0, i > 0) the column
+ * (w, w x (p_i - p_j)) with w the joint's axis in the base frame and p the link
+ * positions, for a prismatic one (0, w), otherwise zero (joint order decides, as in the
+ * reference). */
+GBMP_API gbmp_status gbmp_space_jacobian(gbmp_robot robot, const float *d_q, int64_t n, float *d_jac,
+                                         void *stream);
+
 /* Collision check of n states, replacing SingleArmSpace::checkStates
  * (SingleArmSpace.cu:1572-1602) with the four collision constraints
  * (SelfCollisionConstraint.cu:60-133, EnvConstraintSphere.cu:35-117,

@@ -206,6 +206,14 @@ class SingleArmStates {
     std::vector<std::vector<float>> getJointStatesHost() const;
     std::vector<std::vector<std::vector<float>>> getLinkPosesInBaseLinkHost();
     std::vector<std::vector<std::vector<float>>> getSelfCollisionSpheresPosInBaseLinkHost();
+    // Space Jacobians of every link (SingleArmStates::calculateSpaceJacobian,
+    // SingleArmStates.cu:793-817, kernel :223-338), kept on the device.
+    void calculateSpaceJacobian(bool synchronize = true);
+    // One link's space Jacobian per state, [n][joints][6] (the reference returns an
+    // Eigen matrix joints x 6 per state, SingleArmStates.cu:999-1039); computed first
+    // if calculateSpaceJacobian has not been called; std::runtime_error for an unknown
+    // link name.
+    std::vector<std::vector<std::vector<float>>> getSpaceJacobianInBaseLinkHost(const std::string &link_name);
     std::vector<float> getTotalCostsHost() const;
     std::vector<std::vector<float>> getCostsHost() const;   // [n][constraints]
     // Keep the states whose flag is true (BaseStates::filterStates, base/States.h:83-140).
@@ -217,7 +225,7 @@ class SingleArmStates {
     int n_, L_, S_;
     bool valid_ = true, updated_ = false;
     const SingleArmSpace *space_;
-    std::shared_ptr<detail::DevArray> q_, costs_, total_, poses_, centers_;
+    std::shared_ptr<detail::DevArray> q_, costs_, total_, poses_, centers_, jac_;
 };
 typedef std::shared_ptr<SingleArmStates> SingleArmStatesPtr;
 typedef SingleArmStatesPtr BaseStatesPtr;
@@ -291,6 +299,13 @@ class SingleArmSpace {
     size_t getDim() const { return dim_; }
     int getNumOfJoints() const { return L_; }
     gbmp_robot robot() const { return robot_; }
+    // Index of a link by name; std::runtime_error("Link <name> not found in the space") if
+    // there is none (the reference's lookup, SingleArmStates.cu:1003-1016).
+    int getLinkIndex(const std::string &link_name) const {
+        for (size_t i = 0; i < link_names_.size(); ++i)
+            if (link_names_[i] == link_name) return (int)i;
+        throw std::runtime_error("Link " + link_name + " not found in the space");
+    }
     gbmp_env env() const { return env_; }
     int numConstraints() const { return (int)constraints_.size(); }
 
@@ -682,6 +697,28 @@ inline std::vector<std::vector<std::vector<float>>> SingleArmStates::getSelfColl
     for (int i = 0; i < n_; ++i)
         for (int k = 0; k < S_; ++k)
             out[i][k].assign(flat.begin() + ((size_t)i * S_ + k) * 3, flat.begin() + ((size_t)i * S_ + k + 1) * 3);
+    return out;
+}
+
+inline void SingleArmStates::calculateSpaceJacobian(bool synchronize) {
+    if (n_ == 0) return;
+    jac_ = std::make_shared<detail::DevArray>(sizeof(float) * (size_t)n_ * L_ * L_ * 6);
+    if (!jac_->ok()) { valid_ = false; return; }
+    detail::check(gbmp_space_jacobian(space_->robot(), getJointStatesCuda(), n_, static_cast<float *>(jac_->p),
+                                      nullptr));
+    if (synchronize) cudaDeviceSynchronize();
+}
+
+inline std::vector<std::vector<std::vector<float>>>
+SingleArmStates::getSpaceJacobianInBaseLinkHost(const std::string &link_name) {
+    const int li = space_->getLinkIndex(link_name);
+    if (!jac_ && n_) calculateSpaceJacobian(true);
+    std::vector<float> flat((size_t)n_ * L_ * L_ * 6);
+    if (n_) cudaMemcpy(flat.data(), jac_->p, sizeof(float) * flat.size(), cudaMemcpyDeviceToHost);
+    std::vector<std::vector<std::vector<float>>> out(n_, std::vector<std::vector<float>>(L_, std::vector<float>(6)));
+    for (int i = 0; i < n_; ++i)
+        for (int j = 0; j < L_; ++j)
+            for (int k = 0; k < 6; ++k) out[i][j][k] = flat[(((size_t)i * L_ + li) * L_ + j) * 6 + k];
     return out;
 }
 

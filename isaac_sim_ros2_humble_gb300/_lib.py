@@ -114,6 +114,7 @@ SIGNATURES = {
     "gbmp_fk": [_vp, _vp, _i64, _vp, _vp, _vp],
     "gbmp_check_states": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp],
     "gbmp_check_states_fk": [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
+    "gbmp_space_jacobian": [_vp, _vp, _i64, _vp, _vp],
     "gbmp_check_batch_create": [_i32, C.POINTER(_vp)],
     "gbmp_check_batch_run": [_vp, C.POINTER(CheckRequest), _i32, _i32, _vp],
     "gbmp_check_batch_destroy": [_vp],

@@ -119,6 +119,13 @@ def fk(robot: Robot, q, poses=None, centers=None, stream=None):
     check(_lib.load().gbmp_fk(robot.handle, ptr(q), n, ptr(poses), ptr(centers), stream_handle(stream)))
 
 
+def space_jacobian(robot: Robot, q, jac, stream=None):
+    """Space Jacobian of every link of the states q [n, L] into jac [n, L, L, 6]
+    (gbmp_space_jacobian)."""
+    n = _n(q, robot.L)
+    check(_lib.load().gbmp_space_jacobian(robot.handle, ptr(q), n, ptr(jac), stream_handle(stream)))
+
+
 def check_states(robot: Robot, env: Env, q, verdict=None, costs=None, total=None, mode=_lib.CHECK_VERDICT,
                  stream=None, poses=None, centers=None):
     """Collision check of the states q [n, L]; with poses [n, L, 4, 4] and / or

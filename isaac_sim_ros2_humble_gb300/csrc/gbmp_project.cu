@@ -384,6 +384,80 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
 
 using namespace gbmp;
 
+// Space Jacobian of every link (SingleArmStates::calculateSpaceJacobian with
+// kin_space_jacobian_per_link_kernel, SingleArmStates.cu:223-338, :793-817): for link i
+// and joint j, w = R_j a_j (a_j the joint's axis as given, R_j the rotation of link j's
+// pose) and p the pose positions; column j is (w, w x (p_i - p_j)) for a revolute
+// joint, (0, w) for a prismatic one, and zero for link 0, joint 0, j > i and other joint
+// types (joint order, not ancestry, as the reference has it).  Output [n][L][L][6]
+// (state, link, joint, column).  One warp per state: FK, then the lanes over (i, j).
+__global__ void __launch_bounds__(kWarpsPerBlock *kWarp)
+    k_space_jacobian(DevRobot R, const float *__restrict__ q, long long n, float *__restrict__ jac) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    DevEnv E0{0, 0, 0, nullptr};
+    SmemTables t = carve_tables(smem, R, 0);
+    if (!stage_tables(R, E0, t, 0)) return;
+    const int warp = threadIdx.x / kWarp, lane = threadIdx.x & 31;
+    WarpScratch w = carve_warp(smem + smem_tables_bytes(R, 0), R, warp);
+    __syncthreads();
+    const int L = R.L;
+    const long long nw = (long long)gridDim.x * kWarpsPerBlock;
+    for (long long s = blockIdx.x * (long long)kWarpsPerBlock + warp; s < n; s += nw) {
+        for (int j = lane; j < L; j += kWarp) w.q[j] = q[s * L + j];
+        __syncwarp();
+        warp_fk(t, L, w, lane);
+        float *out = jac + s * L * L * 6;
+        for (int e = lane; e < L * L; e += kWarp) {
+            const int i = e / L, j = e - i * L;
+            float c[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            const int ty = t.type[j];
+            if (i > 0 && j > 0 && j <= i && (ty == 1 || ty == 2)) {
+                const float *Tj = w.lp + 12 * j, *Ti = w.lp + 12 * i;
+                const float *a = t.axr + 4 * j;
+                const float w0 = dot3(Tj[0], Tj[1], Tj[2], a[0], a[1], a[2]);
+                const float w1 = dot3(Tj[4], Tj[5], Tj[6], a[0], a[1], a[2]);
+                const float w2 = dot3(Tj[8], Tj[9], Tj[10], a[0], a[1], a[2]);
+                if (ty == 1) {
+                    const float d0 = __fadd_rn(Ti[3], -Tj[3]), d1 = __fadd_rn(Ti[7], -Tj[7]),
+                                d2 = __fadd_rn(Ti[11], -Tj[11]);
+                    c[0] = w0; c[1] = w1; c[2] = w2;
+                    c[3] = __fadd_rn(__fmul_rn(w1, d2), -__fmul_rn(w2, d1));
+                    c[4] = __fadd_rn(__fmul_rn(w2, d0), -__fmul_rn(w0, d2));
+                    c[5] = __fadd_rn(__fmul_rn(w0, d1), -__fmul_rn(w1, d0));
+                } else {
+                    c[3] = w0; c[4] = w1; c[5] = w2;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 6; ++k) out[6 * e + k] = c[k];
+        }
+        __syncwarp();
+    }
+}
+
+extern "C" gbmp_status gbmp_space_jacobian(gbmp_robot r, const float *d_q, int64_t n, float *d_jac, void *stream) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    GBMP_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return GBMP_OK;
+    GBMP_CHECK_ARG(d_q && d_jac, "q/jacobian is NULL");
+    const size_t smem = smem_tables_bytes(r->dev, 0) + smem_warp_bytes(r->dev) * kWarpsPerBlock;
+    gbmp_status so = ensure_smem_optin((const void *)k_space_jacobian);
+    if (so) return so;
+    int per_sm = 0;
+    GBMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_space_jacobian, kWarpsPerBlock * kWarp, smem));
+    if (per_sm < 1) {
+        set_error("Jacobian kernel does not fit on an SM (%zu bytes of shared memory)", smem);
+        return GBMP_ERR_CAPACITY;
+    }
+    long long grid = (long long)per_sm * r->num_sms;
+    const long long need = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (need < grid) grid = need;
+    ProfScope ps(GBMP_PROF_OTHER, (cudaStream_t)stream);
+    k_space_jacobian<<<(unsigned)grid, kWarpsPerBlock * kWarp, smem, (cudaStream_t)stream>>>(r->dev, d_q, n, d_jac);
+    GBMP_CUDA(cudaGetLastError());
+    return GBMP_OK;
+}
+
 extern "C" gbmp_status gbmp_project_states(gbmp_robot r, const gbmp_projection *proj, float *d_q, int64_t n,
                                            float *d_task_cost, float *d_bound_cost, void *stream) {
     GBMP_CHECK_ARG(r && proj, "robot/projection is NULL");

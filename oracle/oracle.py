@@ -165,6 +165,31 @@ class OracleModel:
             lib().or_fk_f32(C.byref(self.r), _c(q, np.float32), n, out)
         return out
 
+    def space_jacobian(self, q, f64=True):
+        """Space Jacobian of every link, [n, L, L, 6] (state, link, joint, column), from
+        the oracle's FK (FP64 by default): the reference's kin_space_jacobian_per_link_kernel
+        (SingleArmStates.cu:223-338) restated in numpy -- for link i and joint j, w = R_j
+        a_j with a_j the joint axis as given; a revolute column is (w, w x (p_i - p_j)), a
+        prismatic one (0, w); link 0, joint 0, j > i and other joint types give zeros."""
+        P = self.fk(q, f64=f64)
+        n, L = P.shape[0], self.L
+        dt = np.float64 if f64 else np.float32
+        R = P[:, :, [0, 1, 2, 4, 5, 6, 8, 9, 10]].reshape(n, L, 3, 3).astype(dt)
+        p = P[:, :, [3, 7, 11]].astype(dt)
+        axes = np.asarray(self.robot.joint_axes, dt).reshape(L, 3)
+        types = np.asarray(self.robot.joint_types).reshape(L)
+        w = np.einsum("njab,jb->nja", R, axes)            # [n, L(joint), 3]
+        out = np.zeros((n, L, L, 6), dt)
+        for i in range(1, L):
+            for j in range(1, i + 1):
+                if types[j] == 1:
+                    d = p[:, i] - p[:, j]
+                    out[:, i, j, :3] = w[:, j]
+                    out[:, i, j, 3:] = np.cross(w[:, j], d)
+                elif types[j] == 2:
+                    out[:, i, j, 3:] = w[:, j]
+        return out
+
     def sphere_centers(self, poses):
         n = poses.shape[0]
         if poses.dtype == np.float64:

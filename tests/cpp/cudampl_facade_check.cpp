@@ -140,6 +140,19 @@ int main(int argc, char **argv) {
         for (auto &state : st->getLinkPosesInBaseLinkHost())
             for (auto &pose : state) lp.insert(lp.end(), pose.begin(), pose.end());
         out.flat("poses", lp);
+        // space Jacobian of the last link, and an unknown link name rejected
+        st->calculateSpaceJacobian();
+        std::vector<float> jl;
+        for (auto &state : st->getSpaceJacobianInBaseLinkHost("link" + std::to_string(L - 1)))
+            for (auto &col : state) jl.insert(jl.end(), col.begin(), col.end());
+        out.flat("jacobian_last", jl);
+        bool threw = false;
+        try {
+            st->getSpaceJacobianInBaseLinkHost("no_such_link");
+        } catch (const std::runtime_error &) {
+            threw = true;
+        }
+        if (!threw) throw std::runtime_error("unknown link name accepted");
 
         auto s1 = space->createStatesFromVector(e_from), s2 = space->createStatesFromVector(e_to);
         std::vector<bool> mf;

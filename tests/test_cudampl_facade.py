@@ -121,6 +121,8 @@ def test_facade_matches_oracle(tmp_path):
     np.testing.assert_allclose(got["costs"].reshape(n, 4), oc.T, rtol=1e-4, atol=2e-5)
     p64 = m.fk(states.astype(np.float64), f64=True)
     assert np.abs(got["poses"].reshape(n, L, 16) - p64).max() < 1e-5
+    jac = m.space_jacobian(states)[:, L - 1]          # [n, joints, 6]
+    assert np.abs(got["jacobian_last"].reshape(n, L, 6) - jac).max() < 2e-5
 
     o_ok, o_fh, o_ns, o_ln = m.check_motions(e_from, e_to, RES, 0)
     ok = got["motion_ok"].astype(bool)

@@ -466,3 +466,24 @@ def test_slab_contact_just_outside_the_band_is_a_collision():
     ok, fh, _, ns = _run_edges(R, E, prev, q, 0.01, 1)
     o_ok, o_fh, o_ns, _ = m.check_motions(prev, q, 0.01, 1)
     assert ns[0] == o_ns[0] and fh[0] == o_fh[0] and not ok[0]
+
+
+def test_space_jacobian_matches_the_oracle(plain, edge):
+    """gbmp_space_jacobian (SingleArmStates::calculateSpaceJacobian): every link's 6 x L
+    space Jacobian within 2e-5 of the FP64 oracle restatement of the reference kernel, on
+    the 7-DOF revolute arm, the prismatic-torso arm and a branching tree with fixed and
+    prismatic joints; the columns the reference leaves zero are exactly zero."""
+    cases = [(plain[0], plain[2][:512], plain[4]), (edge[0], edge[2][:512], edge[5])]
+    tree = W.tree_robot(3)
+    cases.append((tree, tree.sample_full(np.random.default_rng(5), 256), api.Robot(tree)))
+    for robot, q, R in cases:
+        n, L = q.shape[0], robot.num_links
+        jac = torch.full((n, L, L, 6), float("nan"), device="cuda")
+        api.space_jacobian(R, dev(q), jac)
+        torch.cuda.synchronize()
+        g = jac.cpu().numpy()
+        o = O.OracleModel(robot).space_jacobian(q)
+        assert np.abs(g - o).max() < 2e-5, np.abs(g - o).max()
+        zero = o == 0
+        assert np.all(g[zero] == 0)
+        assert np.abs(g).max() > 0.1
