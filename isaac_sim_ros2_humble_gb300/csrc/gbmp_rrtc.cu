@@ -276,7 +276,7 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     DevRobot DR = r->dev;
     DR.work = nullptr;
     const int nwords = env_words(E.ns, E.nb, E.nc);
-    const size_t smem = smem_tables_bytes(DR, nwords) + smem_warp_bytes(DR) * kRrtcWarps + 6 * kMaxLinks * 4 + 256;
+    const size_t smem = rrtc_block_smem(DR, nwords, false);
     RrtcParams prm;
     prm.lanes = s->lanes;
     prm.max_iters = s->max_iters;
@@ -646,8 +646,7 @@ gbmp_status batch_begin(gbmp_batch_planner b, int n, const gbmp_rrtc_problem *pr
         const DevEnv E = pr.env->dev();
         spl = std::max(spl, R.spl);
         cull = cull && R.cull;
-        smem = std::max(smem, smem_tables_bytes(R, env_words(E.ns, E.nb, E.nc)) + smem_warp_bytes(R) * kRrtcWarps +
-                                  6 * kMaxLinks * 4 + 256);
+        smem = std::max(smem, rrtc_block_smem(R, env_words(E.ns, E.nb, E.nc), true));
         BatchProblem &bp = b->h_table[i];
         bp.R = R;
         bp.R.work = nullptr;

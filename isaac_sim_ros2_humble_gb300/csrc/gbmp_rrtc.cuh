@@ -4,12 +4,26 @@
 // translation units so that they compile in parallel.
 #pragma once
 
+#include "gbmp_chunk_device.cuh"
 #include "gbmp_internal.h"
 
 namespace gbmp {
 
 constexpr int kRrtcWarps = 4;
 constexpr int kRrtcThreads = kRrtcWarps * kWarp;
+// States per chunk of the planner's edge checks: an extension of at most `range` has a
+// dozen states or so, split over the lane's four warps, so chunks stay small (and so
+// does the per-warp chunk scratch in shared memory).
+constexpr int kRrtcChunk = 4;
+
+// Shared memory of a planning block: staged tables, four warp scratches, the lane's
+// joint vectors and flags, and, when the edge checks run by chunks (batched planning,
+// robots of at most 32 sphere groups), four chunk scratches.
+__host__ __device__ inline size_t rrtc_misc_bytes() { return align16(6 * kMaxLinks * 4 + 256); }
+__host__ __device__ inline size_t rrtc_block_smem(const DevRobot &R, int nwords, bool chunks) {
+    return smem_tables_bytes(R, nwords) + smem_warp_bytes(R) * kRrtcWarps + rrtc_misc_bytes() +
+           (chunks && R.cull ? smem_chunk_bytes(R, kRrtcChunk) * kRrtcWarps : 0);
+}
 
 enum : int { kStRunning = 0, kStSolved = 1, kStNodeCap = 2, kStIterCap = 3, kStDeadline = 4 };
 
