@@ -194,7 +194,7 @@ __device__ __forceinline__ float3 xform_point_a16(const float *T, float x, float
 template <int SPL, bool CNT>
 __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                    const ChunkScratch &cs, const float *lp, int ns_end, int nb_end, int nc_end,
-                                   unsigned need, int npr, bool pairs_overflow, int nn, int lane,
+                                   unsigned need, unsigned pneed, int npr, bool pairs_overflow, int nn, int lane,
                                    unsigned long long &fl) {
     constexpr bool count = CNT;   // executed-work accounting compiled in only when asked for
     float cx[SPL], cy[SPL], cz[SPL], cr[SPL], A[SPL];
@@ -211,14 +211,14 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             const float3 p = xform_point_a16(lp + 12 * t.slink[k], s.x, s.y, s.z);
             cx[m] = p.x; cy[m] = p.y; cz[m] = p.z; cr[m] = s.w;
             gbit[m] = 1u << t.sgrp[k];
-            w.cen[k] = make_float4(p.x, p.y, p.z, s.w);
+            if (pneed & gbit[m]) w.cen[k] = make_float4(p.x, p.y, p.z, s.w);   // only self pairs read it
         } else {
             cx[m] = kFar; cy[m] = kFar; cz[m] = kFar; cr[m] = 0.f;
             gbit[m] = 0u;
         }
         A[m] = __fmaf_rn(cz[m], cz[m], __fmaf_rn(cy[m], cy[m], __fmaf_rn(cx[m], cx[m], -cr[m] * cr[m])));
     }
-    if (lane < R.G && ((need >> lane) & 1u)) {
+    if (lane < R.G && ((pneed >> lane) & 1u)) {
         const float4 g = t.grp[lane];
         const float3 c = xform_point_a16(lp + 12 * t.glink[lane], g.x, g.y, g.z);
         w.gb[lane] = make_float4(c.x, c.y, c.z, g.w);
@@ -241,7 +241,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             if (count) fl += (unsigned long long)__popc(__ballot_sync(kFull, (cm & gbit[m]) != 0u)) * kFlSphereX;
         }
     }
-    if (__any_sync(kFull, hit)) return true;
+    if (ns_end > 0 && __any_sync(kFull, hit)) return true;
 
     // --- cuboids ---
     const float4 *bx = t.env + E.ns;
@@ -261,7 +261,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             }
         }
     }
-    if (__any_sync(kFull, hit)) return true;
+    if (nb_end > ns_end && __any_sync(kFull, hit)) return true;
 
     // --- cylinders ---
     const float4 *cyl = t.env + E.ns + 5 * E.nb;
@@ -283,7 +283,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             }
         }
     }
-    if (__any_sync(kFull, hit)) return true;
+    if (nc_end > nb_end && __any_sync(kFull, hit)) return true;
 
     // --- self collision: listed group pairs whose per-state bounding spheres overlap ---
     const int nlist = pairs_overflow ? R.NPL : npr;
@@ -298,7 +298,7 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
             const float rr = a.w + b.w;
             // (with pairs_overflow every enabled pair is walked; a group outside `need`
             // has no sphere placed this state, and its pairs cannot touch in this chunk)
-            on = ((need >> lpr.x) & (need >> lpr.y) & 1u) && sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
+            on = ((pneed >> lpr.x) & (pneed >> lpr.y) & 1u) && sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
             ga = lpr.x;
             gb = lpr.y;
             p0 = lpr.z;
@@ -498,6 +498,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     const int ns_end = nsph, nb_end = nsph + nbox;
     // enabled group pairs whose swept spheres overlap
     int npr = 0;
+    unsigned pneed = 0u;
     for (int k0 = 0; k0 < R.NPL; k0 += kWarp) {
         const int k = k0 + lane;
         bool on = false;
@@ -506,7 +507,7 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
             const float4 a = cs.sgb[lpr.x], b = cs.sgb[lpr.y];
             const float rr = a.w + b.w;
             on = sq3(a.x - b.x, a.y - b.y, a.z - b.z) < rr * rr;
-            if (on) need |= (1u << lpr.x) | (1u << lpr.y);
+            if (on) pneed |= (1u << lpr.x) | (1u << lpr.y);
         }
         const unsigned bal = __ballot_sync(kFull, on);
         if (on) {
@@ -516,7 +517,8 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
         npr += __popc(bal);
         if (count) fl += (unsigned long long)min(kWarp, R.NPL - k0) * kFlGroupPair;
     }
-    need = __reduce_or_sync(kFull, need);
+    pneed = __reduce_or_sync(kFull, pneed);
+    need = __reduce_or_sync(kFull, need) | pneed;
     __syncwarp();
     const bool overflow = nc > kChunkCands;
     const bool pairs_overflow = npr > kChunkPairs;
@@ -549,8 +551,8 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
         if (overflow) {
             hit = chunk_fallback<SPL>(t, R, E, w, lp, lane);
         } else {
-            hit = chunk_state<SPL, CNT>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, npr, pairs_overflow, nn, lane,
-                                        fl);
+            hit = chunk_state<SPL, CNT>(t, R, E, w, cs, lp, ns_end, nb_end, nc, need, pneed, npr, pairs_overflow, nn,
+                                        lane, fl);
         }
         __syncwarp();
         if (hit) {
