@@ -321,20 +321,21 @@ __device__ inline bool chunk_state(const SmemTables &t, const DevRobot &R, const
                 const float4 GA = w.gb[xa], GB = w.gb[xb];
                 bool ia = false, ib = false;
                 float4 cj = make_float4(kFar, kFar, kFar, 0.f), c = cj;
-                if (lane < na) {
-                    c = w.cen[t.gsl[a0 + lane]];
-                    const float rr = c.w + GB.w;
-                    ia = sq3(c.x - GB.x, c.y - GB.y, c.z - GB.z) < rr * rr;
-                }
+                // b's spheres against a's group sphere first: when none touches it, no
+                // pair of this group pair can touch and a's spheres are not loaded
                 if (lane < nb) {
                     cj = w.cen[t.gsl[b0 + lane]];
                     const float rr = cj.w + GA.w;
                     ib = sq3(cj.x - GA.x, cj.y - GA.y, cj.z - GA.z) < rr * rr;
                 }
-                unsigned ma = __ballot_sync(kFull, ia);
                 const unsigned mb = __ballot_sync(kFull, ib);
-                if (count) fl += (unsigned long long)(na + nb + __popc(ma) * __popc(mb)) * kFlSelf;
-                if (!mb) ma = 0u;
+                if (mb && lane < na) {
+                    c = w.cen[t.gsl[a0 + lane]];
+                    const float rr = c.w + GB.w;
+                    ia = sq3(c.x - GB.x, c.y - GB.y, c.z - GB.z) < rr * rr;
+                }
+                unsigned ma = __ballot_sync(kFull, ia);
+                if (count) fl += (unsigned long long)(nb + (mb ? na : 0) + __popc(ma) * __popc(mb)) * kFlSelf;
                 while (ma) {
                     const int x = __ffs(ma) - 1;
                     ma &= ma - 1u;
