@@ -78,8 +78,10 @@ __global__ void k_rrtc_batch_finish(BatchProblem *__restrict__ probs, int n) {
     probs[p].prev[1] = min(probs[p].P.size[1], probs[p].P.cap) * probs[p].P.stride;
 }
 
-__global__ void k_read_clock(unsigned long long *t) {
-    if (threadIdx.x == 0) *t = global_ns();
+// The single-problem deadline, set on the device just before the planning launch (no
+// host round trip to read the device clock).
+__global__ void k_set_deadline(unsigned long long *deadline, unsigned long long limit_ns) {
+    if (threadIdx.x == 0) *deadline = global_ns() + limit_ns;
 }
 
 // Walk both parent chains into the path (start tree root first).  One thread.
@@ -181,6 +183,13 @@ struct gbmp_planner_s {
     int cap = 0, stride = 0, path_cap = 0;
     void *block = nullptr;
     RrtcDev dev{};
+    // tree slots written since the last reset, per tree (all of them after creation or an
+    // interrupted solve): only these are re-poisoned before the next solve
+    int dirty[2] = {0, 0}, dirty_radii[2] = {0, 0};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the traced path goes straight to pinned host memory (the trace kernel writes it
+    // through the mapped pointer), so reading a result takes one synchronisation
+    float *h_path = nullptr;
 };
 
 extern "C" {
@@ -199,7 +208,7 @@ gbmp_status gbmp_planner_create(gbmp_robot r, int32_t max_nodes, int32_t path_ca
     const size_t par_b = align16(sizeof(int) * (size_t)max_nodes);
     const size_t path_b = align16(sizeof(float) * (size_t)path_cap * r->L);
     const size_t rad_b = align16(sizeof(float) * (size_t)max_nodes);   // dynamic-domain radii, per tree
-    const size_t bytes = 2 * nodes_b + 2 * par_b + 256 + path_b + 2 * rad_b;
+    const size_t bytes = 2 * nodes_b + 2 * par_b + 256 + 2 * rad_b;
     cudaError_t e = cudaMalloc(&p->block, bytes);
     if (e != cudaSuccess) {
         delete p;
@@ -212,16 +221,28 @@ gbmp_status gbmp_planner_create(gbmp_robot r, int32_t max_nodes, int32_t path_ca
     D.parent[0] = (int *)(b + 2 * nodes_b); D.parent[1] = (int *)(b + 2 * nodes_b + par_b);
     int *ints = (int *)(b + 2 * nodes_b + 2 * par_b);
     D.size = ints; D.state = ints + 4; D.path_len = ints + 16;
-    D.path = (float *)(b + 2 * nodes_b + 2 * par_b + 256);
     D.cap = max_nodes; D.stride = p->stride; D.path_cap = path_cap;
-    D.radii[0] = (float *)(b + 2 * nodes_b + 2 * par_b + 256 + path_b);
-    D.radii[1] = (float *)(b + 2 * nodes_b + 2 * par_b + 256 + path_b + rad_b);
+    D.radii[0] = (float *)(b + 2 * nodes_b + 2 * par_b + 256);
+    D.radii[1] = (float *)(b + 2 * nodes_b + 2 * par_b + 256 + rad_b);
+    p->dirty[0] = p->dirty[1] = p->dirty_radii[0] = p->dirty_radii[1] = max_nodes;
+    void *mapped = nullptr;
+    if (cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess ||
+        cudaHostAlloc((void **)&p->h_path, path_b, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&mapped, p->h_path, 0) != cudaSuccess) {
+        gbmp_planner_destroy(p);
+        set_error("planner events or pinned path buffer could not be created");
+        return GBMP_ERR_CUDA;
+    }
+    D.path = static_cast<float *>(mapped);
     *out = p;
     return GBMP_OK;
 }
 
 gbmp_status gbmp_planner_destroy(gbmp_planner p) {
     if (!p) return GBMP_OK;
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->h_path) cudaFreeHost(p->h_path);
     if (p->block) cudaFree(p->block);
     delete p;
     return GBMP_OK;
@@ -254,14 +275,22 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     memset(res, 0, sizeof *res);
     cudaStream_t st = (cudaStream_t)stream;
     const RrtcDev &D = p->dev;
-    // reset: NaN sentinels, counters, roots (RobotSolver.cu:361-388 with a float sentinel)
-    GBMP_CUDA(cudaMemsetAsync(D.nodes[0], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
-    GBMP_CUDA(cudaMemsetAsync(D.nodes[1], 0xff, sizeof(float) * (size_t)p->cap * p->stride, st));
+    // reset: NaN sentinels, counters, roots (RobotSolver.cu:361-388 with a float sentinel);
+    // only the slots written since the last reset (a solve of a 1,000,000-node planner
+    // otherwise re-poisons 64 MB of trees)
+    for (int t = 0; t < 2; ++t)
+        if (p->dirty[t] > 0)
+            GBMP_CUDA(cudaMemsetAsync(D.nodes[t], 0xff, sizeof(float) * (size_t)p->dirty[t] * p->stride, st));
     GBMP_CUDA(cudaMemsetAsync(D.size, 0, 256, st));
     if (s->dynamic_domain) {   // every radius unset (kRadiusUnset = bytes 0x7f)
-        GBMP_CUDA(cudaMemsetAsync(D.radii[0], 0x7f, sizeof(float) * (size_t)p->cap, st));
-        GBMP_CUDA(cudaMemsetAsync(D.radii[1], 0x7f, sizeof(float) * (size_t)p->cap, st));
+        for (int t = 0; t < 2; ++t)
+            if (p->dirty_radii[t] > 0)
+                GBMP_CUDA(cudaMemsetAsync(D.radii[t], 0x7f, sizeof(float) * (size_t)p->dirty_radii[t], st));
+        p->dirty_radii[0] = p->dirty_radii[1] = 0;
     }
+    // until this solve's tree sizes are read back, every slot counts as written
+    p->dirty[0] = p->dirty[1] = p->cap;
+    if (s->dynamic_domain) p->dirty_radii[0] = p->dirty_radii[1] = p->cap;
     // the goal tree starts with every goal as a root (a node that is its own parent)
     std::vector<int> h_init{1, n_goals}, h_roots(n_goals);
     for (int g = 0; g < n_goals; ++g) h_roots[g] = g;
@@ -290,24 +319,17 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     prm.dd_min = s->dd_min_radius;
     prm.balance = balance;
     prm.tree_ratio = tree_ratio;
-    // device deadline from the host clock offset: read %globaltimer through a 1-thread probe
-    unsigned long long now_ns = 0;
-    {
-        unsigned long long *d_t = (unsigned long long *)(D.state + 8);
-        {
-            ProfScope ps(GBMP_PROF_OTHER, st);
-            k_read_clock<<<1, 32, 0, st>>>(d_t);
-        }
-        GBMP_CUDA(cudaGetLastError());
-        GBMP_CUDA(cudaMemcpyAsync(&now_ns, d_t, sizeof now_ns, cudaMemcpyDeviceToHost, st));
-        GBMP_CUDA(cudaStreamSynchronize(st));
-    }
+    // device deadline: the device clock at the launch plus the limit, set on the device
     const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
-    prm.deadline_ns = now_ns + (unsigned long long)(lim * 1e9);
-    prm.deadline_ptr = nullptr;
-    cudaEvent_t e0, e1;
-    GBMP_CUDA(cudaEventCreate(&e0));
-    GBMP_CUDA(cudaEventCreate(&e1));
+    unsigned long long *d_deadline = (unsigned long long *)(D.state + 8);
+    {
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        k_set_deadline<<<1, 32, 0, st>>>(d_deadline, (unsigned long long)(lim * 1e9));
+    }
+    GBMP_CUDA(cudaGetLastError());
+    prm.deadline_ns = 0;
+    prm.deadline_ptr = d_deadline;
+    cudaEvent_t e0 = p->ev0, e1 = p->ev1;
     GBMP_CUDA(cudaEventRecord(e0, st));
     gbmp_status stt = GBMP_OK;
     {
@@ -335,8 +357,12 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     GBMP_CUDA(cudaStreamSynchronize(st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    p->dirty[0] = std::min(std::max(h_size[0], 1), p->cap);
+    p->dirty[1] = std::min(std::max(h_size[1], n_goals), p->cap);
+    if (s->dynamic_domain) {
+        p->dirty_radii[0] = p->dirty[0];
+        p->dirty_radii[1] = p->dirty[1];
+    }
     res->status = h_state[0];
     res->solved = h_state[0] == kStSolved;
     res->start_tree_size = std::min(h_size[0], p->cap);
@@ -350,7 +376,7 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
             set_error("path of %d states does not fit the buffer of %d", res->path_len, path_cap);
             return GBMP_ERR_CAPACITY;
         }
-        GBMP_CUDA(cudaMemcpy(h_path, D.path, sizeof(float) * (size_t)h_len * L, cudaMemcpyDeviceToHost));
+        memcpy(h_path, p->h_path, sizeof(float) * (size_t)h_len * L);   // written by the trace, before the sync
         res->path_len = h_len;
         double cost = 0.0;
         for (int k = 1; k < h_len; ++k) {
