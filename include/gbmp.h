@@ -216,11 +216,16 @@ GBMP_API gbmp_status gbmp_check_batch_destroy(gbmp_check_batch batch);
  * resolution.  Asynchronous: three launches on `stream`, no host synchronisation (the
  * reference reads step counts back to the host, SingleArmSpace.cu:728-739).  The working
  * memory belongs to the robot handle: calls with one robot on different streams must be
- * ordered by the caller.  Each edge is validated by one warp, state order, stopping at its
- * first colliding state; the edges are taken longest first.  Robots of up to 32
- * sphere-carrying links are validated by chunks of consecutive states (the first 4
- * states, then 10 at a time; 4 for robots of more than 16 links), others state by state;
- * gbmp_robot_set_edge_form overrides the form for one robot handle. */
+ * ordered by the caller.  Each edge is validated by one warp, stopping at a colliding
+ * state; the edges are taken longest first.  Robots of up to 32 sphere-carrying links are
+ * validated by chunks of consecutive states (10 states; 4 for robots of more than 16
+ * links), others state by state; gbmp_robot_set_edge_form overrides the form for one
+ * robot handle.  With d_first_hit the chunks go in state order (the first 4 states, then
+ * the chunks in turn) and the edge stops at its lowest colliding state.  Without it (the
+ * reference's outputs: verdict and cost) the chunks go coarse to fine -- the first 4
+ * states, the last chunk, then the chunks between in 8 interleaved passes -- and the
+ * edge stops at the first colliding state met: the same verdicts, fewer states checked
+ * on colliding edges. */
 #define GBMP_STEP_L2 0
 #define GBMP_STEP_LINF 1
 /* pRRTC's `granularity` (pRRTC/src/planning/pRRTC.cu:430-440): every edge is checked at

@@ -12,11 +12,54 @@ constexpr int kChunkWarps = 8;
 
 // Edge validation by chunks: a warp takes the next edge of `order` (a shared counter; the
 // edges come longest first, so the last edges taken are the shortest and the warps end
-// together), walks its states in chunks -- the first 4 states, then K at a time -- and
-// stops at the first colliding state.  One warp per edge, so no state past the edge's
-// first hit is placed in a later chunk.  Writes the edge's outputs (ok, first hit; -2 for
-// an edge too long to validate).
+// together), walks its states in chunks of consecutive states and stops at the first chunk
+// that holds a colliding state.  One warp per edge, so no state past that hit is placed in
+// a later chunk.  Writes the edge's outputs (ok, first hit; -2 for an edge too long to
+// validate).
+//
+// Two chunk orders.  When the first hit is asked for, state order: the first 4 states,
+// then K at a time, so the hit found is the lowest colliding index.  When only the verdict
+// is (the reference's output), an edge is infeasible as soon as any of its states collides,
+// so the chunks are visited coarse to fine: the first 4 states, the last K, then the
+// K-state chunks between them in kAnyStride interleaved passes (chunks j, j + S, j + 2S, ...
+// for j = 0 .. S-1).  A colliding stretch of the edge longer than S chunks is then met
+// after about 1/S of the states before it, and a goal state that collides after K; a free
+// edge still has every state checked, in either order.  On the 65,536 edges of the 8-DOF
+// benchmark (uniform endpoints, 82 % colliding) the states checked fall from 8.89 M to
+// 4.90 M, 4.19 M of them on the free edges; passes of 4 / 6 / 8 / 16 chunks give 4.97 /
+// 4.91 / 4.90 / 5.02 M.
 constexpr int kFirstChunk = 4;
+constexpr int kAnyStride = 8;
+
+template <int K>
+__device__ __forceinline__ int edge_chunk_count(int n, bool any) {
+    if (n <= kFirstChunk) return 1;
+    if (!any) return 1 + (n - kFirstChunk + K - 1) / K;
+    const int ts = max(kFirstChunk, n - K);   // the last chunk is [ts, n)
+    return 2 + (ts - kFirstChunk + K - 1) / K;
+}
+
+// States [x, y) of chunk `idx` (0 <= idx < edge_chunk_count) of an edge of n states.
+template <int K>
+__device__ __forceinline__ int2 edge_chunk_range(int idx, int n, bool any) {
+    if (idx == 0) return make_int2(0, min(n, kFirstChunk));
+    if (!any) {
+        const int a = kFirstChunk + (idx - 1) * K;
+        return make_int2(a, min(n, a + K));
+    }
+    const int ts = max(kFirstChunk, n - K);
+    if (idx == 1) return make_int2(ts, n);
+    const int nm = (ts - kFirstChunk + K - 1) / K;   // chunks between, [4 + jK, min(ts, 4 + (j + 1)K))
+    int r = idx - 2, p = 0;
+    for (;;) {   // pass p holds chunks p, p + S, ... below nm; r < nm, so p < min(S, nm) at exit
+        const int sz = (nm - p + kAnyStride - 1) / kAnyStride;
+        if (r < sz) break;
+        r -= sz;
+        ++p;
+    }
+    const int a = kFirstChunk + (p + r * kAnyStride) * K;
+    return make_int2(a, min(ts, a + K));
+}
 
 template <int SPL, int K, bool CNT>
 __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
@@ -33,6 +76,7 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
     ChunkScratch cs;
     carve_chunk(smem + smem_tables_bytes(R, nwords), R, K, warp, cs, w);
     const int lane = threadIdx.x & 31;
+    const bool any = first_hit_out == nullptr;
     for (;;) {
         int i = 0;
         if (lane == 0) i = atomicAdd(next, 1);
@@ -45,13 +89,13 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
             hit = -2;   // too long to validate
         } else {
             const long long off = (long long)e * R.L;
-            for (int s0 = 0; s0 < n;) {
-                const int s1 = min(s0 + (s0 == 0 ? kFirstChunk : K), n);
-                const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, s0,
-                                                           s1, n, nullptr);
+            const int nch = edge_chunk_count<K>(n, any);
+            for (int c = 0; c < nch; ++c) {
+                const int2 r = edge_chunk_range<K>(c, n, any);
+                const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, r.x,
+                                                           r.y, n, nullptr);
                 __syncwarp();
                 if (h >= 0) { hit = h; break; }
-                s0 = s1;
             }
         }
         if (lane == 0) {

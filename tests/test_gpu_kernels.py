@@ -326,13 +326,15 @@ def test_many_links_uses_full_path():
                  ns.cpu().numpy())
 
 
-def _run_edges(R, E, qf, qt, res, rule):
+def _run_edges(R, E, qf, qt, res, rule, first_hit=True):
+    """Outputs of one gbmp_check_edges call; without first hits (the verdict-only call,
+    which walks each edge coarse to fine) the returned first hits are all 99."""
     n = qf.shape[0]
     ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
-    fh = torch.zeros(n, dtype=torch.int32, device="cuda")
+    fh = torch.full((n,), 99, dtype=torch.int32, device="cuda")
     ln = torch.zeros(n, device="cuda")
     ns = torch.zeros(n, dtype=torch.int32, device="cuda")
-    api.check_edges(R, E, dev(qf), dev(qt), res, rule, ok, fh, ln, ns)
+    api.check_edges(R, E, dev(qf), dev(qt), res, rule, ok, fh if first_hit else None, ln, ns)
     torch.cuda.synchronize()
     return ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(), ns.cpu().numpy()
 
@@ -376,10 +378,17 @@ def test_edge_forms_agree_on_every_edge_of_the_benchmark_call():
     for form in (1, 4, 10):
         R.set_edge_form(form)
         out[form] = _run_edges(R, E, qf, qt, 0.01, 1)
+        if form > 1:   # verdict only: coarse-to-fine chunk order, the same verdicts
+            out[-form] = _run_edges(R, E, qf, qt, 0.01, 1, first_hit=False)
     R.set_edge_form(0)
     for form in (4, 10):
         for a, b in zip(out[form], out[1]):
             np.testing.assert_array_equal(a, b)
+        vo = out[-form]
+        np.testing.assert_array_equal(vo[0], out[1][0])
+        np.testing.assert_array_equal(vo[2], out[1][2])
+        np.testing.assert_array_equal(vo[3], out[1][3])
+        assert np.all(vo[1] == 99)
     for bad in (3, 8):
         with pytest.raises(_lib.GbmpError):
             R.set_edge_form(bad)
@@ -401,9 +410,11 @@ def test_edge_forms_agree_for_large_sphere_groups(dof, n_spheres):
     for form in (1, 10):
         R.set_edge_form(form)
         out[form] = _run_edges(R, E, qf, qt, 0.02, 1)
+    out[-10] = _run_edges(R, E, qf, qt, 0.02, 1, first_hit=False)
     R.set_edge_form(0)
     for a, b in zip(out[10], out[1]):
         np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[-10][0], out[1][0])
     ok, fh, ln, ns = out[10]
     assert 0 < ok.sum() < len(ok)
     m = O.OracleModel(robot, env)
