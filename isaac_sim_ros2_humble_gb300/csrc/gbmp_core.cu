@@ -153,9 +153,27 @@ __global__ void k_edge_order(const int *__restrict__ nsteps, long long E, const 
     }
 }
 
+// State checked at step c (0 <= c < n) of an edge of n states when only the verdict is
+// asked for: the first state, the last, then the states between in 16 interleaved passes
+// taken in bit-reversed order (offsets 0, 8, 4, 12, 2, ...), so that a colliding stretch
+// of the edge is met after a fraction of the states before it.
+__device__ __forceinline__ int verdict_order_state(int c, int n) {
+    if (c == 0 || n <= 2) return c;
+    if (c == 1) return n - 1;
+    const int m = n - 2;   // states 1 .. n-2
+    int r = c - 2;
+    for (int p = 0;; ++p) {   // r < m, so the pass is found within 16 steps
+        const int o = (int)(__brev((unsigned)p) >> 28);
+        const int sz = (m - o + 15) / 16;
+        if (r < sz) return 1 + o + r * 16;
+        r -= sz;
+    }
+}
+
 // Edge validation state by state (robots with more than 32 sphere groups, and the
 // per-state form of the others): a warp takes the next edge of `order` (a shared
-// counter), walks its states in order and stops at the first colliding state.
+// counter), walks its states -- in order when the first hit is asked for, else in
+// verdict_order_state's order -- and stops at a colliding state.
 template <int SPL, bool CULL>
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, CULL ? 3 : 1)
     k_edge_states(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,
@@ -180,7 +198,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, CULL ? 3 : 1)
             hit = -2;   // too long to validate
         } else {
             const long long off = (long long)e * R.L;
-            for (int s = 0; s < n; ++s) {
+            const bool any = first_hit_out == nullptr;
+            for (int c = 0; c < n; ++c) {
+                const int s = any ? verdict_order_state(c, n) : c;
                 for (int j = lane; j < R.L; j += kWarp)
                     w.q[j] = (s == n - 1) ? to[off + j] : __fmaf_rn(dir[off + j], (float)s, from[off + j]);
                 __syncwarp();

@@ -371,19 +371,21 @@ def test_edge_forms_agree_on_every_edge_of_the_benchmark_call():
     """All 65,536 edges of the benchmark call validated state by state (k_edge_states) and
     by chunks of 4 and 10 states (k_edge_chunk): identical verdicts, first hits, state
     counts and lengths on every edge (the chunk form's narrow tests are the per-state
-    tests)."""
+    tests); the verdict-only calls of every form (coarse-to-fine state orders) give the
+    same verdicts, counts and lengths."""
     robot, env, qf, qt = W.edge_workload()
     R, E = api.Robot(robot), api.Env(env)
     out = {}
     for form in (1, 4, 10):
         R.set_edge_form(form)
         out[form] = _run_edges(R, E, qf, qt, 0.01, 1)
-        if form > 1:   # verdict only: coarse-to-fine chunk order, the same verdicts
-            out[-form] = _run_edges(R, E, qf, qt, 0.01, 1, first_hit=False)
+        # verdict only: states walked coarse to fine, the same verdicts
+        out[-form] = _run_edges(R, E, qf, qt, 0.01, 1, first_hit=False)
     R.set_edge_form(0)
     for form in (4, 10):
         for a, b in zip(out[form], out[1]):
             np.testing.assert_array_equal(a, b)
+    for form in (1, 4, 10):
         vo = out[-form]
         np.testing.assert_array_equal(vo[0], out[1][0])
         np.testing.assert_array_equal(vo[2], out[1][2])
