@@ -311,64 +311,16 @@ gbmp_status gbmp_device_count(int32_t *count) {
     return GBMP_OK;
 }
 
-gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robot *out) {
-    GBMP_CHECK_ARG(d && out, "desc/out is NULL");
-    *out = nullptr;
-    const int L = d->num_links, S = d->num_spheres;
-    GBMP_CHECK_ARG(L >= 1 && L <= kMaxLinks, "num_links %d outside [1, %d]", L, kMaxLinks);
-    GBMP_CHECK_ARG(S >= 0 && S <= kMaxSpheres, "num_spheres %d outside [0, %d]", S, kMaxSpheres);
-    GBMP_CHECK_ARG(d->joint_types && d->joint_poses && d->joint_axes && d->parent, "kinematic table is NULL");
-    GBMP_CHECK_ARG(d->active_joints && d->lower && d->upper && d->default_values, "joint table is NULL");
-    GBMP_CHECK_ARG(S == 0 || (d->sphere_link && d->sphere_pos && d->sphere_radius), "sphere table is NULL");
-    GBMP_CHECK_ARG(d->resolution > 0.f && std::isfinite(d->resolution), "resolution must be > 0");
-    // SingleArmSpace.cu:63-69: every parent index must be smaller than its link index.
-    for (int i = 0; i < L; ++i) {
-        GBMP_CHECK_ARG(d->parent[i] < i, "Link parent link map is not valid at index %d. Value: %d", i, d->parent[i]);
-        GBMP_CHECK_ARG(i == 0 || d->parent[i] >= 0, "link %d has no parent", i);
-    }
-    for (int k = 0; k < S; ++k)
-        GBMP_CHECK_ARG(d->sphere_link[k] >= 0 && d->sphere_link[k] < L, "sphere %d attached to link %d", k,
-                       d->sphere_link[k]);
+}  // extern "C"
 
-    auto *r = new gbmp_robot_s();
-    r->L = L;
-    r->S = S;
-    r->resolution = d->resolution;
-    r->type.assign(d->joint_types, d->joint_types + L);
-    r->parent.assign(d->parent, d->parent + L);
-    r->pose16.assign(d->joint_poses, d->joint_poses + 16 * L);
-    r->axis.assign(d->joint_axes, d->joint_axes + 3 * L);
-    r->active.assign(d->active_joints, d->active_joints + L);
-    r->lower.assign(d->lower, d->lower + L);
-    r->upper.assign(d->upper, d->upper + L);
-    r->defv.assign(d->default_values, d->default_values + L);
-    if (S) {
-        r->slink.assign(d->sphere_link, d->sphere_link + S);
-        r->sph_pos.assign(d->sphere_pos, d->sphere_pos + 3 * S);
-        r->sph_r.assign(d->sphere_radius, d->sphere_radius + S);
-    }
-    if (d->self_enables) r->enables.assign(d->self_enables, d->self_enables + L * L);
-    r->dim = 0;
-    for (int i = 0; i < L; ++i) r->dim += r->active[i] != 0;
-    // Self-collision pair list, SelfCollisionConstraint.cu:28-38.
-    for (int i = 0; i < S; ++i)
-        for (int j = i + 1; j < S; ++j) {
-            const int li = r->slink[i], lj = r->slink[j];
-            if (li == lj) continue;
-            if (!r->enables.empty() && !r->enables[li * L + lj]) continue;
-            r->pairs.push_back(i);
-            r->pairs.push_back(j);
-            const float s = r->sph_r[i] + r->sph_r[j];
-            r->thr.push_back(s * s);
-        }
-    r->P = (int)r->thr.size();
-    if (r->P > kMaxSelfPairs) {
-        delete r;
-        set_error("%d self-collision pairs exceed the limit %d", (int)r->thr.size(), kMaxSelfPairs);
-        return GBMP_ERR_CAPACITY;
-    }
+namespace gbmp {
+constexpr int kGroupPiece = 8;   // smallest piece of a link's spheres in the chunk kernels' groups
+}  // namespace gbmp
 
-    // Pack the device tables.
+// The robot's device tables, packed and uploaded as one block (*block) with the sphere
+// groups of `piece` (see below), and their device view D.
+static gbmp_status pack_tables(gbmp_robot_s *r, int piece, void **block, DevRobot &D) {
+    const int L = r->L, S = r->S;
     std::vector<unsigned char> blob;
     auto put = [&](const void *src, size_t bytes) {
         size_t off = align16(blob.size());
@@ -390,13 +342,54 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     r->h_jl = jl;
     r->h_axn = axn;
     r->h_axr = axr;
-    // Sphere groups (links that carry spheres, in link order) and their bounding spheres.
-    std::vector<int> link2grp(L, -1), glink, sgrp(S ? S : 1, 0);
-    for (int l = 0; l < L; ++l)
-        for (int k = 0; k < S; ++k)
-            if (r->slink[k] == l) { link2grp[l] = (int)glink.size(); glink.push_back(l); break; }
+    // Sphere groups and their bounding spheres.  With piece == 0 a group is the spheres of
+    // one link.  Otherwise each link's spheres, ordered along the longest extent of their
+    // centres, are cut into ceil(n / M) pieces of consecutive spheres, M the smallest
+    // piece size from `piece` up that keeps the robot within min(kMaxGroups, 3 L) groups
+    // (3 L: the chunk kernels keep K x G group centres where K x L pose rows were); if none
+    // does, one group per link.  Groups come in link order.
+    std::vector<int> glink, sgrp(S ? S : 1, 0);
+    {
+        std::vector<std::vector<int>> by_link(L);
+        for (int k = 0; k < S; ++k) by_link[r->slink[k]].push_back(k);
+        int most = 1;
+        for (int l = 0; l < L; ++l) most = std::max(most, (int)by_link[l].size());
+        auto count = [&](int m) {
+            int g = 0;
+            for (int l = 0; l < L; ++l) g += ((int)by_link[l].size() + m - 1) / m;
+            return g;
+        };
+        int M = most;
+        if (piece > 0) {
+            const int gmax = std::min(kMaxGroups, 3 * L);
+            M = std::min(piece, most);
+            while (M < most && count(M) > gmax) ++M;
+        }
+        for (int l = 0; l < L; ++l) {
+            std::vector<int> &ks = by_link[l];
+            const int nl = (int)ks.size();
+            if (nl == 0) continue;
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (int k : ks)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], (double)r->sph_pos[3 * k + a]);
+                    hi[a] = std::max(hi[a], (double)r->sph_pos[3 * k + a]);
+                }
+            int ax = 0;
+            for (int a = 1; a < 3; ++a)
+                if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+            std::stable_sort(ks.begin(), ks.end(),
+                             [&](int x, int y) { return r->sph_pos[3 * x + ax] < r->sph_pos[3 * y + ax]; });
+            const int pieces = (nl + M - 1) / M;
+            for (int q = 0; q < pieces; ++q) {
+                const int g = (int)glink.size();
+                glink.push_back(l);
+                for (int i = (int)((long long)q * nl / pieces); i < (int)((long long)(q + 1) * nl / pieces); ++i)
+                    sgrp[ks[i]] = g;
+            }
+        }
+    }
     const int G = (int)glink.size();
-    for (int k = 0; k < S; ++k) sgrp[k] = link2grp[r->slink[k]];
     std::vector<float> grp(4 * (G ? G : 1), 0.f);
     for (int g = 0; g < G; ++g) {
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -461,23 +454,14 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     const unsigned zero = 0;
     size_t o_fault = put(&zero, sizeof zero);
 
-    int dev = 0;
-    r->num_sms = current_device_sms(&dev);
-    r->device = dev;
-    if (r->num_sms <= 0) {
-        delete r;
-        set_error("no CUDA device available");
-        return GBMP_ERR_CUDA;
-    }
-    cudaError_t e = cudaMalloc(&r->d_block, blob.size());
-    if (e == cudaSuccess) e = cudaMemcpy(r->d_block, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMalloc(block, blob.size());
+    if (e == cudaSuccess) e = cudaMemcpy(*block, blob.data(), blob.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         set_error("uploading robot tables failed: %s", cudaGetErrorString(e));
-        gbmp_robot_destroy(r);
         return e == cudaErrorMemoryAllocation ? GBMP_ERR_OUT_OF_MEMORY : GBMP_ERR_CUDA;
     }
-    auto *b = static_cast<unsigned char *>(r->d_block);
-    DevRobot &D = r->dev;
+    auto *b = static_cast<unsigned char *>(*block);
+    D = DevRobot{};
     D.L = L; D.S = S; D.P = r->P; D.spl = S ? (S + kWarp - 1) / kWarp : 1;
     D.jl = (const float *)(b + o_jl); D.axn = (const float *)(b + o_axn); D.axr = (const float *)(b + o_axr);
     D.sph = (const float *)(b + o_sph); D.type = (const int *)(b + o_type); D.parent = (const int *)(b + o_par);
@@ -500,9 +484,90 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
     if (staged_bytes != smem_tables_bytes(D, 0)) {   // the layouts must agree byte for byte
         set_error("internal: staged table block of %zu bytes, shared-memory layout of %zu", staged_bytes,
                   smem_tables_bytes(D, 0));
-        gbmp_robot_destroy(r);
         return GBMP_ERR_CUDA;
     }
+    return GBMP_OK;
+}
+
+extern "C" {
+
+gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robot *out) {
+    GBMP_CHECK_ARG(d && out, "desc/out is NULL");
+    *out = nullptr;
+    const int L = d->num_links, S = d->num_spheres;
+    GBMP_CHECK_ARG(L >= 1 && L <= kMaxLinks, "num_links %d outside [1, %d]", L, kMaxLinks);
+    GBMP_CHECK_ARG(S >= 0 && S <= kMaxSpheres, "num_spheres %d outside [0, %d]", S, kMaxSpheres);
+    GBMP_CHECK_ARG(d->joint_types && d->joint_poses && d->joint_axes && d->parent, "kinematic table is NULL");
+    GBMP_CHECK_ARG(d->active_joints && d->lower && d->upper && d->default_values, "joint table is NULL");
+    GBMP_CHECK_ARG(S == 0 || (d->sphere_link && d->sphere_pos && d->sphere_radius), "sphere table is NULL");
+    GBMP_CHECK_ARG(d->resolution > 0.f && std::isfinite(d->resolution), "resolution must be > 0");
+    // SingleArmSpace.cu:63-69: every parent index must be smaller than its link index.
+    for (int i = 0; i < L; ++i) {
+        GBMP_CHECK_ARG(d->parent[i] < i, "Link parent link map is not valid at index %d. Value: %d", i, d->parent[i]);
+        GBMP_CHECK_ARG(i == 0 || d->parent[i] >= 0, "link %d has no parent", i);
+    }
+    for (int k = 0; k < S; ++k)
+        GBMP_CHECK_ARG(d->sphere_link[k] >= 0 && d->sphere_link[k] < L, "sphere %d attached to link %d", k,
+                       d->sphere_link[k]);
+
+    auto *r = new gbmp_robot_s();
+    r->L = L;
+    r->S = S;
+    r->resolution = d->resolution;
+    r->type.assign(d->joint_types, d->joint_types + L);
+    r->parent.assign(d->parent, d->parent + L);
+    r->pose16.assign(d->joint_poses, d->joint_poses + 16 * L);
+    r->axis.assign(d->joint_axes, d->joint_axes + 3 * L);
+    r->active.assign(d->active_joints, d->active_joints + L);
+    r->lower.assign(d->lower, d->lower + L);
+    r->upper.assign(d->upper, d->upper + L);
+    r->defv.assign(d->default_values, d->default_values + L);
+    if (S) {
+        r->slink.assign(d->sphere_link, d->sphere_link + S);
+        r->sph_pos.assign(d->sphere_pos, d->sphere_pos + 3 * S);
+        r->sph_r.assign(d->sphere_radius, d->sphere_radius + S);
+    }
+    if (d->self_enables) r->enables.assign(d->self_enables, d->self_enables + L * L);
+    r->dim = 0;
+    for (int i = 0; i < L; ++i) r->dim += r->active[i] != 0;
+    // Self-collision pair list, SelfCollisionConstraint.cu:28-38.
+    for (int i = 0; i < S; ++i)
+        for (int j = i + 1; j < S; ++j) {
+            const int li = r->slink[i], lj = r->slink[j];
+            if (li == lj) continue;
+            if (!r->enables.empty() && !r->enables[li * L + lj]) continue;
+            r->pairs.push_back(i);
+            r->pairs.push_back(j);
+            const float s = r->sph_r[i] + r->sph_r[j];
+            r->thr.push_back(s * s);
+        }
+    r->P = (int)r->thr.size();
+    if (r->P > kMaxSelfPairs) {
+        delete r;
+        set_error("%d self-collision pairs exceed the limit %d", (int)r->thr.size(), kMaxSelfPairs);
+        return GBMP_ERR_CAPACITY;
+    }
+
+    int dev = 0;
+    r->num_sms = current_device_sms(&dev);
+    r->device = dev;
+    if (r->num_sms <= 0) {
+        delete r;
+        set_error("no CUDA device available");
+        return GBMP_ERR_CUDA;
+    }
+    // Two views of the tables: sphere groups by link for the per-state kernels, and links
+    // cut into pieces of kGroupPiece or more spheres for the chunk kernels, whose broad
+    // phase and self-pair tests run once per chunk and gain from tighter groups (the
+    // per-state kernels test every obstacle against every group and lose).  Both views
+    // share one device-status word.
+    gbmp_status pst = pack_tables(r, 0, &r->d_block, r->dev);
+    if (!pst) pst = pack_tables(r, kGroupPiece, &r->d_block_chunk, r->dev_chunk);
+    if (pst) {
+        gbmp_robot_destroy(r);
+        return pst;
+    }
+    r->dev_chunk.fault = r->dev.fault;
     if (flags & GBMP_ROBOT_CODEGEN) {
         gbmp_status st = codegen_build(r);
         if (st) {
@@ -520,6 +585,7 @@ gbmp_status gbmp_robot_create(const gbmp_robot_desc *d, int32_t flags, gbmp_robo
 gbmp_status gbmp_robot_destroy(gbmp_robot r) {
     if (!r) return GBMP_OK;
     if (r->d_block) cudaFree(r->d_block);
+    if (r->d_block_chunk) cudaFree(r->d_block_chunk);
     codegen_free(r->cg);
     delete r;
     return GBMP_OK;
@@ -869,9 +935,12 @@ static gbmp_status edge_validate(gbmp_robot r, gbmp_env env, const float *d_from
     size_t smem = block_smem(D, env_words(Ev.ns, Ev.nb, Ev.nc));
     int grid = 0;
     const bool cull = r->dev.cull != 0;
+    // the chunk kernel reads the tables grouped by pieces of links
+    DevRobot Dc = r->dev_chunk;
+    Dc.work = D.work;
     int K = edge_chunk_states(D, r->edge_form);
     if (K) {
-        st = edge_chunk_prepare(D, Ev, r->num_sms, K, &smem, &grid);
+        st = edge_chunk_prepare(Dc, Ev, r->num_sms, K, &smem, &grid);
         if (st == GBMP_ERR_CAPACITY) {   // chunk scratch does not fit next to a large scene
             K = 0;
             st = GBMP_OK;
@@ -890,7 +959,7 @@ static gbmp_status edge_validate(gbmp_robot r, gbmp_env env, const float *d_from
     {
         ProfScope ps(GBMP_PROF_EDGE_WAVE, s);
         if (K) {
-            st = edge_chunk_launch(D, Ev, K, grid, smem, s, d_from, d_to, nsteps, dir, order, E, next, d_ok,
+            st = edge_chunk_launch(Dc, Ev, K, grid, smem, s, d_from, d_to, nsteps, dir, order, E, next, d_ok,
                                    d_first_hit);
             if (st) return st;
         } else {

@@ -117,9 +117,10 @@ struct gbmp_robot_s {
     std::vector<float> h_jl, h_axn, h_axr;   // host copies of the uploaded joint tables
     std::vector<int> pairs;          // 2*P
     std::vector<float> thr;          // P
-    // device tables (one allocation)
-    void *d_block = nullptr;
-    gbmp::DevRobot dev{};
+    // device tables: sphere groups by link (dev, the per-state kernels) and by pieces of
+    // links (dev_chunk, the chunk kernels); one allocation each
+    void *d_block = nullptr, *d_block_chunk = nullptr;
+    gbmp::DevRobot dev{}, dev_chunk{};
     // edge validation form: 0 automatic, 1 state by state, 4 or 10 states per chunk
     int edge_form = 0;
     // edge-check scratch

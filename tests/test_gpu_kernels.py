@@ -398,10 +398,10 @@ def test_edge_forms_agree_on_every_edge_of_the_benchmark_call():
 
 @pytest.mark.parametrize("dof,n_spheres", [(4, 100), (3, 120), (6, 70)])
 def test_edge_forms_agree_for_large_sphere_groups(dof, n_spheres):
-    """Self-pair tests of the chunk form for links of 16 or fewer spheres (two group pairs
-    at a time, half a warp each), 17-32 spheres (a pair on the whole warp) and more than
-    32 (the pair list): the same first hits as the per-state form on every edge, and the
-    oracle's outside the clearance band."""
+    """Robots whose links carry many spheres: the per-state form groups spheres by link
+    (groups of 14-40 spheres, so its self-pair tests take both the sphere-against-group
+    path and the pair list), the chunk form by pieces of links (groups of 8-10 spheres):
+    the same first hits on every edge, and the oracle's outside the clearance band."""
     robot = W.serial_arm(30 + dof, dof=dof, n_spheres=n_spheres, offset_range=(0.1, 0.3),
                          radius_range=(0.02, 0.05))
     env = W.random_env(31, 40, 12, 4, oriented=True)
