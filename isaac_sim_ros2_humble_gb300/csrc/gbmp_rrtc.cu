@@ -78,15 +78,46 @@ __global__ void k_rrtc_batch_finish(BatchProblem *__restrict__ probs, int n) {
     probs[p].prev[1] = min(probs[p].P.size[1], probs[p].P.cap) * probs[p].P.stride;
 }
 
-// The single-problem deadline, set on the device just before the planning launch (no
-// host round trip to read the device clock).
-__global__ void k_set_deadline(unsigned long long *deadline, unsigned long long limit_ns) {
-    if (threadIdx.x == 0) *deadline = global_ns() + limit_ns;
+// Goals a single-problem solve stages in its pinned input block; more are copied into the
+// goal tree after the reset.
+constexpr int kStagedGoals = 64;
+
+// Reset of a single-problem solve, one launch: NaN sentinels over the words the previous
+// solve wrote (w[t] words of tree t past its root rows), unset dynamic-domain radii (r[t]),
+// the root rows (the start; the staged goals, other goal rows NaN until their copy), the
+// roots' parents, the counters and the deadline (the device clock plus the limit, set here
+// so that no host round trip reads the clock).  `in` is the mapped pinned input block:
+// start [L], then up to kStagedGoals goals [L] each.  The root rows and the words past
+// them are written by different loops, so no word has two writers.
+__global__ void k_rrtc_init(RrtcDev P, int L, long long w0, long long w1, int r0, int r1,
+                            const float *__restrict__ in, int n_goals, unsigned long long limit_ns) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nth = (long long)gridDim.x * blockDim.x;
+    const float nan = __int_as_float(0xffffffff);
+    const long long root0 = P.stride, root1 = (long long)n_goals * P.stride;
+    for (long long i = root0 + tid; i < w0; i += nth) P.nodes[0][i] = nan;
+    for (long long i = root1 + tid; i < w1; i += nth) P.nodes[1][i] = nan;
+    if (P.radii[0])
+        for (long long i = tid; i < r0; i += nth) P.radii[0][i] = __uint_as_float(kRadiusUnset);
+    if (P.radii[1])
+        for (long long i = tid; i < r1; i += nth) P.radii[1][i] = __uint_as_float(kRadiusUnset);
+    for (long long i = tid; i < root0; i += nth) P.nodes[0][i] = i < L ? in[i] : nan;
+    for (long long i = tid; i < root1; i += nth) {
+        const long long g = i / P.stride, j = i - g * P.stride;
+        P.nodes[1][i] = (j < L && g < kStagedGoals) ? in[L + g * L + j] : nan;
+    }
+    for (long long g = tid; g < n_goals; g += nth) P.parent[1][g] = (int)g;
+    if (tid == 0) {
+        P.parent[0][0] = 0;
+        for (int k = 0; k < 64; ++k) P.size[k] = 0;   // sizes, state, deadline, path length
+        P.size[0] = 1;
+        P.size[1] = n_goals;
+        *(unsigned long long *)(P.state + 8) = global_ns() + limit_ns;
+    }
 }
 
 // Walk both parent chains into the path (start tree root first).  One thread.
-__global__ void k_rrtc_trace(RrtcDev P, int L) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void rrtc_trace_path(const RrtcDev &P, int L) {
     if (P.state[0] != kStSolved) { *P.path_len = 0; return; }
     const int tr = P.state[2];
     const int a = P.state[3], b = P.state[4];
@@ -103,6 +134,17 @@ __global__ void k_rrtc_trace(RrtcDev P, int L) {
     for (int i = nb; i >= 0; i = (P.parent[1][i] == i ? -1 : P.parent[1][i]), ++k)
         for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[1][(long long)i * P.stride + j];
     *P.path_len = len0 + len1;
+}
+
+// The trace, then the solve's outcome into the mapped pinned block `out` (state [6], tree
+// sizes [2], path length), so that the host reads everything after one synchronisation.
+__global__ void k_rrtc_trace(RrtcDev P, int L, int *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    rrtc_trace_path(P, L);
+    for (int k = 0; k < 6; ++k) out[k] = P.state[k];
+    out[6] = P.size[0];
+    out[7] = P.size[1];
+    out[8] = *P.path_len;
 }
 
 __global__ void k_rrtc_batch_trace(const BatchProblem *__restrict__ probs, int n, int *__restrict__ summary) {
@@ -190,6 +232,9 @@ struct gbmp_planner_s {
     // the traced path goes straight to pinned host memory (the trace kernel writes it
     // through the mapped pointer), so reading a result takes one synchronisation
     float *h_path = nullptr;
+    // mapped pinned block: the outcome the trace kernel writes (16 ints), then the staged
+    // start and goals the reset kernel reads
+    int *h_io = nullptr, *d_io = nullptr;
 };
 
 extern "C" {
@@ -225,15 +270,19 @@ gbmp_status gbmp_planner_create(gbmp_robot r, int32_t max_nodes, int32_t path_ca
     D.radii[0] = (float *)(b + 2 * nodes_b + 2 * par_b + 256);
     D.radii[1] = (float *)(b + 2 * nodes_b + 2 * par_b + 256 + rad_b);
     p->dirty[0] = p->dirty[1] = p->dirty_radii[0] = p->dirty_radii[1] = max_nodes;
-    void *mapped = nullptr;
+    void *mapped = nullptr, *mapped_io = nullptr;
+    const size_t io_b = sizeof(int) * 16 + sizeof(float) * (size_t)r->L * (1 + kStagedGoals);
     if (cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess ||
         cudaHostAlloc((void **)&p->h_path, path_b, cudaHostAllocMapped) != cudaSuccess ||
-        cudaHostGetDevicePointer(&mapped, p->h_path, 0) != cudaSuccess) {
+        cudaHostGetDevicePointer(&mapped, p->h_path, 0) != cudaSuccess ||
+        cudaHostAlloc((void **)&p->h_io, io_b, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&mapped_io, p->h_io, 0) != cudaSuccess) {
         gbmp_planner_destroy(p);
-        set_error("planner events or pinned path buffer could not be created");
+        set_error("planner events or pinned buffers could not be created");
         return GBMP_ERR_CUDA;
     }
     D.path = static_cast<float *>(mapped);
+    p->d_io = static_cast<int *>(mapped_io);
     *out = p;
     return GBMP_OK;
 }
@@ -243,6 +292,7 @@ gbmp_status gbmp_planner_destroy(gbmp_planner p) {
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->h_path) cudaFreeHost(p->h_path);
+    if (p->h_io) cudaFreeHost(p->h_io);
     if (p->block) cudaFree(p->block);
     delete p;
     return GBMP_OK;
@@ -275,31 +325,33 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     memset(res, 0, sizeof *res);
     cudaStream_t st = (cudaStream_t)stream;
     const RrtcDev &D = p->dev;
-    // reset: NaN sentinels, counters, roots (RobotSolver.cu:361-388 with a float sentinel);
-    // only the slots written since the last reset (a solve of a 1,000,000-node planner
-    // otherwise re-poisons 64 MB of trees)
-    for (int t = 0; t < 2; ++t)
-        if (p->dirty[t] > 0)
-            GBMP_CUDA(cudaMemsetAsync(D.nodes[t], 0xff, sizeof(float) * (size_t)p->dirty[t] * p->stride, st));
-    GBMP_CUDA(cudaMemsetAsync(D.size, 0, 256, st));
-    if (s->dynamic_domain) {   // every radius unset (kRadiusUnset = bytes 0x7f)
-        for (int t = 0; t < 2; ++t)
-            if (p->dirty_radii[t] > 0)
-                GBMP_CUDA(cudaMemsetAsync(D.radii[t], 0x7f, sizeof(float) * (size_t)p->dirty_radii[t], st));
-        p->dirty_radii[0] = p->dirty_radii[1] = 0;
+    // reset (RobotSolver.cu:361-388 with a float sentinel), one launch: only the slots
+    // written since the last reset are re-poisoned (a solve of a 1,000,000-node planner
+    // otherwise re-poisons 64 MB of trees); start and goals come from the mapped pinned
+    // input block, the goals past kStagedGoals by a copy after the reset
+    const long long w0 = (long long)std::max(p->dirty[0], 1) * p->stride;
+    const long long w1 = (long long)std::max(p->dirty[1], n_goals) * p->stride;
+    const int r0 = s->dynamic_domain ? p->dirty_radii[0] : 0, r1 = s->dynamic_domain ? p->dirty_radii[1] : 0;
+    if (s->dynamic_domain) p->dirty_radii[0] = p->dirty_radii[1] = 0;
+    float *in = reinterpret_cast<float *>(p->h_io + 16);
+    memcpy(in, h_start, sizeof(float) * L);
+    memcpy(in + L, h_goals, sizeof(float) * (size_t)std::min(n_goals, kStagedGoals) * L);
+    const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
+    {
+        const long long most = std::max(std::max(w0, w1), (long long)std::max(r0, r1));
+        const int blocks = (int)std::max(1LL, std::min<long long>((most + 255) / 256, 8LL * r->num_sms));
+        ProfScope ps(GBMP_PROF_OTHER, st);
+        k_rrtc_init<<<blocks, 256, 0, st>>>(D, L, w0, w1, r0, r1, reinterpret_cast<const float *>(p->d_io + 16),
+                                            n_goals, (unsigned long long)(lim * 1e9));
     }
+    GBMP_CUDA(cudaGetLastError());
+    if (n_goals > kStagedGoals)
+        GBMP_CUDA(cudaMemcpy2DAsync(D.nodes[1] + (size_t)kStagedGoals * p->stride, sizeof(float) * p->stride,
+                                    h_goals + (size_t)kStagedGoals * L, sizeof(float) * L, sizeof(float) * L,
+                                    n_goals - kStagedGoals, cudaMemcpyHostToDevice, st));
     // until this solve's tree sizes are read back, every slot counts as written
     p->dirty[0] = p->dirty[1] = p->cap;
     if (s->dynamic_domain) p->dirty_radii[0] = p->dirty_radii[1] = p->cap;
-    // the goal tree starts with every goal as a root (a node that is its own parent)
-    std::vector<int> h_init{1, n_goals}, h_roots(n_goals);
-    for (int g = 0; g < n_goals; ++g) h_roots[g] = g;
-    GBMP_CUDA(cudaMemcpyAsync(D.size, h_init.data(), sizeof(int) * 2, cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpyAsync(D.nodes[0], h_start, sizeof(float) * L, cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpy2DAsync(D.nodes[1], sizeof(float) * p->stride, h_goals, sizeof(float) * L, sizeof(float) * L,
-                                n_goals, cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpyAsync(D.parent[0], h_roots.data(), sizeof(int), cudaMemcpyHostToDevice, st));
-    GBMP_CUDA(cudaMemcpyAsync(D.parent[1], h_roots.data(), sizeof(int) * n_goals, cudaMemcpyHostToDevice, st));
 
     const DevEnv E = env->dev();
     DevRobot DR = r->dev;
@@ -319,16 +371,9 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     prm.dd_min = s->dd_min_radius;
     prm.balance = balance;
     prm.tree_ratio = tree_ratio;
-    // device deadline: the device clock at the launch plus the limit, set on the device
-    const double lim = s->time_limit_s > 0.0 ? s->time_limit_s : 10.0;
-    unsigned long long *d_deadline = (unsigned long long *)(D.state + 8);
-    {
-        ProfScope ps(GBMP_PROF_OTHER, st);
-        k_set_deadline<<<1, 32, 0, st>>>(d_deadline, (unsigned long long)(lim * 1e9));
-    }
-    GBMP_CUDA(cudaGetLastError());
+    // device deadline: set by the reset kernel
     prm.deadline_ns = 0;
-    prm.deadline_ptr = d_deadline;
+    prm.deadline_ptr = (unsigned long long *)(D.state + 8);
     cudaEvent_t e0 = p->ev0, e1 = p->ev1;
     GBMP_CUDA(cudaEventRecord(e0, st));
     gbmp_status stt = GBMP_OK;
@@ -347,14 +392,16 @@ gbmp_status gbmp_rrtc_solve_goals(gbmp_planner p, gbmp_env env, const float *h_s
     GBMP_CUDA(cudaEventRecord(e1, st));
     {
         ProfScope ps(GBMP_PROF_OTHER, st);
-        k_rrtc_trace<<<1, 32, 0, st>>>(D, L);
+        k_rrtc_trace<<<1, 32, 0, st>>>(D, L, p->d_io);
     }
     GBMP_CUDA(cudaGetLastError());
-    int h_state[6], h_size[2], h_len = 0;
-    GBMP_CUDA(cudaMemcpyAsync(h_state, D.state, sizeof h_state, cudaMemcpyDeviceToHost, st));
-    GBMP_CUDA(cudaMemcpyAsync(h_size, D.size, sizeof h_size, cudaMemcpyDeviceToHost, st));
-    GBMP_CUDA(cudaMemcpyAsync(&h_len, D.path_len, sizeof h_len, cudaMemcpyDeviceToHost, st));
     GBMP_CUDA(cudaStreamSynchronize(st));
+    const volatile int *io = p->h_io;
+    int h_state[6], h_size[2];
+    for (int k = 0; k < 6; ++k) h_state[k] = io[k];
+    h_size[0] = io[6];
+    h_size[1] = io[7];
+    const int h_len = io[8];
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     p->dirty[0] = std::min(std::max(h_size[0], 1), p->cap);

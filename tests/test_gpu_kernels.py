@@ -185,6 +185,11 @@ def test_check_edges(edge, rule):
     _edge_parity(m, qf, qt, res, rule, ok.cpu().numpy().astype(bool), fh.cpu().numpy(), ln.cpu().numpy(),
                  ns.cpu().numpy())
     assert ok.sum().item() > 0 and ok.sum().item() < n
+    # the verdict-only call (states coarse to fine) gives the same verdicts
+    ok2 = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    api.check_edges(R, E, dev(qf), dev(qt), res, rule, ok2)
+    torch.cuda.synchronize()
+    assert torch.equal(ok2, ok)
 
 
 def test_check_edges_count_rule(edge):
@@ -199,6 +204,10 @@ def test_check_edges_count_rule(edge):
     ns = torch.zeros(n, dtype=torch.int32, device="cuda")
     api.check_edges(R, E, dev(qf[:n]), dev(qt[:n]), 7, _lib.STEP_COUNT, ok, fh, ln, ns)
     torch.cuda.synchronize()
+    ok2 = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    api.check_edges(R, E, dev(qf[:n]), dev(qt[:n]), 7, _lib.STEP_COUNT, ok2)
+    torch.cuda.synchronize()
+    assert torch.equal(ok2, ok)
     nsn = ns.cpu().numpy()
     assert np.all(nsn == 8)
     _edge_parity(m, qf[:n], qt[:n], 7, O.STEP_COUNT, ok.cpu().numpy().astype(bool), fh.cpu().numpy(),

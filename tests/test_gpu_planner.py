@@ -101,6 +101,29 @@ def test_rrtc_count_rule_several_goals(scene):
         planner.solve(E, start, goals, resolution=0.5, rule=_lib.STEP_COUNT)
 
 
+def test_rrtc_many_goals_then_one(scene):
+    """More goals than the solve stages in its pinned input block (64): the rest are
+    copied into the goal tree after the reset.  The path ends at one of the goals, every
+    goal is a root (the goal tree holds at least all of them), and a following one-goal
+    solve on the same planner finds none of the earlier goal rows left."""
+    robot, env, m, free, edge_free, R, E = scene
+    start, g0 = W.pick_problem(free, edge_free, 5)
+    others = [q for q in free if not np.array_equal(q, start)]
+    goals = np.stack([g0] + [others[i % len(others)] for i in range(99)])
+    planner = api.Planner(R, max_nodes=100_000, path_cap=8192)
+    res, path = planner.solve(E, start, goals, lanes=512, range_=0.1, resolution=RES, rule=RULE, seed=6,
+                              time_limit_s=20.0)
+    assert res["solved"] == 1, res
+    assert res["goal_tree_size"] >= len(goals)
+    np.testing.assert_array_equal(path[0], start)
+    assert any(np.array_equal(path[-1], g) for g in goals)
+    _validate_path(m, path, start, path[-1])
+    res, path = planner.solve(E, start, g0, lanes=512, range_=0.1, resolution=RES, rule=RULE, seed=7,
+                              time_limit_s=20.0)
+    assert res["solved"] == 1, res
+    _validate_path(m, path, start, g0)
+
+
 def test_rrtc_dynamic_domain_paths_are_valid(scene):
     """pRRTC's dynamic domain (samples beyond a node's radius skipped, radii set, shrunk
     and grown as extensions fail and succeed) changes which samples are used, not what a
