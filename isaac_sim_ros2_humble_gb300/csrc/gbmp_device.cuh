@@ -216,12 +216,8 @@ __device__ inline bool stage_tables(const DevRobot &R, const DevEnv &E, const Sm
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         // order earlier generic-proxy accesses of this shared memory before the copies
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        unsigned long long state;
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
-                     : "=l"(state)
-                     : "r"(bar), "r"(bytes_r + bytes_e)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes_r + bytes_e)
                      : "memory");
-        (void)state;
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                          smem_u32(t.jl)),
                      "l"(R.stage), "r"(bytes_r), "r"(bar)
