@@ -2,6 +2,7 @@
 // chunks of consecutive states; the chunk routines are in gbmp_chunk_device.cuh), its
 // launch set-up, and FK alone by chunks of consecutive states (gbmp_fk).
 #include "gbmp_chunk_device.cuh"
+#include "gbmp_order.h"
 
 namespace gbmp {
 
@@ -17,51 +18,11 @@ constexpr int kChunkWarps = 8;
 // a later chunk.  Writes the edge's outputs (ok, first hit; -2 for an edge too long to
 // validate).
 //
-// Two chunk orders.  When the first hit is asked for, state order: the first 4 states,
-// then K at a time, so the hit found is the lowest colliding index.  When only the verdict
-// is (the reference's output), an edge is infeasible as soon as any of its states collides,
-// so the chunks are visited coarse to fine: the first 4 states, the last K, then the
-// K-state chunks between them in 16 interleaved passes (chunks o, o + 16, o + 32, ...) taken
-// in bit-reversed order of o (0, 8, 4, 12, 2, ...).  A colliding stretch of the edge
-// longer than 16 chunks is then met after about 1/16 of the states before it, and a goal
-// state that collides after K; a free edge still has every state checked, in either
-// order.  On the 65,536 edges of the 8-DOF benchmark (uniform endpoints, 82 % colliding)
-// the states checked fall from 8.89 M to 4.94 M, 4.19 M of them on the free edges; 8
-// passes give 4.97 M (5.01 M in plain order), 4 passes 5.06 M, a full bit-reversed
-// order of the chunks 4.96 M.
-constexpr int kFirstChunk = 4;
-constexpr int kAnyPasses = 16;
-
-template <int K>
-__device__ __forceinline__ int edge_chunk_count(int n, bool any) {
-    if (n <= kFirstChunk) return 1;
-    if (!any) return 1 + (n - kFirstChunk + K - 1) / K;
-    const int ts = max(kFirstChunk, n - K);   // the last chunk is [ts, n)
-    return 2 + (ts - kFirstChunk + K - 1) / K;
-}
-
-// States [x, y) of chunk `idx` (0 <= idx < edge_chunk_count) of an edge of n states.
-template <int K>
-__device__ __forceinline__ int2 edge_chunk_range(int idx, int n, bool any) {
-    if (idx == 0) return make_int2(0, min(n, kFirstChunk));
-    if (!any) {
-        const int a = kFirstChunk + (idx - 1) * K;
-        return make_int2(a, min(n, a + K));
-    }
-    const int ts = max(kFirstChunk, n - K);
-    if (idx == 1) return make_int2(ts, n);
-    const int nm = (ts - kFirstChunk + K - 1) / K;   // chunks between, [4 + jK, min(ts, 4 + (j + 1)K))
-    int r = idx - 2;
-    for (int p = 0;; ++p) {   // pass p holds chunks o, o + 16, ... below nm; r < nm, so p < 16 at exit
-        const int o = (int)(__brev((unsigned)p) >> 28);
-        const int sz = (nm - o + kAnyPasses - 1) / kAnyPasses;
-        if (r < sz) {
-            const int a = kFirstChunk + (o + r * kAnyPasses) * K;
-            return make_int2(a, min(ts, a + K));
-        }
-        r -= sz;
-    }
-}
+// The chunk orders are gbmp_order.h's: state order when the first hit is asked for,
+// coarse to fine when only the verdict is.  On the 65,536 edges of the 8-DOF benchmark
+// (uniform endpoints, 82 % colliding) the coarse-to-fine order checks 4.94 M states
+// against 8.89 M, 4.19 M of them on the free edges; 8 passes give 4.97 M (5.01 M in plain
+// order), 4 passes 5.06 M, a full bit-reversed order of the chunks 4.96 M.
 
 template <int SPL, int K, bool CNT>
 __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
@@ -91,9 +52,9 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
             hit = -2;   // too long to validate
         } else {
             const long long off = (long long)e * R.L;
-            const int nch = edge_chunk_count<K>(n, any);
+            const int nch = edge_chunk_count(n, K, any);
             for (int c = 0; c < nch; ++c) {
-                const int2 r = edge_chunk_range<K>(c, n, any);
+                const StateRange r = edge_chunk_range(c, n, K, any);
                 const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, r.x,
                                                            r.y, n, nullptr);
                 __syncwarp();

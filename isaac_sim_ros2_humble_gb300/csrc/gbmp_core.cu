@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "gbmp_internal.h"
+#include "gbmp_order.h"
 
 namespace gbmp {
 
@@ -153,27 +154,10 @@ __global__ void k_edge_order(const int *__restrict__ nsteps, long long E, const 
     }
 }
 
-// State checked at step c (0 <= c < n) of an edge of n states when only the verdict is
-// asked for: the first state, the last, then the states between in 16 interleaved passes
-// taken in bit-reversed order (offsets 0, 8, 4, 12, 2, ...), so that a colliding stretch
-// of the edge is met after a fraction of the states before it.
-__device__ __forceinline__ int verdict_order_state(int c, int n) {
-    if (c == 0 || n <= 2) return c;
-    if (c == 1) return n - 1;
-    const int m = n - 2;   // states 1 .. n-2
-    int r = c - 2;
-    for (int p = 0;; ++p) {   // r < m, so the pass is found within 16 steps
-        const int o = (int)(__brev((unsigned)p) >> 28);
-        const int sz = (m - o + 15) / 16;
-        if (r < sz) return 1 + o + r * 16;
-        r -= sz;
-    }
-}
-
 // Edge validation state by state (robots with more than 32 sphere groups, and the
 // per-state form of the others): a warp takes the next edge of `order` (a shared
-// counter), walks its states -- in order when the first hit is asked for, else in
-// verdict_order_state's order -- and stops at a colliding state.
+// counter), walks its states -- in order when the first hit is asked for, else coarse to
+// fine (verdict_order_state, gbmp_order.h) -- and stops at a colliding state.
 template <int SPL, bool CULL>
 __global__ void __launch_bounds__(kWarpsPerBlock *kWarp, CULL ? 3 : 1)
     k_edge_states(DevRobot R, DevEnv E, const float *__restrict__ from, const float *__restrict__ to,

@@ -147,6 +147,22 @@ def test_kernel_setup_is_recorded_per_device(tmp_path):
     assert "devset ok" in out.stdout
 
 
+def test_edge_state_orders_cover_every_state_once(tmp_path):
+    """The orders in which edge validation visits an edge's states (csrc/gbmp_order.h,
+    compiled here for the host): every state of every edge length up to 6,000 exactly
+    once, for both chunk sizes; state order from the start; coarse to fine with the first
+    4 states, then the last chunk, then the chunks between pass by pass in bit-reversed
+    offset order; the state-by-state form a permutation starting with the first and last
+    states."""
+    exe = tmp_path / "order_check"
+    src = os.path.join(ROOT, "tests", "cpp", "order_check.cpp")
+    inc = os.path.join(ROOT, "isaac_sim_ros2_humble_gb300", "csrc")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", inc, src, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "order ok" in out.stdout
+
+
 def test_batch_autotuner_policy_with_a_fake_timer(tmp_path):
     """The batched planner's launch-shape tuner (csrc/gbmp_autotune.h), driven by a fake
     timer: each allowed candidate tried twice in order, the least time of each kept, the
