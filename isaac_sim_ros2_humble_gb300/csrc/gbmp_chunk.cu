@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kChunkWarps *kWarp, 2)
             for (int c = 0; c < nch; ++c) {
                 const StateRange r = edge_chunk_range(c, n, K, any);
                 const int h = warp_edge_chunk<SPL, K, CNT>(t, R, E, w, cs, lane, from + off, to + off, dir + off, r.x,
-                                                           r.y, n, nullptr);
+                                                           r.y, n);
                 __syncwarp();
                 if (h >= 0) { hit = h; break; }
             }

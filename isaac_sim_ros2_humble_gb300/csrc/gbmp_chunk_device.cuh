@@ -377,7 +377,7 @@ template <int SPL, int K, bool CNT>
 __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, const DevEnv &E, const WarpScratch &w,
                                       const ChunkScratch &cs, int lane, const float *__restrict__ f,
                                       const float *__restrict__ to, const float *__restrict__ d, int s0, int s1,
-                                      int n, const int *first_hit) {
+                                      int n) {
     const int ks = s1 - s0;
     constexpr bool count = CNT;   // executed-work accounting compiled in only when asked for
     // FK and the group-centre transforms of every state; sphere placements are counted
@@ -541,12 +541,6 @@ __device__ inline int warp_edge_chunk(const SmemTables &t, const DevRobot &R, co
     }
     for (int k = 0; k < kend; ++k) {
         const int s = s0 + k;
-        if (k == 4 && first_hit) {   // once per chunk: stop if another warp found an earlier hit on this edge
-            int known = 0;
-            if (lane == 0) known = *(volatile const int *)first_hit;
-            known = __shfl_sync(kFull, known, 0);
-            if (known < s) break;
-        }
         const float *lp = cs.lpK + k * 12 * R.L;
         bool hit;
         if (overflow) {

@@ -196,8 +196,7 @@ __device__ bool block_edge_free(const SmemTables &t, const DevRobot &R, const De
             const int s0 = c0 + warp * per, s1 = min(s0 + per, last);
             int h = -1;
             if (s0 < s1)
-                h = warp_edge_chunk<SPL, kRrtcChunk, false>(t, R, E, wc, cs, lane, a, b, s_dir, s0, s1, nstates,
-                                                            nullptr);
+                h = warp_edge_chunk<SPL, kRrtcChunk, false>(t, R, E, wc, cs, lane, a, b, s_dir, s0, s1, nstates);
             if (h >= 0 && lane == 0) *s_flag = 1;
             __syncthreads();
             const bool any = *s_flag != 0;
