@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "gbmp_groups.h"
 #include "gbmp_internal.h"
 #include "gbmp_order.h"
 
@@ -326,53 +327,12 @@ static gbmp_status pack_tables(gbmp_robot_s *r, int piece, void **block, DevRobo
     r->h_jl = jl;
     r->h_axn = axn;
     r->h_axr = axr;
-    // Sphere groups and their bounding spheres.  With piece == 0 a group is the spheres of
-    // one link.  Otherwise each link's spheres, ordered along the longest extent of their
-    // centres, are cut into ceil(n / M) pieces of consecutive spheres, M the smallest
-    // piece size from `piece` up that keeps the robot within min(kMaxGroups, 3 L) groups
-    // (3 L: the chunk kernels keep K x G group centres where K x L pose rows were); if none
-    // does, one group per link.  Groups come in link order.
-    std::vector<int> glink, sgrp(S ? S : 1, 0);
-    {
-        std::vector<std::vector<int>> by_link(L);
-        for (int k = 0; k < S; ++k) by_link[r->slink[k]].push_back(k);
-        int most = 1;
-        for (int l = 0; l < L; ++l) most = std::max(most, (int)by_link[l].size());
-        auto count = [&](int m) {
-            int g = 0;
-            for (int l = 0; l < L; ++l) g += ((int)by_link[l].size() + m - 1) / m;
-            return g;
-        };
-        int M = most;
-        if (piece > 0) {
-            const int gmax = std::min(kMaxGroups, 3 * L);
-            M = std::min(piece, most);
-            while (M < most && count(M) > gmax) ++M;
-        }
-        for (int l = 0; l < L; ++l) {
-            std::vector<int> &ks = by_link[l];
-            const int nl = (int)ks.size();
-            if (nl == 0) continue;
-            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-            for (int k : ks)
-                for (int a = 0; a < 3; ++a) {
-                    lo[a] = std::min(lo[a], (double)r->sph_pos[3 * k + a]);
-                    hi[a] = std::max(hi[a], (double)r->sph_pos[3 * k + a]);
-                }
-            int ax = 0;
-            for (int a = 1; a < 3; ++a)
-                if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
-            std::stable_sort(ks.begin(), ks.end(),
-                             [&](int x, int y) { return r->sph_pos[3 * x + ax] < r->sph_pos[3 * y + ax]; });
-            const int pieces = (nl + M - 1) / M;
-            for (int q = 0; q < pieces; ++q) {
-                const int g = (int)glink.size();
-                glink.push_back(l);
-                for (int i = (int)((long long)q * nl / pieces); i < (int)((long long)(q + 1) * nl / pieces); ++i)
-                    sgrp[ks[i]] = g;
-            }
-        }
-    }
+    // Sphere groups (gbmp_groups.h) and their bounding spheres.  Pieces of links stay
+    // within min(kMaxGroups, 3 L) groups: the chunk kernels keep K x G group centres where
+    // the chunk's K x L pose rows were.
+    std::vector<int> glink, sgrp;
+    split_sphere_groups(L, S, r->slink.data(), r->sph_pos.data(), piece, piece > 0 ? std::min(kMaxGroups, 3 * L) : 0,
+                        glink, sgrp);
     const int G = (int)glink.size();
     std::vector<float> grp(4 * (G ? G : 1), 0.f);
     for (int g = 0; g < G; ++g) {

@@ -163,6 +163,20 @@ def test_edge_state_orders_cover_every_state_once(tmp_path):
     assert "order ok" in out.stdout
 
 
+def test_sphere_groups_split_links_within_the_group_limit(tmp_path):
+    """The robots' sphere groups (csrc/gbmp_groups.h, compiled here for the host): one
+    group per link for the per-state kernels; pieces of links for the chunk kernels, each
+    within one link, at most M spheres (M the smallest size from the piece up within the
+    group limit), following the link's longest extent, in link order."""
+    exe = tmp_path / "groups_check"
+    src = os.path.join(ROOT, "tests", "cpp", "groups_check.cpp")
+    inc = os.path.join(ROOT, "isaac_sim_ros2_humble_gb300", "csrc")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", inc, src, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "groups ok" in out.stdout
+
+
 def test_batch_autotuner_policy_with_a_fake_timer(tmp_path):
     """The batched planner's launch-shape tuner (csrc/gbmp_autotune.h), driven by a fake
     timer: each allowed candidate tried twice in order, the least time of each kept, the
