@@ -152,28 +152,7 @@ __global__ void k_rrtc_batch_trace(const BatchProblem *__restrict__ probs, int n
     if (p >= n) return;
     if (threadIdx.x == 0) {
         const RrtcDev &P = probs[p].P;
-        // reuse the single-problem trace (one thread)
-        const int L = probs[p].R.L;
-        if (P.state[0] != kStSolved) {
-            *P.path_len = 0;
-        } else {
-            const int tr = P.state[2], a = P.state[3], b = P.state[4];
-            const int na = tr == 0 ? a : b, nb = tr == 0 ? b : a;
-            int len0 = 0, len1 = 0;
-            for (int i = na; i >= 0 && len0 <= P.cap; i = (P.parent[0][i] == i ? -1 : P.parent[0][i])) ++len0;
-            for (int i = nb; i >= 0 && len1 <= P.cap; i = (P.parent[1][i] == i ? -1 : P.parent[1][i])) ++len1;
-            if (len0 + len1 > P.path_cap || len0 > P.cap || len1 > P.cap) {
-                *P.path_len = -(len0 + len1);
-            } else {
-                int k = len0 - 1;
-                for (int i = na; i >= 0; i = (P.parent[0][i] == i ? -1 : P.parent[0][i]), --k)
-                    for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[0][(long long)i * P.stride + j];
-                k = len0;
-                for (int i = nb; i >= 0; i = (P.parent[1][i] == i ? -1 : P.parent[1][i]), ++k)
-                    for (int j = 0; j < L; ++j) P.path[k * L + j] = P.nodes[1][(long long)i * P.stride + j];
-                *P.path_len = len0 + len1;
-            }
-        }
+        rrtc_trace_path(P, probs[p].R.L);   // the single-problem trace (one thread)
         int *o = summary + 8 * p;
         o[0] = P.state[0];
         o[1] = *P.path_len;
