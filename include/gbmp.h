@@ -397,6 +397,10 @@ typedef struct gbmp_rrtc_result {
     double kernel_ms;       /* device time of the planning launch                           */
 } gbmp_rrtc_result;
 
+/* A planner owns its trees (two of max_nodes nodes), a pinned path buffer of path_cap
+ * states and a pinned input / outcome block; a solve resets only the tree slots the
+ * previous solve wrote, in one launch, and reads its outcome after one synchronisation.
+ * Solves on one planner must not overlap (one at a time, from any thread). */
 GBMP_API gbmp_status gbmp_planner_create(gbmp_robot robot, int32_t max_nodes, int32_t path_cap,
                                          gbmp_planner *out);
 GBMP_API gbmp_status gbmp_planner_destroy(gbmp_planner planner);
