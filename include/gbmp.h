@@ -117,6 +117,12 @@ GBMP_API gbmp_status gbmp_robot_joints(gbmp_robot robot, uint8_t *h_active, floa
  * limit), GBMP_OK otherwise.  Synchronous (reads one word).  No reference counterpart
  * (the reference exits the process on a CUDA error, util.h:12-19). */
 GBMP_API gbmp_status gbmp_robot_device_status(gbmp_robot robot, int32_t *status);
+/* Test control of the bounded staging wait of one robot handle's kernels: `polls` polls
+ * before a block gives up (0: at once, so the give-up path runs and reports through
+ * gbmp_robot_device_status; -1: the default, far beyond any copy).  A block that gives up
+ * still waits, again bounded, for its copies in flight before it leaves.  The fault word
+ * stays set for the handle's life.  No reference counterpart. */
+GBMP_API gbmp_status gbmp_robot_set_stage_wait(gbmp_robot robot, int32_t polls);
 /* Select the kernel family used by later calls: 0 table-driven, 1 generated. */
 GBMP_API gbmp_status gbmp_robot_use_codegen(gbmp_robot robot, int32_t enable);
 /* The generated kernels of a robot created with GBMP_ROBOT_CODEGEN (the reference writes

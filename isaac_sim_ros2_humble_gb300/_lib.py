@@ -119,6 +119,7 @@ SIGNATURES = {
     "gbmp_check_batch_run": [_vp, C.POINTER(CheckRequest), _i32, _i32, _vp],
     "gbmp_check_batch_destroy": [_vp],
     "gbmp_robot_set_edge_form": [_vp, _i32],
+    "gbmp_robot_set_stage_wait": [_vp, _i32],
     "gbmp_check_edges": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
     "gbmp_check_edges_noalloc": [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp],
     "gbmp_nearest": [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp],

@@ -63,6 +63,17 @@ class Robot:
         states per chunk (tuning and tests; results do not depend on it)."""
         check(_lib.load().gbmp_robot_set_edge_form(self.handle, int(form)))
 
+    def set_stage_wait(self, polls: int):
+        """Polls of the kernels' bounded staging wait before a block gives up (0: at once,
+        so the give-up path runs; -1: the default).  Test control."""
+        check(_lib.load().gbmp_robot_set_stage_wait(self.handle, int(polls)))
+
+    def device_status(self) -> int:
+        """GBMP_ERR_TIMEOUT once a kernel working for this handle gave up a bounded wait."""
+        st = C.c_int32(-1)
+        check(_lib.load().gbmp_robot_device_status(self.handle, C.byref(st)))
+        return st.value
+
     def use_codegen(self, enable: bool):
         check(_lib.load().gbmp_robot_use_codegen(self.handle, int(enable)))
 

@@ -425,6 +425,7 @@ static gbmp_status pack_tables(gbmp_robot_s *r, int piece, void **block, DevRobo
     D.stage = b;
     D.stage_bytes = (unsigned)staged_bytes;
     D.fault = (unsigned *)(b + o_fault);
+    D.stage_polls = kStageWaitPolls;
     if (staged_bytes != smem_tables_bytes(D, 0)) {   // the layouts must agree byte for byte
         set_error("internal: staged table block of %zu bytes, shared-memory layout of %zu", staged_bytes,
                   smem_tables_bytes(D, 0));
@@ -796,6 +797,13 @@ gbmp_status gbmp_check_states_fk(gbmp_robot r, gbmp_env env, const float *d_q, i
 gbmp_status gbmp_check_states(gbmp_robot r, gbmp_env env, const float *d_q, int64_t n, int32_t mode,
                               uint8_t *d_verdict, float *d_costs, float *d_total, void *stream) {
     return gbmp_check_states_fk(r, env, d_q, n, mode, d_verdict, d_costs, d_total, nullptr, nullptr, stream);
+}
+
+gbmp_status gbmp_robot_set_stage_wait(gbmp_robot r, int32_t polls) {
+    GBMP_CHECK_ARG(r, "robot is NULL");
+    GBMP_CHECK_ARG(polls >= -1, "polls %d < -1", polls);
+    r->dev.stage_polls = r->dev_chunk.stage_polls = polls < 0 ? kStageWaitPolls : polls;
+    return GBMP_OK;
 }
 
 gbmp_status gbmp_robot_set_edge_form(gbmp_robot r, int32_t form) {

@@ -67,10 +67,12 @@ struct DevRobot {
     // The staged tables (jl .. gsl above) as one block laid out exactly as carve_tables
     // lays them out in shared memory: `stage_bytes` bytes at `stage` (16-byte aligned), so
     // that one bulk copy stages them.  `fault`: device word a kernel sets (bit 0) when a
-    // bounded device-side wait gave up.
+    // bounded device-side wait gave up.  `stage_polls`: polls of the staging wait before it
+    // gives up (kStageWaitPolls; a test sets 0 to see the give-up path report).
     const void *stage;
     unsigned stage_bytes;
     unsigned *fault;
+    int stage_polls;
 };
 
 // Flop weights of the executed tests (multiply/add/compare = 1, FMA = 2).
@@ -229,23 +231,34 @@ __device__ inline bool stage_tables(const DevRobot &R, const DevEnv &E, const Sm
                          : "memory");
     }
     __syncthreads();   // the mbarrier is initialised before anyone polls it
-    unsigned done = 0;
-    for (int it = 0; it < kStageWaitPolls; ++it) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar)
-            : "memory");
-        if (done) break;
-        if (it > 8) __nanosleep(100);
-    }
-    if (!done) s_fail = 1;
+    auto poll = [&](int limit) {
+        unsigned done = 0;
+        for (int it = 0; it < limit; ++it) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done)
+                : "r"(bar)
+                : "memory");
+            if (done) break;
+            if (it > 8) __nanosleep(100);
+        }
+        return done != 0;
+    };
+    if (!poll(R.stage_polls)) s_fail = 1;
     __syncthreads();
     const bool ok = s_fail == 0;
-    if (threadIdx.x == 0) {
-        if (ok) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
-        else if (R.fault) atomicOr(R.fault, 1u);
+    if (!ok) {
+        // gave up: the results of this launch are not valid, but the block does not leave
+        // while its copies may still write into its shared memory (a second wait, also
+        // bounded), and the fault word tells the host
+        if (threadIdx.x == 0) {
+            poll(kStageWaitPolls);
+            if (R.fault) atomicOr(R.fault, 1u);
+        }
+        __syncthreads();
+        return false;
     }
+    if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
     return ok;
 }
 

@@ -432,6 +432,30 @@ def test_edge_forms_agree_for_large_sphere_groups(dof, n_spheres):
     _edge_parity(m, qf[:192], qt[:192], 0.02, 1, ok[:192], fh[:192], ln[:192], ns[:192])
 
 
+def test_staging_wait_that_gives_up_is_reported_and_the_context_stays_usable(plain):
+    """The bounded staging wait's give-up path, forced on a fresh handle (a wait of zero
+    polls; no fault, no hang): the launch returns, the handle reports GBMP_ERR_TIMEOUT
+    (and keeps reporting it), and another handle's next check on the same context gives
+    the oracle's verdicts."""
+    robot, env, q, m, R0, E = plain
+    R = api.Robot(robot)
+    assert R.device_status() == _lib.OK
+    R.set_stage_wait(0)
+    v = torch.zeros(256, dtype=torch.uint8, device="cuda")
+    api.check_states(R, E, dev(q[:256]), verdict=v)
+    torch.cuda.synchronize()
+    assert R.device_status() == 6   # GBMP_ERR_TIMEOUT
+    R.set_stage_wait(-1)
+    assert R.device_status() == 6   # sticky for the handle's life
+    with pytest.raises(_lib.GbmpError):
+        R.set_stage_wait(-2)
+    v2 = torch.zeros(256, dtype=torch.uint8, device="cuda")
+    api.check_states(R0, E, dev(q[:256]), verdict=v2)
+    torch.cuda.synchronize()
+    _verdict_parity(m, q[:256], v2.cpu().numpy().astype(bool))
+    assert R0.device_status() == _lib.OK
+
+
 def test_device_status_is_clean_after_every_kernel_family(plain, edge):
     """Every kernel stages its tables with bulk asynchronous copies and a bounded wait;
     none of the launches above gave up that wait (gbmp_robot_device_status)."""
